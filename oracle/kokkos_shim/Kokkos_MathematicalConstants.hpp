@@ -1,0 +1,2 @@
+// Kokkos-API shim (test infrastructure only).
+#include <Kokkos_Core.hpp>

@@ -1,0 +1,63 @@
+"""Generate the golden fixtures of tests/golden from the reference itself.
+
+Each fixture is the reference's OWN solver code (the upstream sources compiled
+unmodified against the Kokkos-API shim, oracle/_ref/ref_run, built by
+oracle/build.sh) run on a seeded initial state from euler_kokkos_gb300.problems.
+Stored per case (compressed .npz): the .ini text, the injected initial state
+U0, the final state U, the dt sequence and the final time.
+
+Run from the repository root (needs the reference sources, so only where
+they are present):  python tests/golden/make_golden.py
+"""
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import eko  # noqa: E402
+from euler_kokkos_gb300 import problems as P  # noqa: E402
+
+CASES = {
+    # name: (builder, nsteps)
+    "implode2d_32": (lambda: P.implode_2d(n=32, nsteps=20), 20),
+    "implode2d_mixedbc_mc": (lambda: P.implode_2d(n=24, ny=20, nsteps=12, bc=(2, 2, 3, 3),
+                                                   slope_type=2.0), 12),
+    "kh2d_16": (lambda: P.kelvin_helmholtz_2d(n=16, nsteps=10), 10),
+    "hydro2d_random_reflect": (lambda: P.smooth_random(dim=2, nx=20, ny=14, seed=3, bc=(1, 1, 1, 1, 1, 1),
+                                                        slope_type=1.0, nsteps=10), 10),
+    "blast3d_12": (lambda: P.blast_3d(n=12, nsteps=8), 8),
+    "hydro3d_random_mixedbc": (lambda: P.smooth_random(dim=3, nx=10, ny=8, nz=6, seed=4,
+                                                        bc=(1, 1, 3, 3, 2, 2), slope_type=2.0,
+                                                        nsteps=6), 6),
+    "ot3d_12": (lambda: P.orszag_tang_3d(n=12, nsteps=6), 6),
+    "mhd3d_random_periodic": (lambda: P.smooth_random(dim=3, mhd=True, nx=8, ny=10, nz=7, seed=5,
+                                                       slope_type=2.0, nsteps=4), 4),
+    "mhd3d_random_reflect_minmod": (lambda: P.smooth_random(dim=3, mhd=True, nx=8, ny=8, nz=8, seed=6,
+                                                             bc=(1, 1, 1, 1, 1, 1), slope_type=1.0,
+                                                             nsteps=4), 4),
+    "mhd3d_random_outflow": (lambda: P.smooth_random(dim=3, mhd=True, nx=9, ny=8, nz=8, seed=7,
+                                                      bc=(2, 2, 2, 2, 2, 2), slope_type=2.0,
+                                                      nsteps=4), 4),
+    "mhdblast3d_10_nan": (lambda: P.mhd_blast_3d(n=10, nsteps=3), 3),
+}
+
+
+def main():
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    work = os.path.join(ROOT, "_work", "golden_tmp")
+    for name, (build, nsteps) in CASES.items():
+        ini, U0 = build()
+        res = eko.run_reference(ini, U0, nsteps, os.path.join(work, name))
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), ini=np.array(ini), U0=U0,
+                            U=res["U"], dts=res["dts"], t=np.array(res["t"]),
+                            iteration=np.array(res["iteration"]))
+        print(name, U0.shape, "steps", len(res["dts"]), "nan", int(np.isnan(res["U"]).sum()))
+
+
+if __name__ == "__main__":
+    main()
