@@ -1,0 +1,289 @@
+"""GB300-native unsplit MUSCL-Hancock step (hydro 2D/3D, CT-MHD 3D).
+
+Python host layer over the C ABI of ``libek_gb300.so`` (include/ek_gb300.h).
+It mirrors the reference's solver interface -- ``SolverFactory.create`` by
+solver name, and a solver object with ``compute_dt``, ``next_iteration``,
+``finished``, ``m_t``/``m_dt``/``m_iteration`` (shared/SolverBase.h:53-259)
+-- so a driver loop reads like the reference's ``src/main.cpp:126-131``:
+
+    params = params_from_ini(open("case.ini").read())
+    solver = SolverFactory.create(params.solver_name, params)
+    solver.set_state(U0)
+    while not solver.finished():
+        solver.next_iteration()
+
+There is no CPU fallback: every call goes to the CUDA library, and creating
+a solver without a GPU raises ``EkError(EK_ERR_NO_DEVICE)``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = [
+    "EkError",
+    "Params",
+    "Solver",
+    "SolverFactory",
+    "params_from_ini",
+    "load_library",
+    "library_path",
+    "EK_PREC_FP64",
+    "EK_PREC_MIXED",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+EK_OK, EK_ERR_INVALID, EK_ERR_UNSUPPORTED, EK_ERR_CUDA = 0, 1, 2, 3
+EK_ERR_NO_MEMORY, EK_ERR_NONFINITE, EK_ERR_PARSE, EK_ERR_NO_DEVICE = 4, 5, 6, 7
+EK_LAYOUT_LEFT, EK_LAYOUT_RIGHT = 0, 1
+EK_PREC_FP64, EK_PREC_MIXED = 0, 1
+
+
+class Params(ctypes.Structure):
+    """ctypes mirror of ``ek_params`` (include/ek_gb300.h)."""
+
+    _fields_ = [
+        ("dim", ctypes.c_int), ("mhd", ctypes.c_int),
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("ghost_width", ctypes.c_int), ("nbvar", ctypes.c_int),
+        ("isize", ctypes.c_int), ("jsize", ctypes.c_int), ("ksize", ctypes.c_int),
+        ("xmin", ctypes.c_double), ("xmax", ctypes.c_double), ("ymin", ctypes.c_double),
+        ("ymax", ctypes.c_double), ("zmin", ctypes.c_double), ("zmax", ctypes.c_double),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+        ("bc", ctypes.c_int * 6),
+        ("gamma0", ctypes.c_double), ("gamma6", ctypes.c_double), ("cfl", ctypes.c_double),
+        ("slope_type", ctypes.c_double), ("smallr", ctypes.c_double), ("smallc", ctypes.c_double),
+        ("smallp", ctypes.c_double), ("smallpp", ctypes.c_double), ("cIso", ctypes.c_double),
+        ("Omega0", ctypes.c_double),
+        ("riemann", ctypes.c_int), ("implementation_version", ctypes.c_int),
+        ("nStepmax", ctypes.c_int), ("tEnd", ctypes.c_double), ("tCurrent", ctypes.c_double),
+        ("nOutput", ctypes.c_int), ("nlog", ctypes.c_int),
+        ("precision", ctypes.c_int), ("exact_fp", ctypes.c_int), ("kchunk", ctypes.c_int),
+        ("solver_name_", ctypes.c_char * 32), ("problem_", ctypes.c_char * 32),
+    ]
+
+    @property
+    def solver_name(self) -> str:
+        return self.solver_name_.decode()
+
+    @property
+    def problem(self) -> str:
+        return self.problem_.decode()
+
+    @property
+    def shape(self):
+        """numpy shape of a full state: (nbvar, ksize, jsize, isize)."""
+        return (self.nbvar, self.ksize if self.dim == 3 else 1, self.jsize, self.isize)
+
+    def copy(self, **changes) -> "Params":
+        p = Params()
+        ctypes.memmove(ctypes.byref(p), ctypes.byref(self), ctypes.sizeof(Params))
+        for k, v in changes.items():
+            setattr(p, k, v)
+        return p
+
+
+class EkError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s (status %d)" % (msg, status))
+        self.status = status
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return os.environ.get("EK_GB300_LIB", os.path.join(_HERE, "_build", "libek_gb300.so"))
+
+
+def load_library():
+    """Load libek_gb300.so; it must have been built (python -m euler_kokkos_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise EkError(EK_ERR_UNSUPPORTED, "CUDA library not built: %s (run python -m euler_kokkos_gb300.build)" % path)
+    L = ctypes.CDLL(path)
+    c_p = ctypes.c_void_p
+    sig = {
+        "ek_abi_version": (ctypes.c_int, []),
+        "ek_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+        "ek_last_error": (ctypes.c_char_p, []),
+        "ek_params_from_ini": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(Params)]),
+        "ek_solver_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.POINTER(c_p)]),
+        "ek_solver_destroy": (ctypes.c_int, [c_p]),
+        "ek_solver_set_state": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
+        "ek_solver_get_state": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
+        "ek_solver_compute_dt": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_double)]),
+        "ek_solver_next_iteration": (ctypes.c_int, [c_p]),
+        "ek_solver_run": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+        "ek_solver_finished": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_int)]),
+        "ek_solver_time": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]),
+        "ek_solver_dt_history": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
+        "ek_solver_totals": (ctypes.c_int, [c_p, c_p]),
+        "ek_solver_device_state": (ctypes.c_int, [c_p, ctypes.POINTER(c_p), ctypes.POINTER(ctypes.c_size_t)]),
+        "ek_solver_synchronize": (ctypes.c_int, [c_p]),
+        "ek_solver_launch_count": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_longlong)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(status: int, what: str, allow=()):
+    if status != EK_OK and status not in allow:
+        L = load_library()
+        raise EkError(status, "%s: %s (%s)" % (what, L.ek_status_string(status).decode(),
+                                               L.ek_last_error().decode()))
+    return status
+
+
+def params_from_ini(text: str, **overrides) -> Params:
+    """ConfigMap + HydroParams semantics (C++ front end of the library)."""
+    L = load_library()
+    p = Params()
+    b = text.encode()
+    _check(L.ek_params_from_ini(b, len(b), ctypes.byref(p)), "params_from_ini")
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p
+
+
+class Solver:
+    """One GPU solver: the SolverBase interface over the C ABI."""
+
+    def __init__(self, params: Params):
+        L = load_library()
+        self._L = L
+        self.params = params.copy()
+        h = ctypes.c_void_p()
+        _check(L.ek_solver_create(ctypes.byref(self.params), ctypes.byref(h)), "ek_solver_create")
+        self._h = h
+        self.last_status = EK_OK
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ek_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- state -------------------------------------------------------------
+    def set_state(self, U: np.ndarray, layout: int = EK_LAYOUT_LEFT):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.size != int(np.prod(self.params.shape)):
+            raise ValueError("state has %d values, expected shape %s" % (U.size, self.params.shape))
+        _check(self._L.ek_solver_set_state(self._h, U.ctypes.data, layout), "set_state")
+
+    def get_state(self, layout: int = EK_LAYOUT_LEFT) -> np.ndarray:
+        U = np.empty(self.params.shape, dtype=np.float64)
+        _check(self._L.ek_solver_get_state(self._h, U.ctypes.data, layout), "get_state")
+        return U
+
+    # -- SolverBase --------------------------------------------------------
+    def compute_dt(self) -> float:
+        d = ctypes.c_double()
+        _check(self._L.ek_solver_compute_dt(self._h, ctypes.byref(d)), "compute_dt")
+        return d.value
+
+    def next_iteration(self, allow_nonfinite: bool = False):
+        allow = (EK_ERR_NONFINITE,) if allow_nonfinite else ()
+        self.last_status = _check(self._L.ek_solver_next_iteration(self._h), "next_iteration", allow)
+
+    def run(self, nsteps: int, allow_nonfinite: bool = False) -> int:
+        done = ctypes.c_int()
+        allow = (EK_ERR_NONFINITE,) if allow_nonfinite else ()
+        self.last_status = _check(self._L.ek_solver_run(self._h, nsteps, ctypes.byref(done)), "run", allow)
+        return done.value
+
+    def finished(self) -> bool:
+        f = ctypes.c_int()
+        _check(self._L.ek_solver_finished(self._h, ctypes.byref(f)), "finished")
+        return bool(f.value)
+
+    def _time(self):
+        t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        _check(self._L.ek_solver_time(self._h, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(it)), "time")
+        return t.value, dt.value, it.value
+
+    @property
+    def m_t(self) -> float:
+        return self._time()[0]
+
+    @property
+    def m_dt(self) -> float:
+        return self._time()[1]
+
+    @property
+    def m_iteration(self) -> int:
+        return self._time()[2]
+
+    def dt_history(self) -> np.ndarray:
+        n = self.m_iteration
+        out = np.empty(n, dtype=np.float64)
+        if n:
+            _check(self._L.ek_solver_dt_history(self._h, out.ctypes.data, n), "dt_history")
+        return out
+
+    def totals(self) -> np.ndarray:
+        out = np.empty(3, dtype=np.float64)
+        _check(self._L.ek_solver_totals(self._h, out.ctypes.data), "totals")
+        return out
+
+    def device_state(self):
+        ptr, nbytes = ctypes.c_void_p(), ctypes.c_size_t()
+        _check(self._L.ek_solver_device_state(self._h, ctypes.byref(ptr), ctypes.byref(nbytes)), "device_state")
+        return ptr.value, nbytes.value
+
+    def synchronize(self):
+        _check(self._L.ek_solver_synchronize(self._h), "synchronize")
+
+    def launch_count(self) -> int:
+        n = ctypes.c_longlong()
+        _check(self._L.ek_solver_launch_count(self._h, ctypes.byref(n)), "launch_count")
+        return n.value
+
+
+class SolverFactory:
+    """Name -> solver registry, as the reference's SolverFactory
+    (shared/SolverFactory.h:72-116, SolverFactory.cpp:18-22)."""
+
+    _registry = {
+        "Hydro_Muscl_2D": Solver,
+        "Hydro_Muscl_3D": Solver,
+        "MHD_Muscl_3D": Solver,
+    }
+
+    @classmethod
+    def register(cls, name: str, creator):
+        cls._registry[name] = creator
+
+    @classmethod
+    def names(cls):
+        return sorted(cls._registry)
+
+    @classmethod
+    def create(cls, name: str, params: Params) -> Solver:
+        if name not in cls._registry:
+            raise EkError(EK_ERR_INVALID, "%s: is not recognized as a valid application name key. "
+                          "Valid solver names are: %s" % (name, ", ".join(cls.names())))
+        return cls._registry[name](params)

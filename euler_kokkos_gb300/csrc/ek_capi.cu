@@ -1,0 +1,628 @@
+// C ABI implementation: solver handle, device buffers, step sequencing.
+//
+// Host-side equivalent of SolverBase + SolverHydroMuscl/SolverMHDMuscl
+// (SolverBase.cpp:124-195, SolverHydroMuscl.h:164-307, 635-700,
+// SolverMHDMuscl.h:384-397, 741-801) with the kernels of ek_kernels.cu.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ek_gb300.h"
+#include "ek_internal.h"
+#include "ek_launch.h"
+
+namespace ek_internal
+{
+static thread_local std::string g_last_error;
+
+ek_status
+fail(ek_status s, const std::string & msg)
+{
+  g_last_error = msg;
+  return s;
+}
+} // namespace ek_internal
+
+using ek_internal::fail;
+using KParams = ekc::KParams;
+using DevClock = ekc::DevClock;
+
+struct ek_solver
+{
+  ek_params     p;
+  KParams       kp;
+  int           prec;
+  bool          exact;
+  void *        U[2] = { nullptr, nullptr }; // ping-pong device states
+  size_t        state_bytes = 0;
+  void *        work = nullptr; // MHD intermediates (if any)
+  size_t        work_bytes = 0;
+  DevClock *    clk = nullptr;  // device
+  double *      dtlog = nullptr;
+  int           dtcap = 0;
+  double *      scratch3 = nullptr; // device totals
+  cudaStream_t  stream = nullptr;
+  int           device = 0;
+  // host mirror of SolverBase state
+  double        t = 0.0, dt = 0.0;
+  int           iteration = 0;
+  bool          has_state = false;
+  long long     launches = 0;
+  std::vector<double> hbuf; // host staging (FP64, LayoutLeft)
+};
+
+static ek_status
+cuda_fail(cudaError_t e, const char * what)
+{
+  return fail(e == cudaErrorMemoryAllocation ? EK_ERR_NO_MEMORY : EK_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define EK_CUDA(call, what)                                                                         \
+  do                                                                                                \
+  {                                                                                                 \
+    cudaError_t e__ = (call);                                                                       \
+    if (e__ != cudaSuccess)                                                                         \
+      return cuda_fail(e__, what);                                                                  \
+  } while (0)
+
+extern "C" int
+ek_abi_version(void)
+{
+  return EK_ABI_VERSION;
+}
+
+extern "C" const char *
+ek_status_string(ek_status s)
+{
+  switch (s)
+  {
+    case EK_OK: return "ok";
+    case EK_ERR_INVALID: return "invalid argument";
+    case EK_ERR_UNSUPPORTED: return "unsupported configuration";
+    case EK_ERR_CUDA: return "CUDA error";
+    case EK_ERR_NO_MEMORY: return "out of memory";
+    case EK_ERR_NONFINITE: return "non-finite time step";
+    case EK_ERR_PARSE: return "ini parse error";
+    case EK_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+extern "C" const char *
+ek_last_error(void)
+{
+  return ek_internal::g_last_error.c_str();
+}
+
+static size_t
+state_bytes_of(const ek_params & p, const KParams & kp)
+{
+  if (p.precision == EK_PREC_FP64)
+    return sizeof(double) * (size_t)kp.vstride * p.nbvar;
+  if (!p.mhd)
+    return sizeof(float) * (size_t)kp.vstride * p.nbvar;
+  return ekc::mixed_bfield_offset(kp.vstride) + sizeof(double) * 3 * (size_t)kp.vstride;
+}
+
+extern "C" ek_status
+ek_solver_create(const ek_params * params, ek_solver ** out)
+{
+  if (!params || !out)
+    return fail(EK_ERR_INVALID, "ek_solver_create: null argument");
+  *out = nullptr;
+  const ek_params & p = *params;
+  if (p.dim != 2 && p.dim != 3)
+    return fail(EK_ERR_INVALID, "dim must be 2 or 3");
+  if (p.nx < 1 || p.ny < 1 || (p.dim == 3 && p.nz < 1))
+    return fail(EK_ERR_INVALID, "grid sizes must be positive");
+  const int gw = p.mhd ? 3 : 2;
+  if (p.ghost_width != gw || p.nbvar != (p.mhd ? 8 : (p.dim == 2 ? 4 : 5)))
+    return fail(EK_ERR_INVALID, "ghost_width/nbvar inconsistent with the solver kind");
+  if (p.isize != p.nx + 2 * gw || p.jsize != p.ny + 2 * gw || (p.dim == 3 && p.ksize != p.nz + 2 * gw))
+    return fail(EK_ERR_INVALID, "isize/jsize/ksize inconsistent with nx/ny/nz");
+  if (p.nx < gw || p.ny < gw || (p.dim == 3 && p.nz < gw))
+    return fail(EK_ERR_INVALID, "each dimension needs at least ghost_width interior cells");
+  for (int f = 0; f < 2 * p.dim; ++f)
+    if (p.bc[f] < 1 || p.bc[f] > 3)
+      return fail(EK_ERR_INVALID, "boundary types must be 1 (reflect), 2 (outflow) or 3 (periodic)");
+  if (p.mhd && p.dim == 2)
+    return fail(EK_ERR_UNSUPPORTED, "MHD_Muscl_2D is not implemented by this library");
+  if (!p.mhd && p.riemann != 3)
+    return fail(EK_ERR_UNSUPPORTED, "hydro: only riemann=hllc is implemented");
+  if (p.mhd && p.riemann != 4)
+    return fail(EK_ERR_UNSUPPORTED, "MHD: only riemann=hlld is implemented");
+  if (p.slope_type != 1.0 && p.slope_type != 2.0)
+    return fail(EK_ERR_UNSUPPORTED, "slope_type must be 1 (minmod) or 2 (MC)");
+  if (p.implementation_version != 0)
+    return fail(EK_ERR_UNSUPPORTED, "only implementationVersion=0 is implemented");
+  if (p.cIso > 0 || p.Omega0 > 0)
+    return fail(EK_ERR_UNSUPPORTED, "isothermal and shearing-box terms are not implemented");
+  if (p.exact_fp && p.precision != EK_PREC_FP64)
+    return fail(EK_ERR_INVALID, "exact_fp requires precision fp64");
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(EK_ERR_NO_DEVICE, "no CUDA device available");
+
+  ek_solver * s = new ek_solver();
+  s->p = p;
+  s->prec = p.precision;
+  s->exact = p.exact_fp != 0;
+  cudaGetDevice(&s->device);
+  KParams & k = s->kp;
+  std::memset(&k, 0, sizeof k);
+  k.nx = p.nx;
+  k.ny = p.ny;
+  k.nz = p.dim == 3 ? p.nz : 1;
+  k.gw = gw;
+  k.isize = p.isize;
+  k.jsize = p.jsize;
+  k.ksize = p.dim == 3 ? p.ksize : 1;
+  k.mhd = p.mhd;
+  k.plane = (long long)k.isize * k.jsize;
+  k.vstride = k.plane * k.ksize;
+  for (int f = 0; f < 6; ++f)
+    k.bc[f] = p.bc[f];
+  k.dx = p.dx;
+  k.dy = p.dy;
+  k.dz = p.dz;
+  k.gamma0 = p.gamma0;
+  k.smallr = p.smallr;
+  k.smallc = p.smallc;
+  k.smallp = p.smallp;
+  k.slope_type = p.slope_type;
+  k.cfl = p.cfl;
+  k.tEnd = p.tEnd;
+  k.cIso = p.cIso;
+  k.riemann = p.riemann;
+  k.kchunk = p.kchunk > 0 ? p.kchunk : (k.nz <= 64 ? k.nz : 64);
+
+  s->state_bytes = state_bytes_of(p, k);
+  cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&s->U[0], s->state_bytes);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&s->U[1], s->state_bytes);
+  if (e == cudaSuccess)
+    e = cudaMalloc((void **)&s->clk, sizeof(DevClock));
+  s->dtcap = p.nStepmax > 0 ? (p.nStepmax < (1 << 22) ? p.nStepmax + 1 : (1 << 22)) : 1;
+  if (e == cudaSuccess)
+    e = cudaMalloc((void **)&s->dtlog, sizeof(double) * s->dtcap);
+  if (e == cudaSuccess)
+    e = cudaMalloc((void **)&s->scratch3, 3 * sizeof(double));
+  if (e == cudaSuccess && p.mhd)
+  {
+    s->work_bytes = s->exact ? ek_exact::mhd_work_bytes(s->prec, k) : ek_fast::mhd_work_bytes(s->prec, k);
+    if (s->work_bytes)
+      e = cudaMalloc(&s->work, s->work_bytes);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemset(s->U[0], 0, s->state_bytes);
+  if (e == cudaSuccess)
+    e = cudaMemset(s->U[1], 0, s->state_bytes);
+  if (e != cudaSuccess)
+  {
+    ek_status st = cuda_fail(e, "ek_solver_create");
+    ek_solver_destroy(s);
+    return st;
+  }
+  *out = s;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_destroy(ek_solver * s)
+{
+  if (!s)
+    return EK_OK;
+  if (s->stream)
+    cudaStreamSynchronize(s->stream);
+  cudaFree(s->U[0]);
+  cudaFree(s->U[1]);
+  cudaFree(s->work);
+  cudaFree(s->clk);
+  cudaFree(s->dtlog);
+  cudaFree(s->scratch3);
+  if (s->stream)
+    cudaStreamDestroy(s->stream);
+  delete s;
+  return EK_OK;
+}
+
+// host FP64 LayoutLeft/Right <-> device storage
+static void
+to_device_layout(const ek_solver * s, const double * U, int layout, std::vector<double> & dst)
+{
+  const ek_params & p = s->p;
+  const long long   n = s->kp.vstride;
+  dst.resize((size_t)n * p.nbvar);
+  if (layout == EK_LAYOUT_LEFT)
+  {
+    std::memcpy(dst.data(), U, sizeof(double) * dst.size());
+    return;
+  }
+  // LayoutRight: ((i*jsize + j)*ksize + k)*nbvar + var
+  const int is = s->kp.isize, js = s->kp.jsize, ks = s->kp.ksize, nb = p.nbvar;
+  for (int i = 0; i < is; ++i)
+    for (int j = 0; j < js; ++j)
+      for (int k = 0; k < ks; ++k)
+        for (int v = 0; v < nb; ++v)
+          dst[(size_t)v * n + ((size_t)k * js + j) * is + i] = U[(((size_t)i * js + j) * ks + k) * nb + v];
+}
+
+static void
+from_device_layout(const ek_solver * s, const std::vector<double> & src, double * U, int layout)
+{
+  const ek_params & p = s->p;
+  const long long   n = s->kp.vstride;
+  if (layout == EK_LAYOUT_LEFT)
+  {
+    std::memcpy(U, src.data(), sizeof(double) * src.size());
+    return;
+  }
+  const int is = s->kp.isize, js = s->kp.jsize, ks = s->kp.ksize, nb = p.nbvar;
+  for (int i = 0; i < is; ++i)
+    for (int j = 0; j < js; ++j)
+      for (int k = 0; k < ks; ++k)
+        for (int v = 0; v < nb; ++v)
+          U[(((size_t)i * js + j) * ks + k) * nb + v] = src[(size_t)v * n + ((size_t)k * js + j) * is + i];
+}
+
+// FP64 LayoutLeft host buffer <-> device state of the solver's precision
+static ek_status
+upload(ek_solver * s, const std::vector<double> & h, void * dev)
+{
+  const long long n = s->kp.vstride;
+  if (s->prec == EK_PREC_FP64)
+  {
+    EK_CUDA(cudaMemcpyAsync(dev, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s->stream),
+            "upload");
+    return EK_OK;
+  }
+  const int nh = s->p.mhd ? 5 : s->p.nbvar;
+  std::vector<float> f((size_t)n * nh);
+  for (size_t i = 0; i < f.size(); ++i)
+    f[i] = (float)h[i];
+  EK_CUDA(cudaMemcpyAsync(dev, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice, s->stream),
+          "upload");
+  if (s->p.mhd)
+    EK_CUDA(cudaMemcpyAsync(ekc::mixed_bfield(dev, s->kp), h.data() + (size_t)5 * n,
+                            sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->stream),
+            "upload");
+  EK_CUDA(cudaStreamSynchronize(s->stream), "upload");
+  return EK_OK;
+}
+
+static ek_status
+download(ek_solver * s, const void * dev, std::vector<double> & h)
+{
+  const long long n = s->kp.vstride;
+  h.resize((size_t)n * s->p.nbvar);
+  if (s->prec == EK_PREC_FP64)
+  {
+    EK_CUDA(cudaMemcpyAsync(h.data(), dev, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s->stream),
+            "download");
+    EK_CUDA(cudaStreamSynchronize(s->stream), "download");
+    return EK_OK;
+  }
+  const int nh = s->p.mhd ? 5 : s->p.nbvar;
+  std::vector<float> f((size_t)n * nh);
+  EK_CUDA(cudaMemcpyAsync(f.data(), dev, sizeof(float) * f.size(), cudaMemcpyDeviceToHost, s->stream),
+          "download");
+  if (s->p.mhd)
+    EK_CUDA(cudaMemcpyAsync(h.data() + (size_t)5 * n, ekc::mixed_bfield(dev, s->kp),
+                            sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s->stream),
+            "download");
+  EK_CUDA(cudaStreamSynchronize(s->stream), "download");
+  for (size_t i = 0; i < f.size(); ++i)
+    h[i] = (double)f[i];
+  return EK_OK;
+}
+
+static ek_status
+launch_dt(ek_solver * s, const void * U, unsigned long long * key)
+{
+  cudaError_t e;
+  if (s->p.mhd)
+    e = s->exact ? ek_exact::mhd_dt(s->prec, U, s->kp, key, s->stream)
+                 : ek_fast::mhd_dt(s->prec, U, s->kp, key, s->stream);
+  else
+    e = s->exact ? ek_exact::hydro_dt(s->p.dim, s->prec, U, s->kp, key, s->stream)
+                 : ek_fast::hydro_dt(s->p.dim, s->prec, U, s->kp, key, s->stream);
+  if (e == cudaErrorNotSupported)
+    return fail(EK_ERR_UNSUPPORTED, "kernel not available for this configuration");
+  EK_CUDA(e, "dt kernel");
+  s->launches += 1;
+  return EK_OK;
+}
+
+// reset the device clock with t0 and the CFL reduction of the state
+static ek_status
+reset_clock(ek_solver * s, double t0)
+{
+  DevClock h;
+  std::memset(&h, 0, sizeof h);
+  for (int i = 0; i < 3; ++i)
+  {
+    h.key[i] = EK_KEY_LOWEST;
+    h.t[i] = 0.0;
+  }
+  h.t[0] = t0;
+  h.iteration = 0;
+  h.error = 0;
+  h.dtlog = s->dtlog;
+  h.dtcap = s->dtcap;
+  EK_CUDA(cudaMemcpyAsync(s->clk, &h, sizeof h, cudaMemcpyHostToDevice, s->stream), "clock reset");
+  // hydro: slot 0 holds the CFL of the initial state (the constructor's
+  // compute_dt()); MHD recomputes dt inside every step
+  if (!s->p.mhd)
+    return launch_dt(s, s->U[0], &s->clk->key[0]);
+  return EK_OK;
+}
+
+static ek_status
+read_clock(ek_solver * s, DevClock * h)
+{
+  EK_CUDA(cudaMemcpyAsync(h, s->clk, sizeof *h, cudaMemcpyDeviceToHost, s->stream), "clock read");
+  EK_CUDA(cudaStreamSynchronize(s->stream), "clock read");
+  return EK_OK;
+}
+
+static double
+clock_dt(const ek_solver * s, const DevClock & h, int step)
+{
+  const double invDt = ekc::dkey_inv(h.key[step % 3]);
+  double       d = s->p.cfl / invDt;
+  const double tt = h.t[step % 3];
+  if (tt + d > s->p.tEnd)
+    d = s->p.tEnd - tt;
+  return d;
+}
+
+extern "C" ek_status
+ek_solver_set_state(ek_solver * s, const double * U, int layout)
+{
+  if (!s || !U || (layout != EK_LAYOUT_LEFT && layout != EK_LAYOUT_RIGHT))
+    return fail(EK_ERR_INVALID, "ek_solver_set_state: bad argument");
+  EK_CUDA(cudaSetDevice(s->device), "cudaSetDevice");
+  to_device_layout(s, U, layout, s->hbuf);
+  ek_status st = upload(s, s->hbuf, s->U[0]);
+  if (st != EK_OK)
+    return st;
+  // U2 = U (deep_copy), ghosts of both follow the boundary conditions
+  ek_status st2 = EK_OK;
+  EK_CUDA(ek_fast::fill_ghosts(s->prec, s->U[0], s->kp, s->p.mhd ? 8 : s->p.nbvar, s->stream), "ghosts");
+  EK_CUDA(cudaMemcpyAsync(s->U[1], s->U[0], s->state_bytes, cudaMemcpyDeviceToDevice, s->stream), "copy");
+  s->launches += 1;
+  s->t = s->p.tCurrent;
+  s->iteration = 0;
+  st2 = reset_clock(s, s->t);
+  if (st2 != EK_OK)
+    return st2;
+  s->has_state = true;
+  // m_dt after the constructor
+  double dt = 0.0;
+  return ek_solver_compute_dt(s, &dt);
+}
+
+extern "C" ek_status
+ek_solver_compute_dt(ek_solver * s, double * dt)
+{
+  if (!s || !s->has_state)
+    return fail(EK_ERR_INVALID, "ek_solver_compute_dt: no state");
+  DevClock h;
+  if (s->p.mhd)
+  {
+    // dt from the primitive variables of the current (boundary-filled) state
+    unsigned long long * tmp = reinterpret_cast<unsigned long long *>(s->scratch3);
+    unsigned long long   low = EK_KEY_LOWEST, key = 0;
+    EK_CUDA(cudaMemcpyAsync(tmp, &low, sizeof low, cudaMemcpyHostToDevice, s->stream), "dt");
+    ek_status st = launch_dt(s, s->U[s->iteration % 2], tmp);
+    if (st != EK_OK)
+      return st;
+    EK_CUDA(cudaMemcpyAsync(&key, tmp, sizeof key, cudaMemcpyDeviceToHost, s->stream), "dt");
+    EK_CUDA(cudaStreamSynchronize(s->stream), "dt");
+    double d = s->p.cfl / ekc::dkey_inv(key);
+    if (s->t + d > s->p.tEnd)
+      d = s->p.tEnd - s->t;
+    s->dt = d;
+  }
+  else
+  {
+    ek_status st = read_clock(s, &h);
+    if (st != EK_OK)
+      return st;
+    s->dt = clock_dt(s, h, s->iteration);
+  }
+  if (dt)
+    *dt = s->dt;
+  return EK_OK;
+}
+
+static ek_status
+launch_step(ek_solver * s, int step)
+{
+  const void * in = s->U[step % 2];
+  void *       outp = s->U[(step + 1) % 2];
+  cudaError_t  e;
+  if (s->p.mhd)
+    e = s->exact ? ek_exact::mhd_step(s->prec, in, outp, s->work, s->kp, s->clk, step, s->stream)
+                 : ek_fast::mhd_step(s->prec, in, outp, s->work, s->kp, s->clk, step, s->stream);
+  else
+    e = s->exact ? ek_exact::hydro_step(s->p.dim, s->prec, in, outp, s->kp, s->clk, step, s->stream)
+                 : ek_fast::hydro_step(s->p.dim, s->prec, in, outp, s->kp, s->clk, step, s->stream);
+  if (e == cudaErrorNotSupported)
+    return fail(EK_ERR_UNSUPPORTED, "kernel not available for this configuration");
+  EK_CUDA(e, "step kernel");
+  s->launches += s->p.mhd ? 2 : 1;
+  return EK_OK;
+}
+
+static int
+host_finished(const ek_solver * s)
+{
+  return s->t >= (s->p.tEnd - 1e-14) || s->iteration >= s->p.nStepmax;
+}
+
+static ek_status
+sync_from_clock(ek_solver * s)
+{
+  DevClock h;
+  ek_status st = read_clock(s, &h);
+  if (st != EK_OK)
+    return st;
+  s->iteration = h.iteration;
+  s->t = h.t[h.iteration % 3];
+  if (h.iteration > 0 && h.iteration - 1 < s->dtcap)
+  {
+    EK_CUDA(cudaMemcpy(&s->dt, s->dtlog + (h.iteration - 1), sizeof(double), cudaMemcpyDeviceToHost),
+            "dt read");
+  }
+  if (!(s->dt > 0.0) || !std::isfinite(s->dt))
+    return fail(EK_ERR_NONFINITE, "time step is not finite and positive (dt = " + std::to_string(s->dt) + ")");
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_next_iteration(ek_solver * s)
+{
+  if (!s || !s->has_state)
+    return fail(EK_ERR_INVALID, "ek_solver_next_iteration: no state");
+  ek_status st = launch_step(s, s->iteration);
+  if (st != EK_OK)
+    return st;
+  return sync_from_clock(s);
+}
+
+extern "C" ek_status
+ek_solver_run(ek_solver * s, int nsteps, int * done)
+{
+  if (!s || !s->has_state || nsteps < 0)
+    return fail(EK_ERR_INVALID, "ek_solver_run: bad argument");
+  const int start = s->iteration;
+  int       issued = 0;
+  // steps are launched back to back; the device skips steps once t >= tEnd,
+  // so the host checks the clock only between batches
+  const int batch = 256;
+  while (issued < nsteps && !host_finished(s))
+  {
+    int n = nsteps - issued;
+    n = n < batch ? n : batch;
+    n = n < s->p.nStepmax - s->iteration ? n : s->p.nStepmax - s->iteration;
+    for (int i = 0; i < n; ++i)
+    {
+      ek_status st = launch_step(s, s->iteration + i);
+      if (st != EK_OK)
+        return st;
+    }
+    issued += n;
+    ek_status st = sync_from_clock(s);
+    if (st != EK_OK)
+      return st;
+    if (s->iteration < start + issued)
+      break; // tEnd reached on the device
+  }
+  if (done)
+    *done = s->iteration - start;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_finished(ek_solver * s, int * finished)
+{
+  if (!s || !finished)
+    return fail(EK_ERR_INVALID, "ek_solver_finished: bad argument");
+  *finished = host_finished(s);
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_time(ek_solver * s, double * t, double * dt, int * iteration)
+{
+  if (!s)
+    return fail(EK_ERR_INVALID, "ek_solver_time: null solver");
+  if (t)
+    *t = s->t;
+  if (dt)
+    *dt = s->dt;
+  if (iteration)
+    *iteration = s->iteration;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_dt_history(ek_solver * s, double * dts, int n)
+{
+  if (!s || (!dts && n > 0) || n < 0 || n > s->iteration || n > s->dtcap)
+    return fail(EK_ERR_INVALID, "ek_solver_dt_history: bad argument");
+  if (n)
+    EK_CUDA(cudaMemcpy(dts, s->dtlog, sizeof(double) * n, cudaMemcpyDeviceToHost), "dt history");
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_get_state(ek_solver * s, double * U, int layout)
+{
+  if (!s || !U || !s->has_state || (layout != EK_LAYOUT_LEFT && layout != EK_LAYOUT_RIGHT))
+    return fail(EK_ERR_INVALID, "ek_solver_get_state: bad argument");
+  void * cur = s->U[s->iteration % 2];
+  EK_CUDA(ek_fast::fill_ghosts(s->prec, cur, s->kp, s->p.mhd ? 8 : s->p.nbvar, s->stream), "ghosts");
+  s->launches += 1;
+  ek_status st = download(s, cur, s->hbuf);
+  if (st != EK_OK)
+    return st;
+  from_device_layout(s, s->hbuf, U, layout);
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_totals(ek_solver * s, double out[3])
+{
+  if (!s || !out || !s->has_state)
+    return fail(EK_ERR_INVALID, "ek_solver_totals: bad argument");
+  cudaError_t e = ek_fast::totals(s->prec, s->U[s->iteration % 2], s->kp, s->p.nbvar, s->scratch3, s->stream);
+  if (e == cudaErrorNotSupported)
+    return fail(EK_ERR_UNSUPPORTED, "totals not available for this configuration");
+  EK_CUDA(e, "totals");
+  s->launches += s->p.mhd ? 2 : 1;
+  EK_CUDA(cudaMemcpyAsync(out, s->scratch3, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "totals");
+  EK_CUDA(cudaStreamSynchronize(s->stream), "totals");
+  const double cell = s->p.dx * s->p.dy * (s->p.dim == 3 ? s->p.dz : 1.0);
+  out[0] *= cell;
+  out[1] *= cell;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_device_state(ek_solver * s, void ** ptr, size_t * bytes)
+{
+  if (!s || !ptr)
+    return fail(EK_ERR_INVALID, "ek_solver_device_state: bad argument");
+  *ptr = s->U[s->iteration % 2];
+  if (bytes)
+    *bytes = s->state_bytes;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_synchronize(ek_solver * s)
+{
+  if (!s)
+    return fail(EK_ERR_INVALID, "ek_solver_synchronize: null solver");
+  EK_CUDA(cudaStreamSynchronize(s->stream), "synchronize");
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_launch_count(ek_solver * s, long long * n)
+{
+  if (!s || !n)
+    return fail(EK_ERR_INVALID, "ek_solver_launch_count: bad argument");
+  *n = s->launches;
+  return EK_OK;
+}

@@ -1,0 +1,264 @@
+// Common device-side definitions for the fused MUSCL-Hancock kernels.
+//
+// Layout (identical to the reference's Kokkos::LayoutLeft device arrays,
+// kokkos_shared.h:24-42): U[var][k][j][i], i fastest, ghost cells included.
+// The step kernels never read the ghost cells stored in memory: a ghost
+// coordinate is mapped to the interior cell the reference's boundary fill
+// would copy from (BoundariesFunctors.h:17-1057), one dimension at a time.
+// Because the reference fills the faces in the order x, y, z over the full
+// transverse ranges (SolverBase.cpp:488-512), every edge/corner ghost ends up
+// as the composition of the per-dimension maps, which is what this mapping
+// computes.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#ifndef EK_NS
+#define EK_NS ek_fast
+#endif
+
+namespace ekc
+{
+
+// variable indexes, enums.h:17-40
+enum : int
+{
+  ID = 0,
+  IP = 1,
+  IU = 2,
+  IV = 3,
+  IW = 4,
+  IA = 5,
+  IB = 6,
+  IC = 7
+};
+
+enum : int
+{
+  BC_DIRICHLET = 1, // reflecting
+  BC_NEUMANN = 2,   // outflow / copy
+  BC_PERIODIC = 3
+};
+
+struct KParams
+{
+  int       nx, ny, nz, gw;
+  int       isize, jsize, ksize;
+  int       mhd;
+  long long plane;   // isize * jsize
+  long long vstride; // isize * jsize * ksize: distance between variables
+  int       bc[6];
+  double    dx, dy, dz;
+  double    gamma0, smallr, smallc, smallp, slope_type, cfl, tEnd, cIso;
+  int       riemann;
+  int       kchunk; // interior planes per CTA (3D kernels)
+};
+
+// Per-step scalars kept on the device so that consecutive steps need no host
+// round trip.  Slot s = step % 3 holds the max-reduced inverse time step
+// (as an order-preserving integer key) and the time at the start of step.
+struct DevClock
+{
+  unsigned long long key[3];
+  double             t[3];
+  int                iteration; // number of steps taken
+  int                error;     // sticky device error flags
+  double *           dtlog;     // dt of each step (capacity dtcap)
+  int                dtcap;
+};
+
+enum : int
+{
+  EK_DEVERR_NONFINITE_DT = 1,
+};
+
+// Mixed-precision MHD state: 5 FP32 hydro planes, then (256-byte aligned) the
+// 3 FP64 face-field planes.
+__host__ __device__ inline size_t
+mixed_bfield_offset(long long vstride)
+{
+  return ((size_t)(5 * vstride * 4) + 255) / 256 * 256;
+}
+__host__ __device__ inline double *
+mixed_bfield(void * U, const KParams & P)
+{
+  return (double *)((char *)U + mixed_bfield_offset(P.vstride));
+}
+__host__ __device__ inline const double *
+mixed_bfield(const void * U, const KParams & P)
+{
+  return (const double *)((const char *)U + mixed_bfield_offset(P.vstride));
+}
+
+// order-preserving map double -> uint64 (total order on non-NaN values)
+__host__ __device__ inline unsigned long long
+dkey(double x)
+{
+  unsigned long long b;
+#ifdef __CUDA_ARCH__
+  b = (unsigned long long)__double_as_longlong(x);
+#else
+  memcpy(&b, &x, 8);
+#endif
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ inline double
+dkey_inv(unsigned long long k)
+{
+  unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+// key of -DBL_MAX: the identity of the reference's Kokkos::Max reducer
+#define EK_KEY_LOWEST 0x0010000000000000ull
+
+} // namespace ekc
+
+namespace EK_NS
+{
+using namespace ekc;
+
+// Map a (possibly ghost) coordinate g in [0, n+2gw) of one dimension to the
+// interior coordinate the boundary fill copies from; *flip is set when the
+// reflecting wall flips the sign of the normal components.
+__device__ __forceinline__ int
+bc_map(int g, int n, int gw, int bc_lo, int bc_hi, bool * flip)
+{
+  // coordinates past the ghost layers only occur in the padding of partial
+  // tiles; clamping keeps every read inside the array
+  g = g < 0 ? 0 : (g > n + 2 * gw - 1 ? n + 2 * gw - 1 : g);
+  if (g < gw)
+  {
+    if (bc_lo == BC_DIRICHLET)
+    {
+      *flip = !*flip;
+      return 2 * gw - 1 - g;
+    }
+    if (bc_lo == BC_NEUMANN)
+      return gw;
+    return n + g;
+  }
+  if (g >= n + gw)
+  {
+    if (bc_hi == BC_DIRICHLET)
+    {
+      *flip = !*flip;
+      return 2 * n + 2 * gw - 1 - g;
+    }
+    if (bc_hi == BC_NEUMANN)
+      return n + gw - 1;
+    return g - n;
+  }
+  return g;
+}
+
+// Source offset (in one variable plane) and per-dimension flips of a cell.
+struct SrcCell
+{
+  long long off;
+  bool      fx, fy, fz;
+};
+
+__device__ __forceinline__ SrcCell
+src_cell(const KParams & P, int gi, int gj, int gk)
+{
+  SrcCell s;
+  s.fx = s.fy = s.fz = false;
+  int si = bc_map(gi, P.nx, P.gw, P.bc[0], P.bc[1], &s.fx);
+  int sj = bc_map(gj, P.ny, P.gw, P.bc[2], P.bc[3], &s.fy);
+  int sk = gk;
+  if (P.ksize > 1)
+    sk = bc_map(gk, P.nz, P.gw, P.bc[4], P.bc[5], &s.fz);
+  s.off = (long long)sk * P.plane + (long long)sj * P.isize + si;
+  return s;
+}
+
+// sign of variable v at a mapped cell: the reflecting fill multiplies the
+// normal velocity (and, for MHD, the normal face field) by -1 per wall
+__device__ __forceinline__ bool
+flips(const SrcCell & s, int v, int mhd)
+{
+  bool f = false;
+  if (v == IU || (mhd && v == IA))
+    f ^= s.fx;
+  if (v == IV || (mhd && v == IB))
+    f ^= s.fy;
+  if (v == IW || (mhd && v == IC))
+    f ^= s.fz;
+  return f;
+}
+
+template <class T>
+__device__ __forceinline__ T
+ldg(const T * p)
+{
+  return __ldg(p);
+}
+
+// dt at the start of a step, SolverBase::compute_dt (SolverBase.cpp:124-154)
+__device__ __forceinline__ void
+step_dt(const KParams & P, const DevClock * clk, int step, double * t, double * dt)
+{
+  const int    s = step % 3;
+  const double invDt = dkey_inv(clk->key[s]);
+  double       d = P.cfl / invDt;
+  const double tt = clk->t[s];
+  if (tt + d > P.tEnd)
+    d = P.tEnd - tt;
+  *t = tt;
+  *dt = d;
+}
+
+// bookkeeping done once per step by block 0, thread 0
+__device__ __forceinline__ void
+step_commit(DevClock * clk, int step, double t, double dt)
+{
+  clk->t[(step + 1) % 3] = t + dt;
+  clk->key[(step + 2) % 3] = EK_KEY_LOWEST;
+  if (step < clk->dtcap)
+    clk->dtlog[step] = dt;
+  clk->iteration = step + 1;
+}
+
+// block-wide max of a thread-local key, then one atomicMax per block
+template <int NT>
+__device__ __forceinline__ void
+block_max_commit(unsigned long long local, unsigned long long * dst)
+{
+  __shared__ unsigned long long red[NT / 32];
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    unsigned long long other = __shfl_xor_sync(0xffffffffu, local, o);
+    local = other > local ? other : local;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    red[warp] = local;
+  __syncthreads();
+  if (warp == 0)
+  {
+    local = lane < NT / 32 ? red[lane] : 0ull;
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      unsigned long long other = __shfl_xor_sync(0xffffffffu, local, o);
+      local = other > local ? other : local;
+    }
+    if (lane == 0)
+      atomicMax(dst, local);
+  }
+}
+
+// fmax semantics of the reference's reduction: a NaN candidate is ignored
+__device__ __forceinline__ unsigned long long
+cand_key(double v)
+{
+  return (v != v) ? 0ull : dkey(v);
+}
+
+} // namespace EK_NS

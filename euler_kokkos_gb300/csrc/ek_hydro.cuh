@@ -1,0 +1,245 @@
+// Hydro cell/face arithmetic of the unsplit MUSCL-Hancock step, written for
+// one cell or one face so the fused kernels can call it on shared-memory
+// tiles.  Every expression keeps the evaluation order of the reference so the
+// FP64 build compiled without FMA contraction reproduces it bit for bit; the
+// cited reference lines define the arithmetic.
+#pragma once
+
+#include "ek_common.cuh"
+
+namespace EK_NS
+{
+
+template <class R>
+struct HydroConst
+{
+  R gamma0, smallr, smallp, smallc, slope_type;
+};
+
+// slope_unsplit_hydro_3d_scalar, one direction (HydroBaseFunctor3D.h:413-462,
+// HydroBaseFunctor2D.h:423-453): minmod (slope_type 1) / MC (slope_type 2)
+template <class R>
+__device__ __forceinline__ R
+slope1(R q, R qp, R qm, R st)
+{
+  const R dlft = st * (q - qm);
+  const R drgt = st * (qp - q);
+  const R dcen = R(0.5) * (qp - qm);
+  const R dsgn = (dcen >= R(0)) ? R(1) : R(-1);
+  const R slop = fmin(fabs(dlft), fabs(drgt));
+  R       dlim = slop;
+  if ((dlft * drgt) <= R(0))
+    dlim = R(0);
+  return dsgn * fmin(dlim, fabs(dcen));
+}
+
+// computePrimitives (HydroBaseFunctor2D.h:78-102, HydroBaseFunctor3D.h:80-106).
+// In the mixed form (R = float) the internal energy is recomputed in FP64
+// when E/rho and the kinetic energy cancel to fewer than ~7 significant bits.
+template <class R, int NV>
+__device__ __forceinline__ void
+hydro_prims(const R (&u)[NV], R (&q)[NV], const HydroConst<R> & C)
+{
+  const R d = fmax(u[ID], C.smallr);
+  const R ux = u[IU] / d;
+  const R uy = u[IV] / d;
+  R       eken, uz = R(0);
+  if constexpr (NV == 4)
+    eken = R(0.5) * (ux * ux + uy * uy);
+  else
+  {
+    uz = u[IW] / d;
+    eken = R(0.5) * (ux * ux + uy * uy + uz * uz);
+  }
+  R e = u[IP] / d - eken;
+  if constexpr (sizeof(R) == 4)
+  {
+    if (e < R(1.0 / 128.0) * (u[IP] / d))
+    {
+      // FP64 island: cancellation between total and kinetic energy
+      const double dd = (double)d;
+      const double vx = (double)u[IU] / dd, vy = (double)u[IV] / dd;
+      double       ek = vx * vx + vy * vy;
+      if constexpr (NV == 5)
+      {
+        const double vz = (double)u[IW] / dd;
+        ek += vz * vz;
+      }
+      e = (R)((double)u[IP] / dd - 0.5 * ek);
+    }
+  }
+  const R p = fmax((C.gamma0 - R(1)) * d * e, d * C.smallp);
+  q[ID] = d;
+  q[IP] = p;
+  q[IU] = ux;
+  q[IV] = uy;
+  if constexpr (NV == 5)
+    q[IW] = uz;
+}
+
+// sound speed as computePrimitives computes it: sqrt(gamma0 * p / d)
+template <class R>
+__device__ __forceinline__ R
+hydro_sound(R d, R p, const HydroConst<R> & C)
+{
+  return sqrt(C.gamma0 * (p) / d);
+}
+
+// Per-cell source terms of trace_unsplit_{2d,3d}_along_dir
+// (HydroBaseFunctor2D.h:250-253, HydroBaseFunctor3D.h:321-325).  They do not
+// depend on the face, so they are computed once per cell.
+template <class R, int NV>
+__device__ __forceinline__ void
+hydro_sources(const R (&q)[NV], const R (&dx)[NV], const R (&dy)[NV], const R (&dz)[NV], R (&s)[NV],
+              const HydroConst<R> & C)
+{
+  const R r = q[ID], p = q[IP], u = q[IU], v = q[IV];
+  if constexpr (NV == 4)
+  {
+    s[ID] = -u * dx[ID] - v * dy[ID] - (dx[IU] + dy[IV]) * r;
+    s[IP] = -u * dx[IP] - v * dy[IP] - (dx[IU] + dy[IV]) * C.gamma0 * p;
+    s[IU] = -u * dx[IU] - v * dy[IU] - (dx[IP]) / r;
+    s[IV] = -u * dx[IV] - v * dy[IV] - (dy[IP]) / r;
+  }
+  else
+  {
+    const R w = q[IW];
+    s[ID] = -u * dx[ID] - v * dy[ID] - w * dz[ID] - (dx[IU] + dy[IV] + dz[IW]) * r;
+    s[IP] = -u * dx[IP] - v * dy[IP] - w * dz[IP] - (dx[IU] + dy[IV] + dz[IW]) * C.gamma0 * p;
+    s[IU] = -u * dx[IU] - v * dy[IU] - w * dz[IU] - (dx[IP]) / r;
+    s[IV] = -u * dx[IV] - v * dy[IV] - w * dz[IV] - (dy[IP]) / r;
+    s[IW] = -u * dx[IW] - v * dy[IW] - w * dz[IW] - (dz[IP]) / r;
+  }
+}
+
+// face state of trace_unsplit_*_along_dir: q -/+ dq/2 + s*dtdx/2, rho floored
+// (HydroBaseFunctor3D.h:327-365); sgn = -1 for the MIN face, +1 for MAX
+template <class R, int NV>
+__device__ __forceinline__ void
+hydro_face(const R (&q)[NV], const R (&d)[NV], const R (&s)[NV], R dtd, bool plus, R (&f)[NV],
+           R smallr)
+{
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+  {
+    if (plus)
+      f[v] = q[v] + R(0.5) * d[v] + s[v] * dtd * R(0.5);
+    else
+      f[v] = q[v] - R(0.5) * d[v] + s[v] * dtd * R(0.5);
+  }
+  f[ID] = fmax(smallr, f[ID]);
+}
+
+// riemann_hllc (RiemannSolvers.h:445-568).  States are in the face frame
+// (normal velocity in IU); NV = 4 (2D) or 5 (3D).
+template <class R, int NV>
+__device__ __forceinline__ void
+hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
+{
+  const R entho = R(1) / (C.gamma0 - R(1));
+  const R rl = fmax(ql[ID], C.smallr);
+  const R pl = fmax(ql[IP], rl * C.smallp);
+  const R ul = ql[IU];
+  R       ecinl = R(0.5) * rl * ul * ul;
+  ecinl += R(0.5) * rl * ql[IV] * ql[IV];
+  if constexpr (NV == 5)
+    ecinl += R(0.5) * rl * ql[IW] * ql[IW];
+  const R etotl = pl * entho + ecinl;
+  const R ptotl = pl;
+
+  const R rr = fmax(qr[ID], C.smallr);
+  const R pr = fmax(qr[IP], rr * C.smallp);
+  const R ur = qr[IU];
+  R       ecinr = R(0.5) * rr * ur * ur;
+  ecinr += R(0.5) * rr * qr[IV] * qr[IV];
+  if constexpr (NV == 5)
+    ecinr += R(0.5) * rr * qr[IW] * qr[IW];
+  const R etotr = pr * entho + ecinr;
+  const R ptotr = pr;
+
+  const R cfastl = sqrt(fmax(C.gamma0 * pl / rl, C.smallc * C.smallc));
+  const R cfastr = sqrt(fmax(C.gamma0 * pr / rr, C.smallc * C.smallc));
+
+  const R SL = fmin(ul, ur) - fmax(cfastl, cfastr);
+  const R SR = fmax(ul, ur) + fmax(cfastl, cfastr);
+
+  const R rcl = rl * (ul - SL);
+  const R rcr = rr * (SR - ur);
+
+  const R ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
+  const R ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+
+  R ro, uo, ptoto, etoto;
+  if (SL > R(0))
+  {
+    ro = rl;
+    uo = ul;
+    ptoto = ptotl;
+    etoto = etotl;
+  }
+  else if (ustar > R(0))
+  {
+    ro = rl * (SL - ul) / (SL - ustar);
+    uo = ustar;
+    ptoto = ptotstar;
+    etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) / (SL - ustar);
+  }
+  else if (SR > R(0))
+  {
+    ro = rr * (SR - ur) / (SR - ustar);
+    uo = ustar;
+    ptoto = ptotstar;
+    etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) / (SR - ustar);
+  }
+  else
+  {
+    ro = rr;
+    uo = ur;
+    ptoto = ptotr;
+    etoto = etotr;
+  }
+  flux[ID] = ro * uo;
+  flux[IU] = ro * uo * uo + ptoto;
+  flux[IP] = (etoto + ptoto) * uo;
+  flux[IV] = flux[ID] * ((flux[ID] > R(0)) ? ql[IV] : qr[IV]);
+  if constexpr (NV == 5)
+    flux[IW] = flux[ID] * ((flux[ID] > R(0)) ? ql[IW] : qr[IW]);
+}
+
+// per-cell CFL candidate of ComputeDtFunctor{2D,3D}
+// (HydroRunFunctors2D.h:56-84, HydroRunFunctors3D.h:49-84), always returned
+// in double so that the max-reduction and dt stay FP64
+template <class R, int NV>
+__device__ __forceinline__ double
+hydro_invdt(const R (&u)[NV], const HydroConst<R> & C, double dx, double dy, double dz)
+{
+  R q[NV];
+  hydro_prims<R, NV>(u, q, C);
+  const R c = hydro_sound<R>(q[ID], q[IP], C);
+  if constexpr (sizeof(R) == 8)
+  {
+    const double vx = c + fabs(q[IU]);
+    const double vy = c + fabs(q[IV]);
+    if constexpr (NV == 4)
+      return vx / dx + vy / dy;
+    else
+    {
+      const double vz = c + fabs(q[IW]);
+      return vx / dx + vy / dy + vz / dz;
+    }
+  }
+  else
+  {
+    const double vx = (double)c + fabs((double)q[IU]);
+    const double vy = (double)c + fabs((double)q[IV]);
+    if constexpr (NV == 4)
+      return vx / dx + vy / dy;
+    else
+    {
+      const double vz = (double)c + fabs((double)q[IW]);
+      return vx / dx + vy / dy + vz / dz;
+    }
+  }
+}
+
+} // namespace EK_NS

@@ -1,0 +1,530 @@
+// Fused hydro step kernels (2D tile, 3D tile marching in z).
+//
+// One launch performs the whole implementationVersion=0 step of
+// SolverHydroMuscl::godunov_unsplit_impl (SolverHydroMuscl.cpp:214-243,
+// 304-330) for its tile: ghost fill (virtual, ek_common.cuh), primitive
+// variables, limited slopes, half-step face traces, HLLC fluxes, conservative
+// update, and the CFL candidate of the NEXT step (ComputeDtFunctor on the new
+// state, SolverHydroMuscl.h:589-631), reduced with one atomicMax per block.
+// U is read from HBM once (plus the tile halo) and written once.
+#pragma once
+
+#include "ek_hydro.cuh"
+
+namespace EK_NS
+{
+
+template <class R>
+__device__ __forceinline__ HydroConst<R>
+hydro_const(const KParams & P)
+{
+  HydroConst<R> C;
+  C.gamma0 = (R)P.gamma0;
+  C.smallr = (R)P.smallr;
+  C.smallp = (R)P.smallp;
+  C.smallc = (R)P.smallc;
+  C.slope_type = (R)P.slope_type;
+  return C;
+}
+
+// Load one (TX+4) x (TY+4) plane of U (global plane gk), convert to primitive
+// variables and store into sQ[NV][HY][HX]; halo cells are mapped through the
+// boundary conditions.
+template <class S, class R, int NV, int TX, int TY>
+__device__ __forceinline__ void
+load_q_plane(const S * __restrict__ U, const KParams & P, const HydroConst<R> & C, int gi0, int gj0,
+             int gk, R * sQ)
+{
+  constexpr int HX = TX + 4, HY = TY + 4, NT = TX * TY;
+  for (int c = threadIdx.x; c < HX * HY; c += NT)
+  {
+    const int     hx = c % HX, hy = c / HX;
+    const SrcCell s = src_cell(P, gi0 - 2 + hx, gj0 - 2 + hy, gk);
+    R             u[NV], q[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+    {
+      R x = (R)ldg(U + v * P.vstride + s.off);
+      u[v] = flips(s, v, 0) ? -x : x;
+    }
+    hydro_prims<R, NV>(u, q, C);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      sQ[(v * HY + hy) * HX + hx] = q[v];
+  }
+}
+
+// slopes of the cell at tile coordinates (hx, hy) of the planes qm/q0/qp
+template <class R, int NV, int HX, int HY>
+__device__ __forceinline__ void
+cell_slopes(const R * q0, const R * qm, const R * qp, int hx, int hy, R st, R (&c)[NV], R (&dX)[NV],
+            R (&dY)[NV], R (&dZ)[NV], bool three_d)
+{
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+  {
+    const R * p = q0 + v * HY * HX;
+    const R   x = p[hy * HX + hx];
+    c[v] = x;
+    dX[v] = slope1<R>(x, p[hy * HX + hx + 1], p[hy * HX + hx - 1], st);
+    dY[v] = slope1<R>(x, p[(hy + 1) * HX + hx], p[(hy - 1) * HX + hx], st);
+    if (three_d)
+      dZ[v] = slope1<R>(x, qp[(v * HY + hy) * HX + hx], qm[(v * HY + hy) * HX + hx], st);
+    else
+      dZ[v] = R(0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 2D: one CTA = one TX x TY tile of interior cells
+// ---------------------------------------------------------------------------
+template <class S, class R, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY)
+hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
+{
+  constexpr int NV = 4, HX = TX + 4, HY = TY + 4, NT = TX * TY;
+  constexpr int FX = TX + 2; // face-state rows in x: cells -1..TX
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R * sQ = reinterpret_cast<R *>(smem_raw);  // [NV][HY][HX]
+  R * sXm = sQ + NV * HY * HX;               // XMIN state of cells -1..TX, then x-flux
+  R * sXp = sXm + NV * TY * FX;              // XMAX state
+  R * sYm = sXp + NV * TY * FX;              // YMIN state of cells -1..TY, then y-flux
+  R * sYp = sYm + NV * (TY + 2) * TX;        // YMAX state
+
+  double t, dt;
+  step_dt(P, clk, step, &t, &dt);
+  if (t >= P.tEnd - 1e-14)
+    return;
+  const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy);
+  const HydroConst<R> C = hydro_const<R>(P);
+
+  const int gi0 = P.gw + blockIdx.x * TX, gj0 = P.gw + blockIdx.y * TY;
+  load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, 0, sQ);
+  __syncthreads();
+
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  // traces of the interior cell
+  {
+    R c[NV], dX[NV], dY[NV], dZ[NV], s[NV], f[NV];
+    cell_slopes<R, NV, HX, HY>(sQ, sQ, sQ, tx + 2, ty + 2, C.slope_type, c, dX, dY, dZ, false);
+    hydro_sources<R, NV>(c, dX, dY, dZ, s, C);
+    hydro_face<R, NV>(c, dX, s, dtdx, false, f, C.smallr);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      sXm[(v * TY + ty) * FX + tx + 1] = f[v];
+    hydro_face<R, NV>(c, dX, s, dtdx, true, f, C.smallr);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      sXp[(v * TY + ty) * FX + tx + 1] = f[v];
+    hydro_face<R, NV>(c, dY, s, dtdy, false, f, C.smallr);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      sYm[(v * (TY + 2) + ty + 1) * TX + tx] = f[v];
+    hydro_face<R, NV>(c, dY, s, dtdy, true, f, C.smallr);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      sYp[(v * (TY + 2) + ty + 1) * TX + tx] = f[v];
+  }
+  // ring cells: only the face state facing the tile
+  for (int r = threadIdx.x; r < 2 * (TX + TY); r += NT)
+  {
+    int cx, cy, kind; // kind 0: left (XMAX), 1: right (XMIN), 2: bottom (YMAX), 3: top (YMIN)
+    if (r < TY)
+    {
+      cx = -1, cy = r, kind = 0;
+    }
+    else if (r < 2 * TY)
+    {
+      cx = TX, cy = r - TY, kind = 1;
+    }
+    else if (r < 2 * TY + TX)
+    {
+      cx = r - 2 * TY, cy = -1, kind = 2;
+    }
+    else
+    {
+      cx = r - 2 * TY - TX, cy = TY, kind = 3;
+    }
+    R c[NV], dX[NV], dY[NV], dZ[NV], s[NV], f[NV];
+    cell_slopes<R, NV, HX, HY>(sQ, sQ, sQ, cx + 2, cy + 2, C.slope_type, c, dX, dY, dZ, false);
+    hydro_sources<R, NV>(c, dX, dY, dZ, s, C);
+    if (kind < 2)
+    {
+      hydro_face<R, NV>(c, dX, s, dtdx, kind == 0, f, C.smallr);
+      R * dst = kind == 0 ? sXp : sXm;
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        dst[(v * TY + cy) * FX + cx + 1] = f[v];
+    }
+    else
+    {
+      hydro_face<R, NV>(c, dY, s, dtdy, kind == 2, f, C.smallr);
+      R * dst = kind == 2 ? sYp : sYm;
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        dst[(v * (TY + 2) + cy + 1) * TX + cx] = f[v];
+    }
+  }
+  __syncthreads();
+
+  // fluxes: x-face i (left face of cell i) from XMAX(i-1), XMIN(i); stored
+  // scaled by dt/dx into the XMIN slot of cell i (HydroRunFunctors2D.h:653-661)
+  for (int fidx = threadIdx.x; fidx < (TX + 1) * TY; fidx += NT)
+  {
+    const int i = fidx % (TX + 1), j = fidx / (TX + 1);
+    R         ql[NV], qr[NV], fl[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+    {
+      ql[v] = sXp[(v * TY + j) * FX + i];
+      qr[v] = sXm[(v * TY + j) * FX + i + 1];
+    }
+    hllc<R, NV>(ql, qr, fl, C);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      sXm[(v * TY + j) * FX + i + 1] = fl[v] * dtdx;
+  }
+  // y-faces: swap IU/IV around the solver (HydroRunFunctors2D.h:741-758)
+  for (int fidx = threadIdx.x; fidx < TX * (TY + 1); fidx += NT)
+  {
+    const int i = fidx % TX, j = fidx / TX;
+    R         ql[NV], qr[NV], fl[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+    {
+      ql[v] = sYp[(v * (TY + 2) + j) * TX + i];
+      qr[v] = sYm[(v * (TY + 2) + j + 1) * TX + i];
+    }
+    R tmp = ql[IU];
+    ql[IU] = ql[IV];
+    ql[IV] = tmp;
+    tmp = qr[IU];
+    qr[IU] = qr[IV];
+    qr[IV] = tmp;
+    hllc<R, NV>(ql, qr, fl, C);
+    tmp = fl[IU];
+    fl[IU] = fl[IV];
+    fl[IV] = tmp;
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      sYm[(v * (TY + 2) + j + 1) * TX + i] = fl[v] * dtdy;
+  }
+  __syncthreads();
+
+  // update (UpdateFunctor2D, HydroRunFunctors2D.h:809-836), in its order
+  const int gi = gi0 + tx, gj = gj0 + ty;
+  unsigned long long kmax = 0ull;
+  if (gi < P.nx + P.gw && gj < P.ny + P.gw)
+  {
+    const long long off = (long long)gj * P.isize + gi;
+    R               u[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+    {
+      R x = (R)ldg(Uin + v * P.vstride + off);
+      x += sXm[(v * TY + ty) * FX + tx + 1];
+      x -= sXm[(v * TY + ty) * FX + tx + 2];
+      x += sYm[(v * (TY + 2) + ty + 1) * TX + tx];
+      x -= sYm[(v * (TY + 2) + ty + 2) * TX + tx];
+      u[v] = x;
+      Uout[v * P.vstride + off] = (S)x;
+    }
+    // the next step's dt is computed on the stored (possibly rounded) state
+    R us[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      us[v] = (R)(S)u[v];
+    kmax = cand_key(hydro_invdt<R, NV>(us, C, P.dx, P.dy, P.dz));
+  }
+  block_max_commit<NT>(kmax, &clk->key[(step + 1) % 3]);
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
+    step_commit(clk, step, t, dt);
+}
+
+// ---------------------------------------------------------------------------
+// 3D: one CTA = a TX x TY column of interior cells marching over kchunk planes
+// ---------------------------------------------------------------------------
+template <class S, class R, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY)
+hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
+{
+  constexpr int NV = 5, HX = TX + 4, HY = TY + 4, NT = TX * TY;
+  constexpr int FX = TX + 2;
+  constexpr int QP = NV * HY * HX; // one primitive plane
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R * sQ = reinterpret_cast<R *>(smem_raw); // [3][NV][HY][HX] ring of planes
+  R * sXm = sQ + 3 * QP;
+  R * sXp = sXm + NV * TY * FX;
+  R * sYm = sXp + NV * TY * FX;
+  R * sYp = sYm + NV * (TY + 2) * TX;
+
+  double t, dt;
+  step_dt(P, clk, step, &t, &dt);
+  if (t >= P.tEnd - 1e-14)
+    return;
+  const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy), dtdz = (R)(dt / P.dz);
+  const HydroConst<R> C = hydro_const<R>(P);
+
+  const int gw = P.gw;
+  const int gi0 = gw + blockIdx.x * TX, gj0 = gw + blockIdx.y * TY;
+  const int k0 = blockIdx.z * P.kchunk; // interior plane index
+  const int k1 = min(k0 + P.kchunk, P.nz);
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  const int gi = gi0 + tx, gj = gj0 + ty;
+  const bool own = gi < P.nx + gw && gj < P.ny + gw;
+  const long long own_off = (long long)gj * P.isize + gi;
+
+  // prologue: planes k0-2, k0-1
+  load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 2 + gw, sQ + ((k0 + 1) % 3) * QP);
+  load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 1 + gw, sQ + ((k0 + 2) % 3) * QP);
+
+  R   zmax_prev[NV]; // ZMAX face state of the cell below
+  R   acc[NV];       // partial update of the cell below, waiting for -Fz(k)
+  unsigned long long kmax = 0ull;
+
+  for (int kc = k0 - 1; kc <= k1; ++kc)
+  {
+    // plane kc+1 into ring slot (kc+1)%3  [(kc+1+3)%3 to stay non-negative]
+    load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, kc + 1 + gw, sQ + ((kc + 4) % 3) * QP);
+    __syncthreads();
+    const R * q0 = sQ + ((kc + 3) % 3) * QP;
+    const R * qm = sQ + ((kc + 2) % 3) * QP;
+    const R * qp = sQ + ((kc + 4) % 3) * QP;
+    const bool full = kc >= k0 && kc < k1;
+
+    R fz[NV];
+    {
+      R c[NV], dX[NV], dY[NV], dZ[NV], s[NV], f[NV];
+      cell_slopes<R, NV, HX, HY>(q0, qm, qp, tx + 2, ty + 2, C.slope_type, c, dX, dY, dZ, true);
+      hydro_sources<R, NV>(c, dX, dY, dZ, s, C);
+      if (full)
+      {
+        hydro_face<R, NV>(c, dX, s, dtdx, false, f, C.smallr);
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          sXm[(v * TY + ty) * FX + tx + 1] = f[v];
+        hydro_face<R, NV>(c, dX, s, dtdx, true, f, C.smallr);
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          sXp[(v * TY + ty) * FX + tx + 1] = f[v];
+        hydro_face<R, NV>(c, dY, s, dtdy, false, f, C.smallr);
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          sYm[(v * (TY + 2) + ty + 1) * TX + tx] = f[v];
+        hydro_face<R, NV>(c, dY, s, dtdy, true, f, C.smallr);
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          sYp[(v * (TY + 2) + ty + 1) * TX + tx] = f[v];
+      }
+      if (kc >= k0)
+      {
+        // z-face between kc-1 and kc: ZMAX(kc-1), ZMIN(kc); swap IU/IW
+        // (HydroRunFunctors3D.h:672-707)
+        R qr[NV];
+        hydro_face<R, NV>(c, dZ, s, dtdz, false, qr, C.smallr);
+        R ql[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          ql[v] = zmax_prev[v];
+        R tmp = ql[IU];
+        ql[IU] = ql[IW];
+        ql[IW] = tmp;
+        tmp = qr[IU];
+        qr[IU] = qr[IW];
+        qr[IW] = tmp;
+        hllc<R, NV>(ql, qr, fz, C);
+        tmp = fz[IU];
+        fz[IU] = fz[IW];
+        fz[IW] = tmp;
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          fz[v] = fz[v] * dtdz;
+      }
+      if (kc < k1)
+        hydro_face<R, NV>(c, dZ, s, dtdz, true, zmax_prev, C.smallr);
+    }
+    if (full)
+    {
+      for (int r = threadIdx.x; r < 2 * (TX + TY); r += NT)
+      {
+        int cx, cy, kind;
+        if (r < TY)
+        {
+          cx = -1, cy = r, kind = 0;
+        }
+        else if (r < 2 * TY)
+        {
+          cx = TX, cy = r - TY, kind = 1;
+        }
+        else if (r < 2 * TY + TX)
+        {
+          cx = r - 2 * TY, cy = -1, kind = 2;
+        }
+        else
+        {
+          cx = r - 2 * TY - TX, cy = TY, kind = 3;
+        }
+        R c[NV], dX[NV], dY[NV], dZ[NV], s[NV], f[NV];
+        cell_slopes<R, NV, HX, HY>(q0, qm, qp, cx + 2, cy + 2, C.slope_type, c, dX, dY, dZ, true);
+        hydro_sources<R, NV>(c, dX, dY, dZ, s, C);
+        if (kind < 2)
+        {
+          hydro_face<R, NV>(c, dX, s, dtdx, kind == 0, f, C.smallr);
+          R * dst = kind == 0 ? sXp : sXm;
+#pragma unroll
+          for (int v = 0; v < NV; ++v)
+            dst[(v * TY + cy) * FX + cx + 1] = f[v];
+        }
+        else
+        {
+          hydro_face<R, NV>(c, dY, s, dtdy, kind == 2, f, C.smallr);
+          R * dst = kind == 2 ? sYp : sYm;
+#pragma unroll
+          for (int v = 0; v < NV; ++v)
+            dst[(v * (TY + 2) + cy + 1) * TX + cx] = f[v];
+        }
+      }
+    }
+    __syncthreads();
+
+    if (full)
+    {
+      for (int fidx = threadIdx.x; fidx < (TX + 1) * TY; fidx += NT)
+      {
+        const int i = fidx % (TX + 1), j = fidx / (TX + 1);
+        R         ql[NV], qr[NV], fl[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+        {
+          ql[v] = sXp[(v * TY + j) * FX + i];
+          qr[v] = sXm[(v * TY + j) * FX + i + 1];
+        }
+        hllc<R, NV>(ql, qr, fl, C);
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          sXm[(v * TY + j) * FX + i + 1] = fl[v] * dtdx;
+      }
+      for (int fidx = threadIdx.x; fidx < TX * (TY + 1); fidx += NT)
+      {
+        const int i = fidx % TX, j = fidx / TX;
+        R         ql[NV], qr[NV], fl[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+        {
+          ql[v] = sYp[(v * (TY + 2) + j) * TX + i];
+          qr[v] = sYm[(v * (TY + 2) + j + 1) * TX + i];
+        }
+        R tmp = ql[IU];
+        ql[IU] = ql[IV];
+        ql[IV] = tmp;
+        tmp = qr[IU];
+        qr[IU] = qr[IV];
+        qr[IV] = tmp;
+        hllc<R, NV>(ql, qr, fl, C);
+        tmp = fl[IU];
+        fl[IU] = fl[IV];
+        fl[IV] = tmp;
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+          sYm[(v * (TY + 2) + j + 1) * TX + i] = fl[v] * dtdy;
+      }
+      __syncthreads();
+    }
+
+    // finish the cell below: U(kc-1) -= Fz(kc)  (UpdateFunctor3D order,
+    // HydroRunFunctors3D.h:775-809), store it and take its CFL candidate
+    if (kc > k0 && own)
+    {
+      R us[NV];
+      const long long off = own_off + (long long)(kc - 1 + gw) * P.plane;
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+      {
+        const R x = acc[v] - fz[v];
+        Uout[v * P.vstride + off] = (S)x;
+        us[v] = (R)(S)x;
+      }
+      unsigned long long kk = cand_key(hydro_invdt<R, NV>(us, C, P.dx, P.dy, P.dz));
+      kmax = kk > kmax ? kk : kmax;
+    }
+    if (full && own)
+    {
+      const long long off = own_off + (long long)(kc + gw) * P.plane;
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+      {
+        R x = (R)ldg(Uin + v * P.vstride + off);
+        x += sXm[(v * TY + ty) * FX + tx + 1];
+        x -= sXm[(v * TY + ty) * FX + tx + 2];
+        x += sYm[(v * (TY + 2) + ty + 1) * TX + tx];
+        x -= sYm[(v * (TY + 2) + ty + 2) * TX + tx];
+        x += fz[v];
+        acc[v] = x;
+      }
+    }
+    __syncthreads(); // ring slot and face buffers are reused next plane
+  }
+  block_max_commit<NT>(kmax, &clk->key[(step + 1) % 3]);
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
+    step_commit(clk, step, t, dt);
+}
+
+// ---------------------------------------------------------------------------
+// CFL reduction over the interior of a state (ComputeDtFunctor{2D,3D});
+// used after the state is set (the constructor's compute_dt()).
+// ---------------------------------------------------------------------------
+template <class S, class R, int NV>
+__global__ void
+hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
+{
+  const HydroConst<R> C = hydro_const<R>(P);
+  const long long     n = (long long)P.nx * P.ny * (NV == 5 ? P.nz : 1);
+  unsigned long long  kmax = 0ull;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x)
+  {
+    const int       i = (int)(c % P.nx);
+    const long long r = c / P.nx;
+    const int       j = (int)(r % P.ny);
+    const int       k = (int)(r / P.ny);
+    const long long off = (long long)(k + (NV == 5 ? P.gw : 0)) * P.plane +
+                          (long long)(j + P.gw) * P.isize + (i + P.gw);
+    R u[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      u[v] = (R)ldg(U + v * P.vstride + off);
+    unsigned long long kk = cand_key(hydro_invdt<R, NV>(u, C, P.dx, P.dy, P.dz));
+    kmax = kk > kmax ? kk : kmax;
+  }
+  block_max_commit<256>(kmax, key);
+}
+
+// Fill the ghost cells of a state in memory (make_boundaries_serial result,
+// SolverBase.cpp:488-512), for callers that read the full array back.  U
+// points at the plane of variable var0; nbvar planes are filled.
+template <class S>
+__global__ void
+fill_ghosts_kernel(S * __restrict__ U, KParams P, int nbvar, int var0)
+{
+  const long long n = P.vstride;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x)
+  {
+    const int       i = (int)(c % P.isize);
+    const long long r = c / P.isize;
+    const int       j = (int)(r % P.jsize);
+    const int       k = (int)(r / P.jsize);
+    const bool ghost = i < P.gw || i >= P.nx + P.gw || j < P.gw || j >= P.ny + P.gw ||
+                       (P.ksize > 1 && (k < P.gw || k >= P.nz + P.gw));
+    if (!ghost)
+      continue;
+    const SrcCell s = src_cell(P, i, j, k);
+    for (int lv = 0; lv < nbvar; ++lv)
+    {
+      const S x = U[(long long)lv * P.vstride + s.off];
+      U[(long long)lv * P.vstride + c] = flips(s, var0 + lv, P.mhd) ? -x : x;
+    }
+  }
+}
+
+} // namespace EK_NS

@@ -1,0 +1,175 @@
+// Kernel instantiations and launchers.  Compiled twice (see ek_launch.h):
+//   -DEK_NS=ek_exact --fmad=false   FP64 only, bitwise parity build
+//   -DEK_NS=ek_fast  --fmad=true    FP64 + mixed FP32
+#include "ek_launch.h"
+#include "ek_hydro_kernels.cuh"
+#include "ek_mhd_kernels.cuh"
+
+namespace EK_NS
+{
+
+namespace
+{
+constexpr int H2_TX = 32, H2_TY = 8;
+constexpr int H3_TX = 32, H3_TY = 8;
+
+template <class R>
+constexpr size_t
+hydro2d_smem()
+{
+  constexpr int NV = 4, HX = H2_TX + 4, HY = H2_TY + 4;
+  return sizeof(R) * (NV * HY * HX + 2 * NV * H2_TY * (H2_TX + 2) + 2 * NV * (H2_TY + 2) * H2_TX);
+}
+template <class R>
+constexpr size_t
+hydro3d_smem()
+{
+  constexpr int NV = 5, HX = H3_TX + 4, HY = H3_TY + 4;
+  return sizeof(R) *
+         (3 * NV * HY * HX + 2 * NV * H3_TY * (H3_TX + 2) + 2 * NV * (H3_TY + 2) * H3_TX);
+}
+
+template <class S, class R>
+cudaError_t
+hydro_step_t(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
+             cudaStream_t st)
+{
+  if (dim == 2)
+  {
+    auto   k = hydro2d_step<S, R, H2_TX, H2_TY>;
+    size_t sm = hydro2d_smem<R>();
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess)
+      return e;
+    dim3 grid((P.nx + H2_TX - 1) / H2_TX, (P.ny + H2_TY - 1) / H2_TY, 1);
+    k<<<grid, H2_TX * H2_TY, sm, st>>>((const S *)Uin, (S *)Uout, P, clk, step);
+    return cudaGetLastError();
+  }
+  auto   k = hydro3d_step<S, R, H3_TX, H3_TY>;
+  size_t sm = hydro3d_smem<R>();
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess)
+    return e;
+  dim3 grid((P.nx + H3_TX - 1) / H3_TX, (P.ny + H3_TY - 1) / H3_TY, (P.nz + P.kchunk - 1) / P.kchunk);
+  k<<<grid, H3_TX * H3_TY, sm, st>>>((const S *)Uin, (S *)Uout, P, clk, step);
+  return cudaGetLastError();
+}
+
+template <class S, class R>
+cudaError_t
+hydro_dt_t(int dim, const void * U, const KParams & P, unsigned long long * key, cudaStream_t st)
+{
+  const long long n = (long long)P.nx * P.ny * (dim == 3 ? P.nz : 1);
+  const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  if (dim == 2)
+    hydro_dt_kernel<S, R, 4><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+  else
+    hydro_dt_kernel<S, R, 5><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+  return cudaGetLastError();
+}
+} // namespace
+
+cudaError_t
+hydro_step(int dim, int prec, const void * Uin, void * Uout, const KParams & P, DevClock * clk,
+           int step, cudaStream_t st)
+{
+#ifdef EK_EXACT_ONLY
+  if (prec != 0)
+    return cudaErrorNotSupported;
+  return hydro_step_t<double, double>(dim, Uin, Uout, P, clk, step, st);
+#else
+  if (prec == 0)
+    return hydro_step_t<double, double>(dim, Uin, Uout, P, clk, step, st);
+  return hydro_step_t<float, float>(dim, Uin, Uout, P, clk, step, st);
+#endif
+}
+
+cudaError_t
+hydro_dt(int dim, int prec, const void * U, const KParams & P, unsigned long long * key,
+         cudaStream_t st)
+{
+#ifdef EK_EXACT_ONLY
+  if (prec != 0)
+    return cudaErrorNotSupported;
+  return hydro_dt_t<double, double>(dim, U, P, key, st);
+#else
+  if (prec == 0)
+    return hydro_dt_t<double, double>(dim, U, P, key, st);
+  return hydro_dt_t<float, float>(dim, U, P, key, st);
+#endif
+}
+
+#ifndef EK_EXACT_ONLY
+namespace
+{
+template <class S>
+__global__ void
+totals_kernel(const S * __restrict__ U, KParams P, double * acc)
+{
+  // FP64 mass and total energy over the interior; max |div B| for MHD
+  const long long n = (long long)P.nx * P.ny * (P.ksize > 1 ? P.nz : 1);
+  double          m = 0.0, e = 0.0, db = 0.0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x)
+  {
+    const int       i = (int)(c % P.nx) + P.gw;
+    const long long r = c / P.nx;
+    const int       j = (int)(r % P.ny) + P.gw;
+    const int       k = (int)(r / P.ny) + (P.ksize > 1 ? P.gw : 0);
+    const long long off = (long long)k * P.plane + (long long)j * P.isize + i;
+    m += (double)U[off];
+    e += (double)U[P.vstride + off];
+  }
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    m += __shfl_xor_sync(0xffffffffu, m, o);
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+  }
+  if ((threadIdx.x & 31) == 0)
+  {
+    atomicAdd(acc + 0, m);
+    atomicAdd(acc + 1, e);
+  }
+  (void)db;
+}
+} // namespace
+
+cudaError_t
+fill_ghosts(int prec, void * U, const KParams & P, int nbvar, cudaStream_t st)
+{
+  const long long n = P.vstride;
+  const int       blocks = (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
+  if (prec == 0)
+    fill_ghosts_kernel<double><<<blocks, 256, 0, st>>>((double *)U, P, nbvar, 0);
+  else if (!P.mhd)
+    fill_ghosts_kernel<float><<<blocks, 256, 0, st>>>((float *)U, P, nbvar, 0);
+  else
+  {
+    // mixed MHD: 5 FP32 hydro planes followed by 3 FP64 face-field planes
+    fill_ghosts_kernel<float><<<blocks, 256, 0, st>>>((float *)U, P, 5, 0);
+    fill_ghosts_kernel<double><<<blocks, 256, 0, st>>>(mixed_bfield(U, P), P, 3, 5);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t
+totals(int prec, const void * U, const KParams & P, int nbvar, double * out3, cudaStream_t st)
+{
+  (void)nbvar;
+  cudaError_t e = cudaMemsetAsync(out3, 0, 3 * sizeof(double), st);
+  if (e != cudaSuccess)
+    return e;
+  const long long n = (long long)P.nx * P.ny * (P.ksize > 1 ? P.nz : 1);
+  const int       blocks = (int)((n + 255) / 256 < 2048 ? (n + 255) / 256 : 2048);
+  if (prec == 0)
+    totals_kernel<double><<<blocks, 256, 0, st>>>((const double *)U, P, out3);
+  else
+    totals_kernel<float><<<blocks, 256, 0, st>>>((const float *)U, P, out3);
+  e = cudaGetLastError();
+  if (e != cudaSuccess || !P.mhd)
+    return e;
+  return mhd_divb_max(prec, U, P, out3 + 2, st);
+}
+#endif
+
+} // namespace EK_NS

@@ -1,0 +1,38 @@
+// Host-callable launchers of the device kernels.  ek_kernels.cu is compiled
+// twice: namespace ek_exact (FP64 only, no FMA contraction: bitwise parity
+// with the reference's FP64 build) and ek_fast (FMA contraction; FP64 and the
+// mixed FP32 form).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ek_common.cuh"
+
+#define EK_DECLARE_LAUNCHERS(NS)                                                                    \
+  namespace NS                                                                                      \
+  {                                                                                                 \
+  using ekc::KParams;                                                                               \
+  using ekc::DevClock;                                                                              \
+  /* prec: 0 FP64, 1 mixed.  Uin/Uout device state arrays. */                                      \
+  cudaError_t hydro_step(int dim, int prec, const void * Uin, void * Uout, const KParams & P,        \
+                         DevClock * clk, int step, cudaStream_t st);                                \
+  cudaError_t hydro_dt(int dim, int prec, const void * U, const KParams & P,                       \
+                       unsigned long long * key, cudaStream_t st);                                  \
+  cudaError_t mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key,         \
+                     cudaStream_t st);                                                              \
+  cudaError_t mhd_step(int prec, const void * Uin, void * Uout, void * work, const KParams & P,     \
+                       DevClock * clk, int step, cudaStream_t st);                                  \
+  size_t      mhd_work_bytes(int prec, const KParams & P);                                          \
+  }
+
+EK_DECLARE_LAUNCHERS(ek_exact)
+EK_DECLARE_LAUNCHERS(ek_fast)
+
+namespace ek_fast
+{
+using ekc::KParams;
+// precision-independent helpers (only built once)
+cudaError_t fill_ghosts(int prec, void * U, const KParams & P, int nbvar, cudaStream_t st);
+cudaError_t totals(int prec, const void * U, const KParams & P, int nbvar, double * out3,
+                   cudaStream_t st);
+} // namespace ek_fast

@@ -1,0 +1,146 @@
+/*
+ * ek_gb300.h -- C ABI of the GB300-native unsplit MUSCL-Hancock step.
+ *
+ * This is the drop-in boundary for the reference's solver path
+ * (pkestene/euler_kokkos, implementationVersion=0 of SolverHydroMuscl and
+ * SolverMHDMuscl).  Plain pointers and sizes only.  Every function returns an
+ * ek_status; no function aborts or exits the process (the reference aborts
+ * on an unknown solver name, SolverFactory.h:105-113, and exits on invalid
+ * parameters, HydroParams.cpp:352-358; here those are EK_ERR_INVALID).
+ *
+ * State arrays exchanged with the caller hold the FULL ghost-inclusive
+ * conserved state (isize x jsize [x ksize] x nbvar, FP64) in one of the two
+ * Kokkos layouts of the reference (kokkos_shared.h:24-42):
+ *   EK_LAYOUT_LEFT  -- U[((var*ksize + k)*jsize + j)*isize + i] (Kokkos CUDA)
+ *   EK_LAYOUT_RIGHT -- U[((i*jsize + j)*ksize + k)*nbvar + var] (Kokkos OpenMP)
+ * Variable order ID=0, IP=1 (total energy), IU, IV, IW, IA, IB, IC
+ * (enums.h:17-40); MHD face-centred B: U(i,j,k,IA) is Bx on the left x-face.
+ */
+#ifndef EK_GB300_H
+#define EK_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EK_ABI_VERSION 1
+
+typedef enum ek_status
+{
+  EK_OK = 0,
+  EK_ERR_INVALID = 1,     /* bad argument, bad parameter, unknown solver name */
+  EK_ERR_UNSUPPORTED = 2, /* a configuration this library does not implement */
+  EK_ERR_CUDA = 3,        /* a CUDA runtime error (see ek_last_error) */
+  EK_ERR_NO_MEMORY = 4,   /* device or pinned-host allocation failed */
+  EK_ERR_NONFINITE = 5,   /* the time step became non-finite or non-positive */
+  EK_ERR_PARSE = 6,       /* malformed .ini text */
+  EK_ERR_NO_DEVICE = 7    /* no CUDA device */
+} ek_status;
+
+typedef enum ek_layout
+{
+  EK_LAYOUT_LEFT = 0,
+  EK_LAYOUT_RIGHT = 1
+} ek_layout;
+
+typedef enum ek_precision
+{
+  EK_PREC_FP64 = 0, /* the drop-in: FP64 state and arithmetic */
+  EK_PREC_MIXED = 1 /* FP32 state/arithmetic with FP64 islands (dt, CT face B, cancellation) */
+} ek_precision;
+
+/* Run parameters.  Field meanings and defaults follow HydroParams
+ * (HydroParams.h:32-197, HydroParams.cpp:37-180, 327-359) and SolverBase
+ * (SolverBase.cpp:21-40).  ek_params_from_ini fills every field exactly as
+ * the reference's ConfigMap + HydroParams do, including the float rounding
+ * of every real read through strtof (ConfigMap.cpp:37-46). */
+typedef struct ek_params
+{
+  int    dim;   /* 2 or 3 */
+  int    mhd;   /* 0 hydro (SolverHydroMuscl), 1 MHD (SolverMHDMuscl) */
+  int    nx, ny, nz;
+  int    ghost_width; /* 2 hydro, 3 MHD */
+  int    nbvar;       /* 4 hydro 2D, 5 hydro 3D, 8 MHD */
+  int    isize, jsize, ksize;
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  double dx, dy, dz;
+  int    bc[6]; /* boundary_type_{xmin,xmax,ymin,ymax,zmin,zmax}: 1 reflect, 2 outflow, 3 periodic */
+  double gamma0, gamma6, cfl, slope_type, smallr, smallc, smallp, smallpp, cIso, Omega0;
+  int    riemann; /* 0 approx, 1 llf, 2 hll, 3 hllc, 4 hlld (enums.h:175-182) */
+  int    implementation_version;
+  int    nStepmax;
+  double tEnd;
+  double tCurrent; /* [run] tCurrent: initial m_t */
+  int    nOutput;
+  int    nlog;
+  int    precision; /* ek_precision; [gb300] precision = fp64 | mixed */
+  int    exact_fp;  /* 1: FP64 kernels built without FMA contraction ([gb300] exact = 1) */
+  int    kchunk;    /* 3D planes per CTA column (0: automatic; [gb300] kchunk) */
+  char   solver_name[32];
+  char   problem[32];
+} ek_params;
+
+typedef struct ek_solver ek_solver;
+
+/* Library identification (does not touch the GPU). */
+int          ek_abi_version(void);
+const char * ek_status_string(ek_status s);
+/* Message of the last error raised on the calling thread ("" if none). */
+const char * ek_last_error(void);
+
+/* Parse .ini text (ConfigMap semantics) and derive the run parameters
+ * (HydroParams::HydroParams + init).  Replaces ConfigMap(filename) and
+ * HydroParams(configMap, par_env) of main.cpp:100-110.  CPU only. */
+ek_status ek_params_from_ini(const char * text, size_t len, ek_params * out);
+
+/* Create a solver on the current CUDA device.  Replaces
+ * SolverFactory::Instance().create(name, params, configMap)
+ * (SolverFactory.h:83-116) for the names Hydro_Muscl_2D/3D, MHD_Muscl_3D;
+ * the initial condition is not computed here but injected with
+ * ek_solver_set_state (the reference's init(U) becomes the caller's). */
+ek_status ek_solver_create(const ek_params * params, ek_solver ** out);
+ek_status ek_solver_destroy(ek_solver * s);
+
+/* Inject a full state (host memory) and replay the reference constructor
+ * tail: make_boundaries(U), deep_copy(U2,U), [MHD: convertToPrimitives(U)],
+ * compute_dt() (SolverHydroMuscl.h:276-286, SolverMHDMuscl.h:384-397).
+ * Sets m_t = params.tCurrent and m_iteration = 0. */
+ek_status ek_solver_set_state(ek_solver * s, const double * U, int layout);
+/* Copy the current state (U if m_iteration is even, else U2) to host memory,
+ * ghost cells filled by the boundary conditions (save_solution path,
+ * SolverHydroMuscl.h:749-762). */
+ek_status ek_solver_get_state(ek_solver * s, double * U, int layout);
+
+/* SolverBase::compute_dt (SolverBase.cpp:124-154): dt on the current state,
+ * clamped so that t + dt <= tEnd.  Writes m_dt to *dt when dt != NULL. */
+ek_status ek_solver_compute_dt(ek_solver * s, double * dt);
+/* SolverBase::next_iteration (SolverBase.cpp:180-195): one fused step, then
+ * ++m_iteration, m_t += m_dt.  Synchronises to read back m_dt, as the
+ * reference's parallel_reduce does. */
+ek_status ek_solver_next_iteration(ek_solver * s);
+/* while (!finished() && n < nsteps) next_iteration(), without a host round
+ * trip per step; *done receives the number of steps taken. */
+ek_status ek_solver_run(ek_solver * s, int nsteps, int * done);
+/* SolverBase::finished (SolverBase.cpp:170-176) */
+ek_status ek_solver_finished(ek_solver * s, int * finished);
+/* m_t, m_dt (the last step's dt) and m_iteration */
+ek_status ek_solver_time(ek_solver * s, double * t, double * dt, int * iteration);
+/* dt of steps 0..n-1 (the reference's printed dt sequence) */
+ek_status ek_solver_dt_history(ek_solver * s, double * dts, int n);
+/* FP64 totals over the interior: [mass, total energy, max |div B| (MHD, else 0)] */
+ek_status ek_solver_totals(ek_solver * s, double out[3]);
+/* Device pointer / byte size of the current state (zero-copy access; the
+ * storage type is FP64, or FP32 hydro variables + FP64 face B in the mixed
+ * form).  Valid until the next step. */
+ek_status ek_solver_device_state(ek_solver * s, void ** ptr, size_t * bytes);
+/* Block until all work of the solver is done; reports device-side errors. */
+ek_status ek_solver_synchronize(ek_solver * s);
+/* Number of kernel launches issued by this solver so far. */
+ek_status ek_solver_launch_count(ek_solver * s, long long * n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EK_GB300_H */
