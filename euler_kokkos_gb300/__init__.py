@@ -195,7 +195,10 @@ class Solver:
         _check(self._L.ek_solver_set_state(self._h, U.ctypes.data, layout), "set_state")
 
     def get_state(self, layout: int = EK_LAYOUT_LEFT) -> np.ndarray:
-        U = np.empty(self.params.shape, dtype=np.float64)
+        """Current state: shape (nbvar, ksize, jsize, isize) for LayoutLeft,
+        (isize, jsize, ksize, nbvar) for LayoutRight."""
+        shp = self.params.shape
+        U = np.empty(shp if layout == EK_LAYOUT_LEFT else shp[::-1], dtype=np.float64)
         _check(self._L.ek_solver_get_state(self._h, U.ctypes.data, layout), "get_state")
         return U
 

@@ -351,7 +351,9 @@ reset_clock(ek_solver * s, double t0)
   {
     h.key[i] = EK_KEY_LOWEST;
     h.t[i] = 0.0;
+    h.sid[i] = -1;
   }
+  h.sid[0] = 0;
   h.t[0] = t0;
   h.iteration = 0;
   h.error = 0;
@@ -592,6 +594,15 @@ ek_solver_totals(ek_solver * s, double out[3])
   s->launches += s->p.mhd ? 2 : 1;
   EK_CUDA(cudaMemcpyAsync(out, s->scratch3, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream), "totals");
   EK_CUDA(cudaStreamSynchronize(s->stream), "totals");
+  if (s->p.mhd)
+  {
+    // the device wrote an order-preserving key of max |div B|
+    unsigned long long key;
+    std::memcpy(&key, &out[2], sizeof key);
+    out[2] = ekc::dkey_inv(key);
+  }
+  else
+    out[2] = 0.0;
   const double cell = s->p.dx * s->p.dy * (s->p.dim == 3 ? s->p.dz : 1.0);
   out[0] *= cell;
   out[1] *= cell;

@@ -62,6 +62,7 @@ struct DevClock
 {
   unsigned long long key[3];
   double             t[3];
+  int                sid[3];    // step number the slot was written for
   int                iteration; // number of steps taken
   int                error;     // sticky device error flags
   double *           dtlog;     // dt of each step (capacity dtcap)
@@ -201,11 +202,16 @@ ldg(const T * p)
   return __ldg(p);
 }
 
-// dt at the start of a step, SolverBase::compute_dt (SolverBase.cpp:124-154)
-__device__ __forceinline__ void
+// dt at the start of a step, SolverBase::compute_dt (SolverBase.cpp:124-154).
+// Returns false when the step must not run: the simulation is finished
+// (SolverBase::finished, t >= tEnd - 1e-14, SolverBase.cpp:170-176) or an
+// earlier launched step did not run (its slot was never committed).
+__device__ __forceinline__ bool
 step_dt(const KParams & P, const DevClock * clk, int step, double * t, double * dt)
 {
-  const int    s = step % 3;
+  const int s = step % 3;
+  if (clk->sid[s] != step)
+    return false;
   const double invDt = dkey_inv(clk->key[s]);
   double       d = P.cfl / invDt;
   const double tt = clk->t[s];
@@ -213,6 +219,7 @@ step_dt(const KParams & P, const DevClock * clk, int step, double * t, double * 
     d = P.tEnd - tt;
   *t = tt;
   *dt = d;
+  return !(tt >= P.tEnd - 1e-14);
 }
 
 // bookkeeping done once per step by block 0, thread 0
@@ -220,6 +227,7 @@ __device__ __forceinline__ void
 step_commit(DevClock * clk, int step, double t, double dt)
 {
   clk->t[(step + 1) % 3] = t + dt;
+  clk->sid[(step + 1) % 3] = step + 1;
   clk->key[(step + 2) % 3] = EK_KEY_LOWEST;
   if (step < clk->dtcap)
     clk->dtlog[step] = dt;

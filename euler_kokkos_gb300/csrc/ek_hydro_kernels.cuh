@@ -92,8 +92,7 @@ hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   R * sYp = sYm + NV * (TY + 2) * TX;        // YMAX state
 
   double t, dt;
-  step_dt(P, clk, step, &t, &dt);
-  if (t >= P.tEnd - 1e-14)
+  if (!step_dt(P, clk, step, &t, &dt))
     return;
   const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy);
   const HydroConst<R> C = hydro_const<R>(P);
@@ -259,8 +258,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   R * sYp = sYm + NV * (TY + 2) * TX;
 
   double t, dt;
-  step_dt(P, clk, step, &t, &dt);
-  if (t >= P.tEnd - 1e-14)
+  if (!step_dt(P, clk, step, &t, &dt))
     return;
   const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy), dtdz = (R)(dt / P.dz);
   const HydroConst<R> C = hydro_const<R>(P);

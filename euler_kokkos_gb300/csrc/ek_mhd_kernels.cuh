@@ -1,26 +1,802 @@
-// CT-MHD 3D step kernels (in progress).
+// CT-MHD 3D step (SolverMHDMuscl<3>::godunov_unsplit_impl v0,
+// SolverMHDMuscl.cpp:461-505) in three launches:
+//   1. mhd_dt_kernel     primitive variables of the boundary-mapped state and
+//                        the CFL max-reduction (ComputeDtFunctor3D_MHD); the
+//                        reference computes MHD dt inside the step, after the
+//                        ghost fill (SolverMHDMuscl.cpp:479-484)
+//   2. mhd_trace_kernel  z-marching: face-field planes, primitive planes and
+//                        edge electric fields in shared memory, limited
+//                        slopes, CT half-step trace -> 47 numbers per cell
+//   3. mhd_update_kernel z-marching: HLLD fluxes (3 faces), 2D-HLLD emfs
+//                        (3 edges), conservative update and CT update of the
+//                        face fields, all from the compact trace
+// The state is read from HBM in 1 and 2 and written once in 3.
 #pragma once
-#include "ek_common.cuh"
+
+#include "ek_mhd.cuh"
+
 namespace EK_NS
 {
-cudaError_t
-mhd_dt(int, const void *, const KParams &, unsigned long long *, cudaStream_t)
+
+template <class R>
+__device__ __forceinline__ MhdConst<R>
+mhd_const(const KParams & P)
 {
-  return cudaErrorNotSupported;
+  MhdConst<R> C;
+  C.gamma0 = (R)P.gamma0;
+  C.smallr = (R)P.smallr;
+  C.smallp = (R)P.smallp;
+  C.smallc = (R)P.smallc;
+  C.slope_type = (R)P.slope_type;
+  return C;
 }
-cudaError_t
-mhd_step(int, const void *, void *, void *, const KParams &, DevClock *, int, cudaStream_t)
+
+// state accessors: hydro planes of type S, face-field planes always FP64
+template <class S>
+struct MhdState
 {
-  return cudaErrorNotSupported;
+  const S *      h; // 5 hydro planes
+  const double * b; // 3 face-field planes
+};
+template <class S>
+__device__ __forceinline__ MhdState<S>
+mhd_state(const void * U, const KParams & P)
+{
+  MhdState<S> m;
+  m.h = (const S *)U;
+  if constexpr (sizeof(S) == 8)
+    m.b = (const double *)U + 5 * P.vstride;
+  else
+    m.b = mixed_bfield(U, P);
+  return m;
 }
+
+// hydro variables of a (mapped) cell, reflect flips applied
+template <class S, class R>
+__device__ __forceinline__ void
+load_hydro(const MhdState<S> & m, const KParams & P, const SrcCell & s, R (&u)[5])
+{
+#pragma unroll
+  for (int v = 0; v < 5; ++v)
+  {
+    const R x = (R)ldg(m.h + v * P.vstride + s.off);
+    u[v] = flips(s, v, 1) ? -x : x;
+  }
+}
+template <class S>
+__device__ __forceinline__ double
+load_face(const MhdState<S> & m, const KParams & P, const SrcCell & s, int comp)
+{
+  const double x = ldg(m.b + comp * P.vstride + s.off);
+  return flips(s, IA + comp, 1) ? -x : x;
+}
+
+// primitive state of cell (gi,gj,gk): constoprim with the face fields of the
+// cell and of its +1 neighbours (ConvertToPrimitivesFunctor3D_MHD)
+template <class S, class R>
+__device__ __forceinline__ void
+cell_prims_global(const MhdState<S> & m, const KParams & P, const MhdConst<R> & C, int gi, int gj,
+                  int gk, R (&q)[8])
+{
+  const SrcCell s = src_cell(P, gi, gj, gk);
+  R             u[5];
+  load_hydro<S, R>(m, P, s, u);
+  double bl[3], br[3];
+  bl[0] = load_face<S>(m, P, s, 0);
+  bl[1] = load_face<S>(m, P, s, 1);
+  bl[2] = load_face<S>(m, P, s, 2);
+  br[0] = load_face<S>(m, P, src_cell(P, gi + 1, gj, gk), 0);
+  br[1] = load_face<S>(m, P, src_cell(P, gi, gj + 1, gk), 1);
+  br[2] = load_face<S>(m, P, src_cell(P, gi, gj, gk + 1), 2);
+  mhd_constoprim<R>(u, bl, br, q, C);
+}
+
+// ---------------------------------------------------------------------------
+// 1. CFL reduction of the step (on the primitive variables of the input)
+// ---------------------------------------------------------------------------
+template <class S, class R>
+__global__ void __launch_bounds__(256)
+mhd_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step,
+              unsigned long long * key)
+{
+  if (clk)
+  {
+    // a step that must not run (finished, or an earlier one did not run)
+    const int s = step % 3;
+    if (clk->sid[s] != step || clk->t[s] >= P.tEnd - 1e-14)
+      return;
+  }
+  const MhdState<S>  m = mhd_state<S>(U, P);
+  const MhdConst<R>  C = mhd_const<R>(P);
+  const long long    n = (long long)P.nx * P.ny * P.nz;
+  unsigned long long kmax = 0ull;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x)
+  {
+    const int       i = (int)(c % P.nx) + P.gw;
+    const long long r = c / P.nx;
+    const int       j = (int)(r % P.ny) + P.gw;
+    const int       k = (int)(r / P.ny) + P.gw;
+    R               q[8];
+    cell_prims_global<S, R>(m, P, C, i, j, k, q);
+    const unsigned long long kk = cand_key(mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz));
+    kmax = kk > kmax ? kk : kmax;
+  }
+  block_max_commit<256>(kmax, key ? key : &clk->key[step % 3]);
+}
+
+// ---------------------------------------------------------------------------
+// 2. trace kernel
+// ---------------------------------------------------------------------------
+// Tile of trace cells [c0, c0+TX) x [d0, d0+TY) (global indices), marching
+// over planes [k0, k1).  Shared planes (x extent / y extent):
+//   sB  face fields, 4 planes (k-1..k+2), x in [c0-1, c0+TX+1], y in [d0-1, d0+TY+1]
+//   sQ  primitives,  3 planes (k-1..k+1), x in [c0-1, c0+TX],   y in [d0-1, d0+TY]
+//   sE  edge fields, 2 planes (k, k+1),   x in [c0,   c0+TX],   y in [d0,   d0+TY]
+template <int TX, int TY>
+struct TraceTile
+{
+  static constexpr int BX = TX + 3, BY = TY + 3, BP = 3 * BX * BY;
+  static constexpr int QX = TX + 2, QY = TY + 2, QP = 8 * QX * QY;
+  static constexpr int EX = TX + 1, EY = TY + 1, EP = 3 * EX * EY;
+};
+
+template <class R, int TX, int TY>
+__device__ __forceinline__ void
+trace_cell_compact(const double * sB, int bslot[4], const R * sQ, int qslot[3], const R * sE,
+                   int eslot[2], int tx, int ty, R dtdx, R dtdy, R dtdz, const MhdConst<R> & C,
+                   R * out, long long ost)
+{
+  using T = TraceTile<TX, TY>;
+  // local tile coordinates of the cell in each buffer
+  const int qx = tx + 1, qy = ty + 1; // sQ
+  const int bx = tx + 1, by = ty + 1; // sB
+  const int ex = tx, ey = ty;         // sE
+  const R * Q0 = sQ + qslot[1] * T::QP;
+  const R * Qm = sQ + qslot[0] * T::QP;
+  const R * Qp = sQ + qslot[2] * T::QP;
+  auto Qv = [&](const R * pl, int v, int x, int y) { return pl[(v * T::QY + y) * T::QX + x]; };
+  auto Bv = [&](int slot, int comp, int x, int y) {
+    return sB[bslot[slot] * T::BP + (comp * T::BY + y) * T::BX + x];
+  };
+  auto Ev = [&](int slot, int comp, int x, int y) {
+    return sE[eslot[slot] * T::EP + (comp * T::EY + y) * T::EX + x];
+  };
+
+  // hydro slopes (slope_unsplit_hydro_3d, MHDBaseFunctor3D.h:340-470); the
+  // z-slope of IC uses qMinusY as the reference does (unused by the trace)
+  R q[8], dq[3][8];
+#pragma unroll
+  for (int v = 0; v < 8; ++v)
+    q[v] = Qv(Q0, v, qx, qy);
+  if (C.slope_type == R(1) || C.slope_type == R(2))
+  {
+#pragma unroll
+    for (int v = 0; v < 8; ++v)
+    {
+      dq[0][v] = slope1<R>(q[v], Qv(Q0, v, qx + 1, qy), Qv(Q0, v, qx - 1, qy), C.slope_type);
+      dq[1][v] = slope1<R>(q[v], Qv(Q0, v, qx, qy + 1), Qv(Q0, v, qx, qy - 1), C.slope_type);
+      dq[2][v] = slope1<R>(q[v], Qv(Qp, v, qx, qy), v == IC ? Qv(Q0, v, qx, qy - 1) : Qv(Qm, v, qx, qy),
+                           C.slope_type);
+    }
+  }
+  else
+  {
+#pragma unroll
+    for (int v = 0; v < 8; ++v)
+      dq[0][v] = dq[1][v] = dq[2][v] = R(0);
+  }
+  // face fields of the cell (bfNb, MHDRunFunctors3D.h:790-795); planes: 0 k-1, 1 k, 2 k+1
+  const R AL = (R)Bv(1, 0, bx, by), AR = (R)Bv(1, 0, bx + 1, by);
+  const R BL = (R)Bv(1, 1, bx, by), BR = (R)Bv(1, 1, bx, by + 1);
+  const R CL = (R)Bv(1, 2, bx, by), CR = (R)Bv(2, 2, bx, by);
+  // transverse face-field slopes (slope_unsplit_mhd_3d, MHDBaseFunctor3D.h:563-668)
+  const R xst = fmin(C.slope_type, R(2.0));
+  auto    sA = [&](int x, int y, bool zdir) {
+    const R b = (R)Bv(1, 0, x, y);
+    return zdir ? slope1<R>(b, (R)Bv(2, 0, x, y), (R)Bv(0, 0, x, y), xst)
+                   : slope1<R>(b, (R)Bv(1, 0, x, y + 1), (R)Bv(1, 0, x, y - 1), xst);
+  };
+  auto sBf = [&](int x, int y, bool zdir) {
+    const R b = (R)Bv(1, 1, x, y);
+    return zdir ? slope1<R>(b, (R)Bv(2, 1, x, y), (R)Bv(0, 1, x, y), xst)
+                : slope1<R>(b, (R)Bv(1, 1, x + 1, y), (R)Bv(1, 1, x - 1, y), xst);
+  };
+  auto sC = [&](int slot, int x, int y, bool ydir) {
+    const R b = (R)Bv(slot, 2, x, y);
+    return ydir ? slope1<R>(b, (R)Bv(slot, 2, x, y + 1), (R)Bv(slot, 2, x, y - 1), xst)
+                : slope1<R>(b, (R)Bv(slot, 2, x + 1, y), (R)Bv(slot, 2, x - 1, y), xst);
+  };
+  R dbf[12];
+  dbf[0] = sA(bx, by, false);      // DeltaA(i,j,k).y
+  dbf[1] = sA(bx, by, true);       // DeltaA(i,j,k).z
+  dbf[2] = sBf(bx, by, false);     // DeltaB(i,j,k).x
+  dbf[3] = sBf(bx, by, true);      // DeltaB(i,j,k).z
+  dbf[4] = sC(1, bx, by, false);   // DeltaC(i,j,k).x
+  dbf[5] = sC(1, bx, by, true);    // DeltaC(i,j,k).y
+  dbf[6] = sA(bx + 1, by, false);  // DeltaA(i+1,j,k).y
+  dbf[7] = sA(bx + 1, by, true);   // DeltaA(i+1,j,k).z
+  dbf[8] = sBf(bx, by + 1, false); // DeltaB(i,j+1,k).x
+  dbf[9] = sBf(bx, by + 1, true);  // DeltaB(i,j+1,k).z
+  dbf[10] = sC(2, bx, by, false);  // DeltaC(i,j,k+1).x
+  dbf[11] = sC(2, bx, by, true);   // DeltaC(i,j,k+1).y
+  // edge electric fields around the cell (MHDRunFunctors3D.h:808-823)
+  const R ELL = Ev(0, 0, ex, ey), ELR = Ev(1, 0, ex, ey), ERL = Ev(0, 0, ex, ey + 1),
+          ERR = Ev(1, 0, ex, ey + 1);
+  const R FLL = Ev(0, 1, ex, ey), FLR = Ev(1, 1, ex, ey), FRL = Ev(0, 1, ex + 1, ey),
+          FRR = Ev(1, 1, ex + 1, ey);
+  const R GLL = Ev(0, 2, ex, ey), GLR = Ev(0, 2, ex, ey + 1), GRL = Ev(0, 2, ex + 1, ey),
+          GRR = Ev(0, 2, ex + 1, ey + 1);
+
+  // trace_unsplit_mhd_3d_simpler (MHDBaseFunctor3D.h:751-917), Omega0 = 0
+  R r = q[ID], p = q[IP], u = q[IU], v = q[IV], w = q[IW], A = q[IA], B = q[IB], Cc = q[IC];
+  const R drx = dq[0][ID] * R(0.5), dpx = dq[0][IP] * R(0.5), dux = dq[0][IU] * R(0.5),
+          dvx = dq[0][IV] * R(0.5), dwx = dq[0][IW] * R(0.5), dCx = dq[0][IC] * R(0.5),
+          dBx = dq[0][IB] * R(0.5);
+  const R dry = dq[1][ID] * R(0.5), dpy = dq[1][IP] * R(0.5), duy = dq[1][IU] * R(0.5),
+          dvy = dq[1][IV] * R(0.5), dwy = dq[1][IW] * R(0.5), dCy = dq[1][IC] * R(0.5),
+          dAy = dq[1][IA] * R(0.5);
+  const R drz = dq[2][ID] * R(0.5), dpz = dq[2][IP] * R(0.5), duz = dq[2][IU] * R(0.5),
+          dvz = dq[2][IV] * R(0.5), dwz = dq[2][IW] * R(0.5), dAz = dq[2][IA] * R(0.5),
+          dBz = dq[2][IB] * R(0.5);
+  const R dALy = R(0.5) * dbf[0], dALz = R(0.5) * dbf[1], dBLx = R(0.5) * dbf[2],
+          dBLz = R(0.5) * dbf[3], dCLx = R(0.5) * dbf[4], dCLy = R(0.5) * dbf[5];
+  const R dARy = R(0.5) * dbf[6], dARz = R(0.5) * dbf[7], dBRx = R(0.5) * dbf[8],
+          dBRz = R(0.5) * dbf[9], dCRx = R(0.5) * dbf[10], dCRy = R(0.5) * dbf[11];
+  const R dAx = R(0.5) * (AR - AL);
+  const R dBy = R(0.5) * (BR - BL);
+  const R dCz = R(0.5) * (CR - CL);
+  const R gamma = C.gamma0;
+  const R C_ = Cc;
+  const R sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
+  const R su0 = (-u * dux - (dpx + B * dBx + C_ * dCx) / r) * dtdx + (-v * duy + B * dAy / r) * dtdy +
+                (-w * duz + C_ * dAz / r) * dtdz;
+  const R sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - (dpy + A * dAy + C_ * dCy) / r) * dtdy +
+                (-w * dvz + C_ * dBz / r) * dtdz;
+  const R sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + B * dCy / r) * dtdy +
+                (-w * dwz - (dpz + A * dAz + B * dBz) / r) * dtdz;
+  const R sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
+                (-w * dpz - dwz * gamma * p) * dtdz;
+  const R sA0 = (u * dBy + B * duy - v * dAy - A * dvy) * dtdy + (u * dCz + C_ * duz - w * dAz - A * dwz) * dtdz;
+  const R sB0 = (v * dAx + A * dvx - u * dBx - B * dux) * dtdx + (v * dCz + C_ * dvz - w * dBz - B * dwz) * dtdz;
+  const R sC0 = (w * dAx + A * dwx - u * dCx - C_ * dux) * dtdx + (w * dBy + B * dwy - v * dCy - C_ * dvy) * dtdy;
+  const R sAL0 = +(GLR - GLL) * dtdy * R(0.5) - (FLR - FLL) * dtdz * R(0.5);
+  const R sAR0 = +(GRR - GRL) * dtdy * R(0.5) - (FRR - FRL) * dtdz * R(0.5);
+  const R sBL0 = -(GRL - GLL) * dtdx * R(0.5) + (ELR - ELL) * dtdz * R(0.5);
+  const R sBR0 = -(GRR - GLR) * dtdx * R(0.5) + (ERR - ERL) * dtdz * R(0.5);
+  const R sCL0 = +(FRL - FLL) * dtdx * R(0.5) - (ERL - ELL) * dtdy * R(0.5);
+  const R sCR0 = +(FRR - FLR) * dtdx * R(0.5) - (ERR - ELR) * dtdy * R(0.5);
+
+  R o[T_N];
+  o[T_R] = r + sr0;
+  o[T_U] = u + su0;
+  o[T_V] = v + sv0;
+  o[T_W] = w + sw0;
+  o[T_P] = p + sp0;
+  o[T_A] = A + sA0;
+  o[T_B] = B + sB0;
+  o[T_C] = C_ + sC0;
+  o[T_AL] = AL + sAL0;
+  o[T_AR] = AR + sAR0;
+  o[T_BL] = BL + sBL0;
+  o[T_BR] = BR + sBR0;
+  o[T_CL] = CL + sCL0;
+  o[T_CR] = CR + sCR0;
+  o[T_DRX] = drx, o[T_DPX] = dpx, o[T_DUX] = dux, o[T_DVX] = dvx, o[T_DWX] = dwx, o[T_DBX] = dBx,
+  o[T_DCX] = dCx;
+  o[T_DRY] = dry, o[T_DPY] = dpy, o[T_DUY] = duy, o[T_DVY] = dvy, o[T_DWY] = dwy, o[T_DAY] = dAy,
+  o[T_DCY] = dCy;
+  o[T_DRZ] = drz, o[T_DPZ] = dpz, o[T_DUZ] = duz, o[T_DVZ] = dvz, o[T_DWZ] = dwz, o[T_DAZ] = dAz,
+  o[T_DBZ] = dBz;
+  o[T_DALY] = dALy, o[T_DALZ] = dALz, o[T_DBLX] = dBLx, o[T_DBLZ] = dBLz, o[T_DCLX] = dCLx,
+  o[T_DCLY] = dCLy;
+  o[T_DARY] = dARy, o[T_DARZ] = dARz, o[T_DBRX] = dBRx, o[T_DBRZ] = dBRz, o[T_DCRX] = dCRx,
+  o[T_DCRY] = dCRy;
+#pragma unroll
+  for (int f = 0; f < T_N; ++f)
+    out[f * ost] = o[f];
+}
+
+template <class S, class R, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY)
+mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P, DevClock * clk,
+                 int step)
+{
+  using T = TraceTile<TX, TY>;
+  constexpr int NT = TX * TY;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double * sB = reinterpret_cast<double *>(smem_raw);          // [4][3][BY][BX]
+  R *      sQ = reinterpret_cast<R *>(sB + 4 * T::BP);         // [3][8][QY][QX]
+  R *      sE = sQ + 3 * T::QP;                                // [2][3][EY][EX]
+
+  double t, dt;
+  if (!step_dt(P, clk, step, &t, &dt))
+    return;
+  const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy), dtdz = (R)(dt / P.dz);
+  const MhdConst<R>  C = mhd_const<R>(P);
+  const MhdState<S>  m = mhd_state<S>(U, P);
+  const int gw = P.gw;
+  // trace cells span global [gw-1, n+gw] in each direction
+  const int c0 = gw - 1 + blockIdx.x * TX, d0 = gw - 1 + blockIdx.y * TY;
+  const int k0 = gw - 1 + blockIdx.z * P.kchunk;
+  const int k1 = min(k0 + P.kchunk, P.nz + gw + 1);
+  const int nti = P.nx + 2, ntj = P.ny + 2; // trace cells per row / column
+
+  auto load_B = [&](int gk, int slot) {
+    double * dst = sB + slot * T::BP;
+    for (int c = threadIdx.x; c < T::BX * T::BY; c += NT)
+    {
+      const int     x = c % T::BX, y = c / T::BX;
+      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+#pragma unroll
+      for (int comp = 0; comp < 3; ++comp)
+        dst[(comp * T::BY + y) * T::BX + x] = load_face<S>(m, P, s, comp);
+    }
+  };
+  // primitives of plane gk from the hydro variables and the face planes
+  // bslot (gk) and bslot1 (gk+1)
+  auto load_Q = [&](int gk, int slot, int bs0, int bs1) {
+    R * dst = sQ + slot * T::QP;
+    const double * B0 = sB + bs0 * T::BP;
+    const double * B1 = sB + bs1 * T::BP;
+    for (int c = threadIdx.x; c < T::QX * T::QY; c += NT)
+    {
+      const int     x = c % T::QX, y = c / T::QX;
+      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+      R             u[5], q[8];
+      load_hydro<S, R>(m, P, s, u);
+      double bl[3], br[3];
+      // sB x index = global - (c0-1): the Q cell at x has B index x
+      bl[0] = B0[(0 * T::BY + y) * T::BX + x];
+      bl[1] = B0[(1 * T::BY + y) * T::BX + x];
+      bl[2] = B0[(2 * T::BY + y) * T::BX + x];
+      br[0] = B0[(0 * T::BY + y) * T::BX + x + 1];
+      br[1] = B0[(1 * T::BY + y + 1) * T::BX + x];
+      br[2] = B1[(2 * T::BY + y) * T::BX + x];
+      mhd_constoprim<R>(u, bl, br, q, C);
+#pragma unroll
+      for (int v = 0; v < 8; ++v)
+        dst[(v * T::QY + y) * T::QX + x] = q[v];
+    }
+  };
+  // edge electric fields of plane gk (ComputeElecFieldFunctor3D,
+  // MHDRunFunctors3D.h:318-356) from Q planes gk-1 (qs0), gk (qs1) and face
+  // planes gk-1 (bs0), gk (bs1)
+  auto compute_E = [&](int slot, int qs0, int qs1, int bs0, int bs1) {
+    R *            dst = sE + slot * T::EP;
+    const R *      Qa = sQ + qs0 * T::QP; // k-1
+    const R *      Qb = sQ + qs1 * T::QP; // k
+    const double * Ba = sB + bs0 * T::BP;
+    const double * Bb = sB + bs1 * T::BP;
+    for (int c = threadIdx.x; c < T::EX * T::EY; c += NT)
+    {
+      const int x = c % T::EX, y = c / T::EX; // E cell global = c0 + x
+      const int qx = x + 1, qy = y + 1;       // sQ index of the same cell
+      const int bx = x + 1, by = y + 1;       // sB index of the same cell
+      auto      Q = [&](const R * pl, int v, int xx, int yy) { return pl[(v * T::QY + yy) * T::QX + xx]; };
+      auto      Bf = [&](const double * pl, int comp, int xx, int yy) {
+        return (R)pl[(comp * T::BY + yy) * T::BX + xx];
+      };
+      R uu, vv, ww, A, B, Cc;
+      vv = R(0.25) * (Q(Qa, IV, qx, qy - 1) + Q(Qb, IV, qx, qy - 1) + Q(Qa, IV, qx, qy) + Q(Qb, IV, qx, qy));
+      ww = R(0.25) * (Q(Qa, IW, qx, qy - 1) + Q(Qb, IW, qx, qy - 1) + Q(Qa, IW, qx, qy) + Q(Qb, IW, qx, qy));
+      B = R(0.5) * (Bf(Ba, 1, bx, by) + Bf(Bb, 1, bx, by));
+      Cc = R(0.5) * (Bf(Bb, 2, bx, by - 1) + Bf(Bb, 2, bx, by));
+      dst[(0 * T::EY + y) * T::EX + x] = vv * Cc - ww * B;
+      uu = R(0.25) * (Q(Qa, IU, qx - 1, qy) + Q(Qb, IU, qx - 1, qy) + Q(Qa, IU, qx, qy) + Q(Qb, IU, qx, qy));
+      ww = R(0.25) * (Q(Qa, IW, qx - 1, qy) + Q(Qb, IW, qx - 1, qy) + Q(Qa, IW, qx, qy) + Q(Qb, IW, qx, qy));
+      A = R(0.5) * (Bf(Ba, 0, bx, by) + Bf(Bb, 0, bx, by));
+      Cc = R(0.5) * (Bf(Bb, 2, bx - 1, by) + Bf(Bb, 2, bx, by));
+      dst[(1 * T::EY + y) * T::EX + x] = ww * A - uu * Cc;
+      uu = R(0.25) * (Q(Qb, IU, qx - 1, qy - 1) + Q(Qb, IU, qx - 1, qy) + Q(Qb, IU, qx, qy - 1) + Q(Qb, IU, qx, qy));
+      vv = R(0.25) * (Q(Qb, IV, qx - 1, qy - 1) + Q(Qb, IV, qx - 1, qy) + Q(Qb, IV, qx, qy - 1) + Q(Qb, IV, qx, qy));
+      A = R(0.5) * (Bf(Bb, 0, bx, by - 1) + Bf(Bb, 0, bx, by));
+      B = R(0.5) * (Bf(Bb, 1, bx - 1, by) + Bf(Bb, 1, bx, by));
+      dst[(2 * T::EY + y) * T::EX + x] = uu * B - vv * A;
+    }
+  };
+
+  // ring slots: face planes by global k modulo 4, Q by k modulo 3, E by k modulo 2
+  auto bsl = [](int k) { return (k + 8) % 4; };
+  auto qsl = [](int k) { return (k + 6) % 3; };
+  auto esl = [](int k) { return (k + 4) % 2; };
+
+  // prologue: face planes k0-1..k0+1, Q(k0-1), Q(k0), E(k0)
+  load_B(k0 - 1, bsl(k0 - 1));
+  load_B(k0, bsl(k0));
+  load_B(k0 + 1, bsl(k0 + 1));
+  __syncthreads();
+  load_Q(k0 - 1, qsl(k0 - 1), bsl(k0 - 1), bsl(k0));
+  load_Q(k0, qsl(k0), bsl(k0), bsl(k0 + 1));
+  __syncthreads();
+  compute_E(esl(k0), qsl(k0 - 1), qsl(k0), bsl(k0 - 1), bsl(k0));
+
+  const int       tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  const bool      own = (c0 + tx) <= P.nx + gw && (d0 + ty) <= P.ny + gw && (c0 - (gw - 1) + tx) < nti &&
+                   (d0 - (gw - 1) + ty) < ntj;
+  const long long ost = P.vstride;
+  for (int k = k0; k < k1; ++k)
+  {
+    load_B(k + 2, bsl(k + 2));
+    __syncthreads();
+    load_Q(k + 1, qsl(k + 1), bsl(k + 1), bsl(k + 2));
+    __syncthreads();
+    compute_E(esl(k + 1), qsl(k), qsl(k + 1), bsl(k), bsl(k + 1));
+    __syncthreads();
+    if (own)
+    {
+      int bslot[4] = { bsl(k - 1), bsl(k), bsl(k + 1), bsl(k + 2) };
+      int qslot[3] = { qsl(k - 1), qsl(k), qsl(k + 1) };
+      int eslot[2] = { esl(k), esl(k + 1) };
+      const long long off = (long long)k * P.plane + (long long)(d0 + ty) * P.isize + (c0 + tx);
+      trace_cell_compact<R, TX, TY>(sB, bslot, sQ, qslot, sE, eslot, tx, ty, dtdx, dtdy, dtdz, C,
+                                    trace + off, ost);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3. fluxes, emfs and update
+// ---------------------------------------------------------------------------
+template <class S, class R, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY)
+mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
+                  KParams P, DevClock * clk, int step)
+{
+  constexpr int NT = TX * TY;
+  constexpr int FXS = (TX + 1) * TY, FYS = TX * (TY + 1);
+  constexpr int EZS = (TX + 1) * (TY + 1), EYS = (TX + 1) * TY, EXS = TX * (TY + 1);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R * sFx = reinterpret_cast<R *>(smem_raw); // [5][TY][TX+1]
+  R * sFy = sFx + 5 * FXS;                   // [5][TY+1][TX]
+  R * sEz = sFy + 5 * FYS;                   // [2][TY+1][TX+1]
+  R * sEy = sEz + 2 * EZS;                   // [2][TY][TX+1]
+  R * sEx = sEy + 2 * EYS;                   // [2][TY+1][TX]
+
+  double t, dt;
+  if (!step_dt(P, clk, step, &t, &dt))
+    return;
+  const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy), dtdz = (R)(dt / P.dz);
+  const double ddtdx = dt / P.dx, ddtdy = dt / P.dy, ddtdz = dt / P.dz;
+  const MhdConst<R> C = mhd_const<R>(P);
+  const int         gw = P.gw;
+  const int         i0 = gw + blockIdx.x * TX, j0 = gw + blockIdx.y * TY;
+  const int         k0 = gw + blockIdx.z * P.kchunk;
+  const int         k1 = min(k0 + P.kchunk, P.nz + gw);
+  const int         tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  const int         gi = i0 + tx, gj = j0 + ty;
+  const bool        own = gi < P.nx + gw && gj < P.ny + gw;
+  const long long   st = P.vstride;
+  const MhdState<S> mi = mhd_state<S>(Uin, P);
+  S *               hout = (S *)Uout;
+  double *          bout = sizeof(S) == 8 ? (double *)Uout + 5 * P.vstride : mixed_bfield(Uout, P);
+  const R           sr = C.smallr, sp = C.smallp;
+
+  auto T = [&](int i, int j, int k) { return trace + (long long)k * P.plane + (long long)j * P.isize + i; };
+  auto esl = [](int k) { return (k + 4) % 2; };
+
+  R                  acc[5];
+  unsigned long long kmax = 0ull;
+  (void)kmax;
+  for (int k = k0; k <= k1; ++k)
+  {
+    const bool plane = k < k1; // cells of plane k are updated (partially) this iteration
+    const int  es = esl(k);
+    R *        Ez = sEz + es * EZS;
+    R *        Ey = sEy + es * EYS;
+    R *        Ex = sEx + es * EXS;
+    if (plane)
+    {
+      // x-faces i in [i0, i0+TX], rows j in [j0, j0+TY): HLLD (MHDRunFunctors3D.h:1839-1846)
+      for (int f = threadIdx.x; f < FXS; f += NT)
+      {
+        const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
+        if (i > P.nx + gw || j >= P.ny + gw)
+          continue; // padding of a partial tile
+        R ql[8], qr[8], fl[5];
+        face_state<R, 0, true>(T(i - 1, j, k), st, ql, sr, sp);
+        face_state<R, 0, false>(T(i, j, k), st, qr, sr, sp);
+        mhd_hlld<R>(ql, qr, fl, C.gamma0);
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          sFx[v * FXS + f] = fl[v];
+      }
+      // y-faces, swap IU<->IV, IA<->IB (MHDRunFunctors3D.h:1848-1860)
+      for (int f = threadIdx.x; f < FYS; f += NT)
+      {
+        const int i = i0 + f % TX, j = j0 + f / TX;
+        if (i >= P.nx + gw || j > P.ny + gw)
+          continue;
+        R ql[8], qr[8], fl[5], x;
+        face_state<R, 1, true>(T(i, j - 1, k), st, ql, sr, sp);
+        face_state<R, 1, false>(T(i, j, k), st, qr, sr, sp);
+        x = ql[IU], ql[IU] = ql[IV], ql[IV] = x;
+        x = ql[IA], ql[IA] = ql[IB], ql[IB] = x;
+        x = qr[IU], qr[IU] = qr[IV], qr[IV] = x;
+        x = qr[IA], qr[IA] = qr[IB], qr[IB] = x;
+        mhd_hlld<R>(ql, qr, fl, C.gamma0);
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          sFy[v * FYS + f] = fl[v];
+      }
+      // z-edge emfs of plane k: edges (i, j) i in [i0, i0+TX], j in [j0, j0+TY]
+      for (int f = threadIdx.x; f < EZS; f += NT)
+      {
+        const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
+        if (i > P.nx + gw || j > P.ny + gw)
+          continue;
+        R a[8], b[8], c[8], d[8];
+        edge_state<R, 2, 0>(T(i - 1, j - 1, k), st, a, sr, sp);
+        edge_state<R, 2, 1>(T(i - 1, j, k), st, b, sr, sp);
+        edge_state<R, 2, 2>(T(i, j - 1, k), st, c, sr, sp);
+        edge_state<R, 2, 3>(T(i, j, k), st, d, sr, sp);
+        Ez[f] = mhd_compute_emf<R, 2>(a, b, c, d, C.gamma0, C.smallc);
+      }
+    }
+    // y-edge emfs at level k: edges (i, j) i in [i0, i0+TX], j in [j0, j0+TY)
+    // corners RT2(i-1,k-1), LT2(i,k-1), RB2(i-1,k), LB2(i,k) (MHDRunFunctors3D.h:2212-2217)
+    for (int f = threadIdx.x; f < EYS; f += NT)
+    {
+      const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
+      if (i > P.nx + gw || j >= P.ny + gw)
+        continue;
+      R a[8], b[8], c[8], d[8];
+      edge_state<R, 1, 0>(T(i - 1, j, k - 1), st, a, sr, sp);
+      edge_state<R, 1, 2>(T(i, j, k - 1), st, b, sr, sp);
+      edge_state<R, 1, 1>(T(i - 1, j, k), st, c, sr, sp);
+      edge_state<R, 1, 3>(T(i, j, k), st, d, sr, sp);
+      Ey[f] = mhd_compute_emf<R, 1>(a, b, c, d, C.gamma0, C.smallc);
+    }
+    // x-edge emfs at level k: edges (i, j) i in [i0, i0+TX), j in [j0, j0+TY]
+    for (int f = threadIdx.x; f < EXS; f += NT)
+    {
+      const int i = i0 + f % TX, j = j0 + f / TX;
+      if (i >= P.nx + gw || j > P.ny + gw)
+        continue;
+      R a[8], b[8], c[8], d[8];
+      edge_state<R, 0, 0>(T(i, j - 1, k - 1), st, a, sr, sp);
+      edge_state<R, 0, 1>(T(i, j - 1, k), st, b, sr, sp);
+      edge_state<R, 0, 2>(T(i, j, k - 1), st, c, sr, sp);
+      edge_state<R, 0, 3>(T(i, j, k), st, d, sr, sp);
+      Ex[f] = mhd_compute_emf<R, 0>(a, b, c, d, C.gamma0, C.smallc);
+    }
+    // z-face flux at level k of the own column: swap IU<->IW, IA<->IC
+    R fz[5];
+    if (own)
+    {
+      R ql[8], qr[8], x;
+      face_state<R, 2, true>(T(gi, gj, k - 1), st, ql, sr, sp);
+      face_state<R, 2, false>(T(gi, gj, k), st, qr, sr, sp);
+      x = ql[IU], ql[IU] = ql[IW], ql[IW] = x;
+      x = ql[IA], ql[IA] = ql[IC], ql[IC] = x;
+      x = qr[IU], qr[IU] = qr[IW], qr[IW] = x;
+      x = qr[IA], qr[IA] = qr[IC], qr[IC] = x;
+      mhd_hlld<R>(ql, qr, fz, C.gamma0);
+    }
+    __syncthreads();
+
+    if (own && k > k0)
+    {
+      // finish cell k-1: hydro (UpdateFunctor3D_MHD, MHDRunFunctors3D.h:2488-2527)
+      const long long off = (long long)(k - 1) * P.plane + (long long)gj * P.isize + gi;
+      acc[ID] -= fz[ID] * dtdz;
+      acc[IP] -= fz[IP] * dtdz;
+      acc[IU] -= fz[IW] * dtdz;
+      acc[IV] -= fz[IV] * dtdz;
+      acc[IW] -= fz[IU] * dtdz;
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        hout[v * st + off] = (S)acc[v];
+      // CT update of the face fields (UpdateEmfFunctor3D, MHDRunFunctors3D.h:2590-2613)
+      const int  pe = esl(k - 1);
+      const R *  Ezp = sEz + pe * EZS;
+      const R *  Eyp = sEy + pe * EYS;
+      const R *  Exp = sEx + pe * EXS;
+      const int  ezi = ty * (TX + 1) + tx, eyi = ty * (TX + 1) + tx, exi = ty * TX + tx;
+      double     bx = mi.b[0 * st + off], by = mi.b[1 * st + off], bz = mi.b[2 * st + off];
+      if constexpr (sizeof(R) == 8)
+      {
+        bx += (Ezp[ezi + (TX + 1)] - Ezp[ezi]) * dtdy;
+        by -= (Ezp[ezi + 1] - Ezp[ezi]) * dtdx;
+        bx -= (Ey[eyi] - Eyp[eyi]) * dtdz;
+        by += (Ex[exi] - Exp[exi]) * dtdz;
+        bz += (Eyp[eyi + 1] - Eyp[eyi]) * dtdx;
+        bz -= (Exp[exi + TX] - Exp[exi]) * dtdy;
+      }
+      else
+      {
+        // FP64 island: the CT update keeps div B at FP64 round-off
+        bx += ((double)Ezp[ezi + (TX + 1)] - (double)Ezp[ezi]) * ddtdy;
+        by -= ((double)Ezp[ezi + 1] - (double)Ezp[ezi]) * ddtdx;
+        bx -= ((double)Ey[eyi] - (double)Eyp[eyi]) * ddtdz;
+        by += ((double)Ex[exi] - (double)Exp[exi]) * ddtdz;
+        bz += ((double)Eyp[eyi + 1] - (double)Eyp[eyi]) * ddtdx;
+        bz -= ((double)Exp[exi + TX] - (double)Exp[exi]) * ddtdy;
+      }
+      bout[0 * st + off] = bx;
+      bout[1 * st + off] = by;
+      bout[2 * st + off] = bz;
+    }
+    if (own && plane)
+    {
+      // partial update of cell k: U + Fx(i) - Fx(i+1) + Fy(j) - Fy(j+1) + Fz(k)
+      const long long off = (long long)k * P.plane + (long long)gj * P.isize + gi;
+      R               u[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        u[v] = (R)ldg(mi.h + v * st + off);
+      const int fx0 = ty * (TX + 1) + tx, fy0 = ty * TX + tx;
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        u[v] += sFx[v * FXS + fx0] * dtdx;
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        u[v] -= sFx[v * FXS + fx0 + 1] * dtdx;
+      u[ID] += sFy[ID * FYS + fy0] * dtdy;
+      u[IP] += sFy[IP * FYS + fy0] * dtdy;
+      u[IU] += sFy[IV * FYS + fy0] * dtdy;
+      u[IV] += sFy[IU * FYS + fy0] * dtdy;
+      u[IW] += sFy[IW * FYS + fy0] * dtdy;
+      u[ID] -= sFy[ID * FYS + fy0 + TX] * dtdy;
+      u[IP] -= sFy[IP * FYS + fy0 + TX] * dtdy;
+      u[IU] -= sFy[IV * FYS + fy0 + TX] * dtdy;
+      u[IV] -= sFy[IU * FYS + fy0 + TX] * dtdy;
+      u[IW] -= sFy[IW * FYS + fy0 + TX] * dtdy;
+      u[ID] += fz[ID] * dtdz;
+      u[IP] += fz[IP] * dtdz;
+      u[IU] += fz[IW] * dtdz;
+      u[IV] += fz[IV] * dtdz;
+      u[IW] += fz[IU] * dtdz;
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        acc[v] = u[v];
+    }
+    __syncthreads(); // flux buffers and the older emf planes are reused
+  }
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
+    step_commit(clk, step, t, dt);
+}
+
+// max |div B| over the interior, face differences with dx normalisation
+template <class S>
+__global__ void
+mhd_divb_kernel(const void * __restrict__ U, KParams P, unsigned long long * key)
+{
+  const MhdState<S> m = mhd_state<S>(U, P);
+  const long long   n = (long long)P.nx * P.ny * P.nz;
+  unsigned long long kmax = 0ull;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x)
+  {
+    const int       i = (int)(c % P.nx) + P.gw;
+    const long long r = c / P.nx;
+    const int       j = (int)(r % P.ny) + P.gw;
+    const int       k = (int)(r / P.ny) + P.gw;
+    const SrcCell   s0 = src_cell(P, i, j, k);
+    const double    d = (load_face<S>(m, P, src_cell(P, i + 1, j, k), 0) - load_face<S>(m, P, s0, 0)) / P.dx +
+                     (load_face<S>(m, P, src_cell(P, i, j + 1, k), 1) - load_face<S>(m, P, s0, 1)) / P.dy +
+                     (load_face<S>(m, P, src_cell(P, i, j, k + 1), 2) - load_face<S>(m, P, s0, 2)) / P.dz;
+    const unsigned long long kk = cand_key(fabs(d));
+    kmax = kk > kmax ? kk : kmax;
+  }
+  block_max_commit<256>(kmax, key);
+}
+
+template <class R>
+constexpr size_t
+mhd_trace_smem(int TX, int TY)
+{
+  return sizeof(double) * 4 * 3 * (TX + 3) * (TY + 3) + sizeof(R) * (3 * 8 * (TX + 2) * (TY + 2) + 2 * 3 * (TX + 1) * (TY + 1));
+}
+template <class R>
+constexpr size_t
+mhd_update_smem(int TX, int TY)
+{
+  return sizeof(R) * (5 * (TX + 1) * TY + 5 * TX * (TY + 1) + 2 * (TX + 1) * (TY + 1) + 2 * (TX + 1) * TY +
+                      2 * TX * (TY + 1));
+}
+
+constexpr int MT_TX = 32, MT_TY = 4; // trace tile
+constexpr int MU_TX = 16, MU_TY = 8; // update tile
+
+template <class S, class R>
+cudaError_t
+mhd_step_t(const void * Uin, void * Uout, void * work, const KParams & P, DevClock * clk, int step,
+           cudaStream_t st)
+{
+  // 1. dt of this step into clock slot step % 3
+  {
+    const long long n = (long long)P.nx * P.ny * P.nz;
+    const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    mhd_dt_kernel<S, R><<<blocks, 256, 0, st>>>(Uin, P, clk, step, nullptr);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+      return e;
+  }
+  // 2. trace
+  {
+    auto       k = mhd_trace_kernel<S, R, MT_TX, MT_TY>;
+    const int  sm = (int)mhd_trace_smem<R>(MT_TX, MT_TY);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e != cudaSuccess)
+      return e;
+    const int nt = P.nz + 2;
+    dim3      grid((P.nx + 2 + MT_TX - 1) / MT_TX, (P.ny + 2 + MT_TY - 1) / MT_TY, (nt + P.kchunk - 1) / P.kchunk);
+    k<<<grid, MT_TX * MT_TY, sm, st>>>(Uin, (R *)work, P, clk, step);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+      return e;
+  }
+  // 3. fluxes, emfs, update
+  {
+    auto       k = mhd_update_kernel<S, R, MU_TX, MU_TY>;
+    const int  sm = (int)mhd_update_smem<R>(MU_TX, MU_TY);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e != cudaSuccess)
+      return e;
+    dim3 grid((P.nx + MU_TX - 1) / MU_TX, (P.ny + MU_TY - 1) / MU_TY, (P.nz + P.kchunk - 1) / P.kchunk);
+    k<<<grid, MU_TX * MU_TY, sm, st>>>(Uin, Uout, (const R *)work, P, clk, step);
+    return cudaGetLastError();
+  }
+}
+
+cudaError_t
+mhd_step(int prec, const void * Uin, void * Uout, void * work, const KParams & P, DevClock * clk,
+         int step, cudaStream_t st)
+{
+#ifdef EK_EXACT_ONLY
+  if (prec != 0)
+    return cudaErrorNotSupported;
+  return mhd_step_t<double, double>(Uin, Uout, work, P, clk, step, st);
+#else
+  if (prec == 0)
+    return mhd_step_t<double, double>(Uin, Uout, work, P, clk, step, st);
+  return mhd_step_t<float, float>(Uin, Uout, work, P, clk, step, st);
+#endif
+}
+
+cudaError_t
+mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key, cudaStream_t st)
+{
+  const long long n = (long long)P.nx * P.ny * P.nz;
+  const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+#ifdef EK_EXACT_ONLY
+  if (prec != 0)
+    return cudaErrorNotSupported;
+  mhd_dt_kernel<double, double><<<blocks, 256, 0, st>>>(U, P, nullptr, 0, key);
+#else
+  if (prec == 0)
+    mhd_dt_kernel<double, double><<<blocks, 256, 0, st>>>(U, P, nullptr, 0, key);
+  else
+    mhd_dt_kernel<float, float><<<blocks, 256, 0, st>>>(U, P, nullptr, 0, key);
+#endif
+  return cudaGetLastError();
+}
+
 size_t
-mhd_work_bytes(int, const KParams &)
+mhd_work_bytes(int prec, const KParams & P)
 {
-  return 0;
+  return (size_t)T_N * (size_t)P.vstride * (prec == 0 ? sizeof(double) : sizeof(float));
 }
+
+#ifndef EK_EXACT_ONLY
 cudaError_t
-mhd_divb_max(int, const void *, const KParams &, double *, cudaStream_t)
+mhd_divb_max(int prec, const void * U, const KParams & P, double * out, cudaStream_t st)
 {
-  return cudaErrorNotSupported;
+  // reuses out as a key slot, then converts in place on the host side
+  unsigned long long * key = reinterpret_cast<unsigned long long *>(out);
+  cudaError_t          e = cudaMemsetAsync(key, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess)
+    return e;
+  const long long n = (long long)P.nx * P.ny * P.nz;
+  const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  if (prec == 0)
+    mhd_divb_kernel<double><<<blocks, 256, 0, st>>>(U, P, key);
+  else
+    mhd_divb_kernel<float><<<blocks, 256, 0, st>>>(U, P, key);
+  return cudaGetLastError();
 }
+#endif
+
 } // namespace EK_NS
