@@ -1,0 +1,430 @@
+"""Benchmark: Mcell-updates/s of the unsplit MUSCL-Hancock step on one GB300.
+
+Headline workload (the reference's 3D blast config, 256^3): Hydro_Muscl_3D,
+HLLC, minmod, CFL 0.7, outflow boundaries, seeded 1% density noise.  A
+"step" is one full time step (dt reduction, fused fluxes and update) of the
+whole grid.  ``value`` is the mixed-FP32 form; the FP64 drop-in is measured
+on the same workload beside it, with the L1 density error between the two.
+The CT-MHD Orszag-Tang 256^3 workload is measured the same way under
+``workloads``.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica of the
+workload on its own GPU (the path has no exchange between ranks); the
+slowest rank's time is used and ``value`` is the sum over ranks.
+``--impl reference`` times the reference algorithm's CPU restatement
+(oracle/) on the host cores instead (rank 0 only).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-updates/s on 1 GB300: mixed-FP32 vs FP64 at stated L1 err; % of HBM BW"
+UNIT = "Mcell-updates/s"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+
+# algorithmic bytes per cell-update: one read and one write of U
+BYTES_PER_CELL = {
+    ("hydro3d", "mixed"): 2 * 5 * 4,
+    ("hydro3d", "fp64"): 2 * 5 * 8,
+    ("mhd3d", "mixed"): 2 * (5 * 4 + 3 * 8),
+    ("mhd3d", "fp64"): 2 * 8 * 8,
+}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    except Exception:
+        return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() in ("active", "1"):
+                        reasons.add(n)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cells_of(p):
+    return p.nx * p.ny * (p.nz if p.dim == 3 else 1)
+
+
+def ghost_cells_of(p):
+    return p.isize * p.jsize * (p.ksize if p.dim == 3 else 1)
+
+
+def time_device_run(ek, s, steps, sync):
+    """K steps on the solver's stream, CUDA events on that stream."""
+    import torch
+
+    st = torch.cuda.ExternalStream(s.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sync()
+    n0 = s.launch_count()
+    e0.record(st)
+    done = s.run(steps)
+    e1.record(st)
+    sync()
+    return e0.elapsed_time(e1), done, s.launch_count() - n0
+
+
+def measure_workload(ek, kind, prec, ini, U0, steps, warmup, sync, profile=True):
+    p = ek.params_from_ini(ini, precision=prec)
+    with ek.Solver(p) as s:
+        s.set_state(U0)
+        s.run(warmup)
+        s.synchronize()
+        ms, done, launches = time_device_run(ek, s, steps, sync)
+        out = {"ms": ms, "steps": done, "launches": launches}
+        if profile:
+            # kernel durations (CUDA events around every launch, same stream)
+            s.set_profiling(True)
+            s.run(steps)
+            s.synchronize()
+            k = {i: s.kernel_time(i) for i in range(3)}
+            out["kernels"] = {i: (v[0] / v[1] if v[1] else None, v[1]) for i, v in k.items()}
+            s.set_profiling(False)
+        out["U"] = s.get_state()
+        out["totals"] = s.totals()
+        out["iteration"] = s.m_iteration
+    out["cells"] = cells_of(p)
+    out["ghost_cells"] = ghost_cells_of(p)
+    return out
+
+
+def e2e_measure(ek, prec, ini, U0, steps):
+    """Reference-facing loop through the C ABI with host buffers: set_state
+    (host -> device), next_iteration per step (the dt read back each step, as
+    the reference's reduction does), get_state (device -> host)."""
+    p = ek.params_from_ini(ini, precision=prec)
+    U0c = np.ascontiguousarray(U0)
+    with ek.Solver(p) as s:
+        s.set_state(U0c)  # warm the paths once (allocation, module load)
+        s.next_iteration()
+        s.synchronize()
+        t0 = time.perf_counter()
+        s.set_state(U0c)
+        for _ in range(steps):
+            s.next_iteration()
+        U = s.get_state()
+        dt = time.perf_counter() - t0
+        _, nbytes = s.device_state()
+    cells = cells_of(p)
+    return {
+        "value": cells * steps / dt / 1e6,
+        "unit": UNIT,
+        "h2d_bytes_per_step": int(round(nbytes / steps)),
+        "d2h_bytes_per_step": int(round(nbytes / steps)) + 8,
+        "wall_s": dt,
+        "path": "ek_solver_set_state + next_iteration x K + ek_solver_get_state (host FP64 arrays)",
+    }, U
+
+
+def oracle_rate(ini, U0, nsteps):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import eko
+
+    p = eko.params_from_ini(ini)
+    o = eko.Oracle(p, U0)
+    t0 = time.perf_counter()
+    done = len(o.run(nsteps))
+    dt = time.perf_counter() - t0
+    o.close()
+    return p.nx * p.ny * p.nz * done / dt / 1e6, dt, eko.num_threads()
+
+
+def ensure_oracle():
+    lib = os.path.join(ROOT, "oracle", "_build", "libek_oracle.so")
+    if not os.path.exists(lib):
+        env = dict(os.environ, EK_SKIP_REF="1")
+        subprocess.run(["sh", os.path.join(ROOT, "oracle", "build.sh")], check=True, env=env,
+                       stdout=subprocess.DEVNULL)
+
+
+def cpu_sample(args, seconds=15.0):
+    """Oracle on a bounded sample of the headline workload (a smaller grid of
+    the same problem), sized for roughly `seconds` of CPU work."""
+    from euler_kokkos_gb300 import problems as P
+
+    ensure_oracle()
+    probe_n = 48
+    ini, U0 = P.blast_3d(n=probe_n, nsteps=2)
+    r, _, _ = oracle_rate(ini, U0, 2)
+    # choose a grid and a step count worth ~seconds of work at the probed rate
+    n = 128 if r * 1e6 * seconds / (128 ** 3) >= 3 else 96
+    steps = max(2, min(20, int(r * 1e6 * seconds / n ** 3)))
+    ini, U0 = P.blast_3d(n=n, nsteps=steps)
+    rate, dt, cores = oracle_rate(ini, U0, steps)
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "3D blast %d^3, %d steps (oracle/ek_oracle.c, OpenMP, %d threads, %.1f s)" %
+                      (n, steps, cores, dt)}
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm's CPU restatement (the
+    reference's own build cannot be compiled on the GPU host: Kokkos is not
+    available offline), all host threads, same workload and metric."""
+    from euler_kokkos_gb300 import problems as P
+
+    ensure_oracle()
+    n_full = args.n
+    # probe the host rate to keep the whole run within a few minutes
+    ini, U0 = P.blast_3d(n=48, nsteps=2)
+    r, _, cores = oracle_rate(ini, U0, 2)
+    est = (args.steps + args.warmup) * n_full ** 3 / (r * 1e6)
+    n = n_full if est < 150 else 128
+    ini, U0 = P.blast_3d(n=n, nsteps=args.steps + args.warmup)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import eko
+
+    p = eko.params_from_ini(ini)
+    o = eko.Oracle(p, U0)
+    o.run(args.warmup)
+    t0 = time.perf_counter()
+    done = len(o.run(args.steps))
+    dt = time.perf_counter() - t0
+    cells = p.nx * p.ny * p.nz
+    value = cells * done / dt / 1e6
+    sample = "3D blast %d^3%s, %d timed steps after %d warm-up, FP64" % (
+        n, "" if n == n_full else " (bounded sample of the %d^3 workload)" % n_full, done, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": done, "warmup": args.warmup, "ms_per_step": dt * 1e3 / max(done, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 3D blast)",
+        "config": {"workload": "3D Euler blast %d^3, Hydro_Muscl_3D, HLLC, minmod, CFL 0.7, outflow" % n,
+                   "engine": "oracle/ek_oracle.c (CPU restatement of the reference step), OpenMP"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="grid size of the headline workload")
+    ap.add_argument("--mhd-steps", type=int, default=20)
+    ap.add_argument("--no-mhd", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def sync():
+        torch.cuda.synchronize()
+        barrier()
+
+    import euler_kokkos_gb300 as ek
+    from euler_kokkos_gb300 import problems as P
+
+    peaks, peak_kind = load_peaks()
+    hbm = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
+
+    ini, U0 = P.blast_3d(n=args.n, nsteps=10 ** 6)
+    with ClockSampler(local) as clk:
+        mixed = measure_workload(ek, "hydro3d", ek.EK_PREC_MIXED, ini, U0, args.steps, args.warmup, sync)
+    clocks = clk.summary()
+    fp64 = measure_workload(ek, "hydro3d", ek.EK_PREC_FP64, ini, U0, args.steps, args.warmup, sync)
+
+    def maxt(ms):
+        if dist is None:
+            return ms
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ms_mixed, ms_fp64 = maxt(mixed["ms"]), maxt(fp64["ms"])
+    cells = mixed["cells"]
+    value = cells * mixed["steps"] / (ms_mixed / 1e3) / 1e6 * world
+    v64 = cells * fp64["steps"] / (ms_fp64 / 1e3) / 1e6 * world
+
+    # accuracy of the mixed form against the FP64 drop-in after the same steps
+    gw = 2
+    a = mixed["U"][0, gw:-gw, gw:-gw, gw:-gw]
+    b = fp64["U"][0, gw:-gw, gw:-gw, gw:-gw]
+    l1 = float(np.abs(a - b).sum() / np.abs(b).sum())
+    linf = float(np.abs(a - b).max() / np.abs(b).max())
+
+    def roofline(meas, key):
+        kms, kn = meas["kernels"][0]
+        achieved = BYTES_PER_CELL[key] * meas["cells"] / (kms / 1e3) / 1e9 if kms else None
+        return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm if achieved else None, "traffic": None,
+                "kernel_ms": kms, "peak_source": peak_kind,
+                "algorithmic_bytes_per_cell": BYTES_PER_CELL[key]}
+
+    workloads = {}
+    if not args.no_mhd:
+        ini_m, U0_m = P.orszag_tang_3d(n=args.n, nsteps=10 ** 6)
+        mm = measure_workload(ek, "mhd3d", ek.EK_PREC_MIXED, ini_m, U0_m, args.mhd_steps, 3, sync)
+        m64 = measure_workload(ek, "mhd3d", ek.EK_PREC_FP64, ini_m, U0_m, max(2, args.mhd_steps // 4), 3, sync)
+        gwm = 3
+        am = mm["U"][0, gwm:-gwm, gwm:-gwm, gwm:-gwm]
+        # error after the same number of steps
+        with ek.Solver(ek.params_from_ini(ini_m, precision=ek.EK_PREC_FP64)) as s64:
+            s64.set_state(U0_m)
+            s64.run(mm["iteration"])
+            bm = s64.get_state()[0, gwm:-gwm, gwm:-gwm, gwm:-gwm]
+        vm = mm["cells"] * mm["steps"] / (maxt(mm["ms"]) / 1e3) / 1e6 * world
+        vm64 = m64["cells"] * m64["steps"] / (maxt(m64["ms"]) / 1e3) / 1e6 * world
+        kt = {name: mm["kernels"][i][0] for i, name in ((0, "update"), (1, "trace"), (2, "cfl"))}
+        workloads["mhd_orszag_tang_%d" % args.n] = {
+            "value_mixed": vm, "value_fp64": vm64, "unit": UNIT, "mixed_over_fp64": vm / vm64,
+            "ms_per_step_mixed": mm["ms"] / mm["steps"], "ms_per_step_fp64": m64["ms"] / m64["steps"],
+            "l1_rel_err_rho_mixed_vs_fp64": float(np.abs(am - bm).sum() / np.abs(bm).sum()),
+            "max_divB_mixed": float(mm["totals"][2]), "max_divB_fp64": float(m64["totals"][2]),
+            "kernel_ms_mixed": kt,
+            "roofline_mixed": roofline(mm, ("mhd3d", "mixed")),
+            "roofline_fp64": roofline(m64, ("mhd3d", "fp64")),
+            "config": "MHD_Muscl_3D Orszag-Tang %d^3, HLLD + CT, slope_type 2, CFL 0.8, periodic" % args.n,
+        }
+
+    line = None
+    if rank == 0:
+        e2e, _ = e2e_measure(ek, ek.EK_PREC_MIXED, ini, U0, args.steps)
+        cpu = None if args.no_cpu else cpu_sample(args)
+        launches = mixed["launches"]
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": mixed["steps"],
+            "warmup": args.warmup,
+            "ms_per_step": ms_mixed / mixed["steps"],
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic: seeded 3D blast (rho 1 + 1% splitmix noise, p 0.1 / 10 sphere r 0.1)",
+            "config": {
+                "workload": "3D Euler blast %d^3 on [0,1]^3, Hydro_Muscl_3D, HLLC, minmod, CFL 0.7, outflow; "
+                            "mixed FP32 (FP64 dt, totals, cancellation islands)" % args.n,
+                "grid": [args.n] * 3,
+                "l2_policy": "no flush: the FP32 state (%.0f MB) is larger than the 129 MB L2" %
+                             (5 * 4 * mixed["ghost_cells"] / 1e6),
+                "parallelism": "replicas" if world > 1 else "single GPU",
+                "kernel": "hydro3d_step<float> (fused: ghost map, primitives, slopes, trace, HLLC, update, next-dt)",
+            },
+            "fp64": {
+                "value": v64, "unit": UNIT, "ms_per_step": ms_fp64 / fp64["steps"],
+                "roofline": roofline(fp64, ("hydro3d", "fp64")),
+                "note": "FP64 drop-in (FMA contraction); GB300 FP64 FMA rate measured at 1.19 TFLOP/s",
+            },
+            "mixed_over_fp64": value / v64,
+            "l1_rel_err_rho_mixed_vs_fp64": l1,
+            "linf_rel_err_rho_mixed_vs_fp64": linf,
+            "roofline": roofline(mixed, ("hydro3d", "mixed")),
+            "reference_formula_mcell_s": mixed["ghost_cells"] * mixed["steps"] / (ms_mixed / 1e3) / 1e6 * world,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "workloads": workloads,
+        }
+    barrier()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

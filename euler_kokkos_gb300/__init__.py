@@ -129,6 +129,10 @@ def load_library():
         "ek_solver_device_state": (ctypes.c_int, [c_p, ctypes.POINTER(c_p), ctypes.POINTER(ctypes.c_size_t)]),
         "ek_solver_synchronize": (ctypes.c_int, [c_p]),
         "ek_solver_launch_count": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_longlong)]),
+        "ek_solver_stream": (ctypes.c_int, [c_p, ctypes.POINTER(c_p)]),
+        "ek_solver_set_profiling": (ctypes.c_int, [c_p, ctypes.c_int]),
+        "ek_solver_kernel_time": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                                 ctypes.POINTER(ctypes.c_longlong)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -264,6 +268,22 @@ class Solver:
         n = ctypes.c_longlong()
         _check(self._L.ek_solver_launch_count(self._h, ctypes.byref(n)), "launch_count")
         return n.value
+
+    # -- timing ------------------------------------------------------------
+    def stream(self) -> int:
+        """cudaStream_t of the solver (e.g. for torch.cuda.ExternalStream)."""
+        p = ctypes.c_void_p()
+        _check(self._L.ek_solver_stream(self._h, ctypes.byref(p)), "stream")
+        return p.value or 0
+
+    def set_profiling(self, enable: bool = True):
+        _check(self._L.ek_solver_set_profiling(self._h, int(enable)), "set_profiling")
+
+    def kernel_time(self, kernel: int = 0):
+        """(total ms, launches) of one step kernel since profiling was enabled."""
+        ms, n = ctypes.c_double(), ctypes.c_longlong()
+        _check(self._L.ek_solver_kernel_time(self._h, kernel, ctypes.byref(ms), ctypes.byref(n)), "kernel_time")
+        return ms.value, n.value
 
 
 class SolverFactory:

@@ -54,7 +54,46 @@ struct ek_solver
   bool          has_state = false;
   long long     launches = 0;
   std::vector<double> hbuf; // host staging (FP64, LayoutLeft)
+  // kernel timing (ek_solver_set_profiling)
+  bool                     profiling = false;
+  std::vector<cudaEvent_t> ev_pool;            // recycled events
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+  double                   kernel_ms[3] = { 0, 0, 0 };
+  long long                kernel_n[3] = { 0, 0, 0 };
 };
+
+static cudaEvent_t
+take_event(ek_solver * s)
+{
+  if (!s->ev_pool.empty())
+  {
+    cudaEvent_t e = s->ev_pool.back();
+    s->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// fold the finished event pairs into the per-kernel totals
+static void
+drain_events(ek_solver * s)
+{
+  for (auto & pe : s->ev_pending)
+  {
+    float ms = 0.f;
+    if (cudaEventSynchronize(pe.second.second) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, pe.second.first, pe.second.second) == cudaSuccess)
+    {
+      s->kernel_ms[pe.first] += ms;
+      s->kernel_n[pe.first] += 1;
+    }
+    s->ev_pool.push_back(pe.second.first);
+    s->ev_pool.push_back(pe.second.second);
+  }
+  s->ev_pending.clear();
+}
 
 static ek_status
 cuda_fail(cudaError_t e, const char * what)
@@ -228,6 +267,9 @@ ek_solver_destroy(ek_solver * s)
   cudaFree(s->clk);
   cudaFree(s->dtlog);
   cudaFree(s->scratch3);
+  drain_events(s);
+  for (auto e : s->ev_pool)
+    cudaEventDestroy(e);
   if (s->stream)
     cudaStreamDestroy(s->stream);
   delete s;
@@ -446,23 +488,49 @@ ek_solver_compute_dt(ek_solver * s, double * dt)
   return EK_OK;
 }
 
+// one kernel of a step, bracketed by timing events when profiling
 static ek_status
-launch_step(ek_solver * s, int step)
+launch_one(ek_solver * s, int kernel_id, int phase, int step)
 {
   const void * in = s->U[step % 2];
   void *       outp = s->U[(step + 1) % 2];
-  cudaError_t  e;
+  cudaEvent_t  e0 = nullptr, e1 = nullptr;
+  if (s->profiling)
+  {
+    e0 = take_event(s);
+    e1 = take_event(s);
+    cudaEventRecord(e0, s->stream);
+  }
+  cudaError_t e;
   if (s->p.mhd)
-    e = s->exact ? ek_exact::mhd_step(s->prec, in, outp, s->work, s->kp, s->clk, step, s->stream)
-                 : ek_fast::mhd_step(s->prec, in, outp, s->work, s->kp, s->clk, step, s->stream);
+    e = s->exact ? ek_exact::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream)
+                 : ek_fast::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream);
   else
     e = s->exact ? ek_exact::hydro_step(s->p.dim, s->prec, in, outp, s->kp, s->clk, step, s->stream)
                  : ek_fast::hydro_step(s->p.dim, s->prec, in, outp, s->kp, s->clk, step, s->stream);
+  if (s->profiling)
+  {
+    cudaEventRecord(e1, s->stream);
+    s->ev_pending.push_back({ kernel_id, { e0, e1 } });
+  }
   if (e == cudaErrorNotSupported)
     return fail(EK_ERR_UNSUPPORTED, "kernel not available for this configuration");
   EK_CUDA(e, "step kernel");
-  s->launches += s->p.mhd ? 2 : 1;
+  s->launches += 1;
   return EK_OK;
+}
+
+static ek_status
+launch_step(ek_solver * s, int step)
+{
+  if (!s->p.mhd)
+    return launch_one(s, 0, 0, step);
+  ek_status st = launch_one(s, 2, 0, step); // CFL of the step
+  if (st == EK_OK)
+    st = launch_one(s, 1, 1, step); // trace
+  if (st == EK_OK)
+    st = launch_one(s, 0, 2, step); // fluxes, emfs, update
+  return st;
 }
 
 static int
@@ -635,5 +703,42 @@ ek_solver_launch_count(ek_solver * s, long long * n)
   if (!s || !n)
     return fail(EK_ERR_INVALID, "ek_solver_launch_count: bad argument");
   *n = s->launches;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_stream(ek_solver * s, void ** stream)
+{
+  if (!s || !stream)
+    return fail(EK_ERR_INVALID, "ek_solver_stream: bad argument");
+  *stream = (void *)s->stream;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_set_profiling(ek_solver * s, int enable)
+{
+  if (!s)
+    return fail(EK_ERR_INVALID, "ek_solver_set_profiling: null solver");
+  drain_events(s);
+  s->profiling = enable != 0;
+  for (int i = 0; i < 3; ++i)
+  {
+    s->kernel_ms[i] = 0.0;
+    s->kernel_n[i] = 0;
+  }
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_kernel_time(ek_solver * s, int kernel, double * total_ms, long long * launches)
+{
+  if (!s || kernel < 0 || kernel > 2)
+    return fail(EK_ERR_INVALID, "ek_solver_kernel_time: bad argument");
+  drain_events(s);
+  if (total_ms)
+    *total_ms = s->kernel_ms[kernel];
+  if (launches)
+    *launches = s->kernel_n[kernel];
   return EK_OK;
 }

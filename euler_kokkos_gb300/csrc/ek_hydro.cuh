@@ -207,37 +207,51 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
 }
 
 // per-cell CFL candidate of ComputeDtFunctor{2D,3D}
-// (HydroRunFunctors2D.h:56-84, HydroRunFunctors3D.h:49-84), always returned
-// in double so that the max-reduction and dt stay FP64
+// (HydroRunFunctors2D.h:56-84, HydroRunFunctors3D.h:49-84).  FP64: the
+// reference's expression.  Mixed: the candidate is formed in FP32 with the
+// inverse cell sizes (FP64 arithmetic costs 64 FP32 operations on GB300);
+// the max-reduction and dt = cfl / max stay FP64.
+struct InvD
+{
+  double dx, dy, dz;    // cell sizes (FP64 path)
+  float  idx, idy, idz; // 1/dx, 1/dy, 1/dz (mixed path)
+};
+__host__ __device__ inline InvD
+make_invd(double dx, double dy, double dz)
+{
+  InvD d;
+  d.dx = dx, d.dy = dy, d.dz = dz;
+  d.idx = (float)(1.0 / dx), d.idy = (float)(1.0 / dy), d.idz = (float)(1.0 / dz);
+  return d;
+}
+
 template <class R, int NV>
 __device__ __forceinline__ double
-hydro_invdt(const R (&u)[NV], const HydroConst<R> & C, double dx, double dy, double dz)
+hydro_invdt(const R (&u)[NV], const HydroConst<R> & C, const InvD & D)
 {
   R q[NV];
   hydro_prims<R, NV>(u, q, C);
   const R c = hydro_sound<R>(q[ID], q[IP], C);
+  const R vx = c + fabs(q[IU]);
+  const R vy = c + fabs(q[IV]);
   if constexpr (sizeof(R) == 8)
   {
-    const double vx = c + fabs(q[IU]);
-    const double vy = c + fabs(q[IV]);
     if constexpr (NV == 4)
-      return vx / dx + vy / dy;
+      return vx / D.dx + vy / D.dy;
     else
     {
-      const double vz = c + fabs(q[IW]);
-      return vx / dx + vy / dy + vz / dz;
+      const R vz = c + fabs(q[IW]);
+      return vx / D.dx + vy / D.dy + vz / D.dz;
     }
   }
   else
   {
-    const double vx = (double)c + fabs((double)q[IU]);
-    const double vy = (double)c + fabs((double)q[IV]);
     if constexpr (NV == 4)
-      return vx / dx + vy / dy;
+      return (double)(vx * D.idx + vy * D.idy);
     else
     {
-      const double vz = (double)c + fabs((double)q[IW]);
-      return vx / dx + vy / dy + vz / dz;
+      const R vz = c + fabs(q[IW]);
+      return (double)(vx * D.idx + vy * D.idy + vz * D.idz);
     }
   }
 }

@@ -96,6 +96,7 @@ hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
     return;
   const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy);
   const HydroConst<R> C = hydro_const<R>(P);
+  const InvD          ID_ = make_invd(P.dx, P.dy, P.dz);
 
   const int gi0 = P.gw + blockIdx.x * TX, gj0 = P.gw + blockIdx.y * TY;
   load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, 0, sQ);
@@ -233,7 +234,7 @@ hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       us[v] = (R)(S)u[v];
-    kmax = cand_key(hydro_invdt<R, NV>(us, C, P.dx, P.dy, P.dz));
+    kmax = cand_key(hydro_invdt<R, NV>(us, C, ID_));
   }
   block_max_commit<NT>(kmax, &clk->key[(step + 1) % 3]);
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
@@ -262,6 +263,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
     return;
   const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy), dtdz = (R)(dt / P.dz);
   const HydroConst<R> C = hydro_const<R>(P);
+  const InvD          ID_ = make_invd(P.dx, P.dy, P.dz);
 
   const int gw = P.gw;
   const int gi0 = gw + blockIdx.x * TX, gj0 = gw + blockIdx.y * TY;
@@ -442,7 +444,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
         Uout[v * P.vstride + off] = (S)x;
         us[v] = (R)(S)x;
       }
-      unsigned long long kk = cand_key(hydro_invdt<R, NV>(us, C, P.dx, P.dy, P.dz));
+      unsigned long long kk = cand_key(hydro_invdt<R, NV>(us, C, ID_));
       kmax = kk > kmax ? kk : kmax;
     }
     if (full && own)
@@ -476,6 +478,7 @@ __global__ void
 hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
 {
   const HydroConst<R> C = hydro_const<R>(P);
+  const InvD          ID_ = make_invd(P.dx, P.dy, P.dz);
   const long long     n = (long long)P.nx * P.ny * (NV == 5 ? P.nz : 1);
   unsigned long long  kmax = 0ull;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
@@ -491,7 +494,7 @@ hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       u[v] = (R)ldg(U + v * P.vstride + off);
-    unsigned long long kk = cand_key(hydro_invdt<R, NV>(u, C, P.dx, P.dy, P.dz));
+    unsigned long long kk = cand_key(hydro_invdt<R, NV>(u, C, ID_));
     kmax = kk > kmax ? kk : kmax;
   }
   block_max_commit<256>(kmax, key);

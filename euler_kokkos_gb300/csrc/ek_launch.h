@@ -20,8 +20,9 @@
                        unsigned long long * key, cudaStream_t st);                                  \
   cudaError_t mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key,         \
                      cudaStream_t st);                                                              \
-  cudaError_t mhd_step(int prec, const void * Uin, void * Uout, void * work, const KParams & P,     \
-                       DevClock * clk, int step, cudaStream_t st);                                  \
+  /* one MHD step = phase 0 (CFL), 1 (trace), 2 (fluxes, emfs, update) */                         \
+  cudaError_t mhd_step(int prec, int phase, const void * Uin, void * Uout, void * work,             \
+                       const KParams & P, DevClock * clk, int step, cudaStream_t st);               \
   size_t      mhd_work_bytes(int prec, const KParams & P);                                          \
   }
 

@@ -28,10 +28,12 @@ mhd_speed_fast(const R (&q)[8], R gamma0)
 }
 
 // find_speed_info<THREE_D> summed as ComputeDtFunctor3D_MHD does
-// (mhd_utils.h:319-366, MHDRunFunctors3D.h:58-76); FP64 result
+// (mhd_utils.h:319-366, MHDRunFunctors3D.h:58-76).  FP64: the reference's
+// expression; mixed: the candidate is formed in FP32 with 1/dx (the
+// max-reduction and dt stay FP64).
 template <class R>
 __device__ __forceinline__ double
-mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz)
+mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz, float idx, float idy, float idz)
 {
   const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
   const R b2 = a * a + b * b + c * c;
@@ -40,37 +42,32 @@ mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz)
   const R cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d));
   const R cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * b * b / d));
   const R cfz = sqrt(d2 + sqrt(d2 * d2 - c2 * c * c / d));
-  const double vx = (double)cfx + fabs((double)q[IU]);
-  const double vy = (double)cfy + fabs((double)q[IV]);
-  const double vz = (double)cfz + fabs((double)q[IW]);
-  return vx / dx + vy / dy + vz / dz;
+  const R vx = cfx + fabs(q[IU]);
+  const R vy = cfy + fabs(q[IV]);
+  const R vz = cfz + fabs(q[IW]);
+  if constexpr (sizeof(R) == 8)
+    return vx / dx + vy / dy + vz / dz;
+  else
+    return (double)(vx * idx + vy * idy + vz * idz);
 }
 
 // constoprim_mhd (MHDBaseFunctor3D.h:194-242).  u: hydro variables of the
-// cell, bl/br: face fields (left faces of this cell and of its +1 neighbours,
-// always FP64 storage).  In the mixed form the internal energy is recomputed
-// in FP64 when total and magnetic+kinetic energy cancel (low beta / high Mach).
-template <class R>
+// cell, bl/br: face fields of the cell and of its +1 neighbours.  In the
+// mixed form (R = float) the internal energy is recomputed in FP64 from the
+// FP64 face fields (bl64/br64, only read then) when total and
+// magnetic+kinetic energy cancel (low beta / high Mach).
+template <class R, class FB>
 __device__ __forceinline__ void
-mhd_constoprim(const R (&u)[5], const double (&bl)[3], const double (&br)[3], R (&q)[8],
-               const MhdConst<R> & C)
+mhd_constoprim(const R (&u)[5], const R (&bl)[3], const R (&br)[3], R (&q)[8], const MhdConst<R> & C,
+               FB && fp64_faces)
 {
   q[ID] = fmax(u[ID], C.smallr);
   q[IU] = u[IU] / q[ID];
   q[IV] = u[IV] / q[ID];
   q[IW] = u[IW] / q[ID];
-  if constexpr (sizeof(R) == 8)
-  {
-    q[IA] = 0.5 * (bl[0] + br[0]);
-    q[IB] = 0.5 * (bl[1] + br[1]);
-    q[IC] = 0.5 * (bl[2] + br[2]);
-  }
-  else
-  {
-    q[IA] = (R)(0.5 * (bl[0] + br[0]));
-    q[IB] = (R)(0.5 * (bl[1] + br[1]));
-    q[IC] = (R)(0.5 * (bl[2] + br[2]));
-  }
+  q[IA] = R(0.5) * (bl[0] + br[0]);
+  q[IB] = R(0.5) * (bl[1] + br[1]);
+  q[IC] = R(0.5) * (bl[2] + br[2]);
   const R eken = R(0.5) * (q[IU] * q[IU] + q[IV] * q[IV] + q[IW] * q[IW]);
   const R emag = R(0.5) * (q[IA] * q[IA] + q[IB] * q[IB] + q[IC] * q[IC]);
   R       eint = (u[IP] - emag) / q[ID] - eken;
@@ -79,7 +76,10 @@ mhd_constoprim(const R (&u)[5], const double (&bl)[3], const double (&br)[3], R 
     // FP64 island: E - emag - rho*eken cancels (low beta or high Mach)
     if (fabs(eint * q[ID]) < R(1.0 / 128.0) * fabs(u[IP]))
     {
-      const double ba = 0.5 * (bl[0] + br[0]), bb = 0.5 * (bl[1] + br[1]), bc = 0.5 * (bl[2] + br[2]);
+      double bl64[3], br64[3];
+      fp64_faces(bl64, br64);
+      const double ba = 0.5 * (bl64[0] + br64[0]), bb = 0.5 * (bl64[1] + br64[1]),
+                   bc = 0.5 * (bl64[2] + br64[2]);
       const double em = 0.5 * (ba * ba + bb * bb + bc * bc);
       const double d = (double)q[ID];
       const double vx = (double)u[IU] / d, vy = (double)u[IV] / d, vz = (double)u[IW] / d;

@@ -88,7 +88,21 @@ cell_prims_global(const MhdState<S> & m, const KParams & P, const MhdConst<R> & 
   br[0] = load_face<S>(m, P, src_cell(P, gi + 1, gj, gk), 0);
   br[1] = load_face<S>(m, P, src_cell(P, gi, gj + 1, gk), 1);
   br[2] = load_face<S>(m, P, src_cell(P, gi, gj, gk + 1), 2);
-  mhd_constoprim<R>(u, bl, br, q, C);
+  R blr[3], brr[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+  {
+    blr[c] = (R)bl[c];
+    brr[c] = (R)br[c];
+  }
+  mhd_constoprim<R>(u, blr, brr, q, C, [&](double (&a)[3], double (&b)[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+      a[c] = bl[c];
+      b[c] = br[c];
+    }
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -119,7 +133,7 @@ mhd_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step,
     const int       k = (int)(r / P.ny) + P.gw;
     R               q[8];
     cell_prims_global<S, R>(m, P, C, i, j, k, q);
-    const unsigned long long kk = cand_key(mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz));
+    const unsigned long long kk = cand_key(mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz, (float)(1.0 / P.dx), (float)(1.0 / P.dy), (float)(1.0 / P.dz)));
     kmax = kk > kmax ? kk : kmax;
   }
   block_max_commit<256>(kmax, key ? key : &clk->key[step % 3]);
@@ -143,7 +157,7 @@ struct TraceTile
 
 template <class R, int TX, int TY>
 __device__ __forceinline__ void
-trace_cell_compact(const double * sB, int bslot[4], const R * sQ, int qslot[3], const R * sE,
+trace_cell_compact(const R * sB, int bslot[4], const R * sQ, int qslot[3], const R * sE,
                    int eslot[2], int tx, int ty, R dtdx, R dtdy, R dtdz, const MhdConst<R> & C,
                    R * out, long long ost)
 {
@@ -305,8 +319,8 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
   using T = TraceTile<TX, TY>;
   constexpr int NT = TX * TY;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double * sB = reinterpret_cast<double *>(smem_raw);          // [4][3][BY][BX]
-  R *      sQ = reinterpret_cast<R *>(sB + 4 * T::BP);         // [3][8][QY][QX]
+  R * sB = reinterpret_cast<R *>(smem_raw); // [4][3][BY][BX] face fields (storage precision R)
+  R * sQ = sB + 4 * T::BP;                  // [3][8][QY][QX]
   R *      sE = sQ + 3 * T::QP;                                // [2][3][EY][EX]
 
   double t, dt;
@@ -323,29 +337,29 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
   const int nti = P.nx + 2, ntj = P.ny + 2; // trace cells per row / column
 
   auto load_B = [&](int gk, int slot) {
-    double * dst = sB + slot * T::BP;
+    R * dst = sB + slot * T::BP;
     for (int c = threadIdx.x; c < T::BX * T::BY; c += NT)
     {
       const int     x = c % T::BX, y = c / T::BX;
       const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
 #pragma unroll
       for (int comp = 0; comp < 3; ++comp)
-        dst[(comp * T::BY + y) * T::BX + x] = load_face<S>(m, P, s, comp);
+        dst[(comp * T::BY + y) * T::BX + x] = (R)load_face<S>(m, P, s, comp);
     }
   };
   // primitives of plane gk from the hydro variables and the face planes
   // bslot (gk) and bslot1 (gk+1)
   auto load_Q = [&](int gk, int slot, int bs0, int bs1) {
-    R * dst = sQ + slot * T::QP;
-    const double * B0 = sB + bs0 * T::BP;
-    const double * B1 = sB + bs1 * T::BP;
+    R *       dst = sQ + slot * T::QP;
+    const R * B0 = sB + bs0 * T::BP;
+    const R * B1 = sB + bs1 * T::BP;
     for (int c = threadIdx.x; c < T::QX * T::QY; c += NT)
     {
       const int     x = c % T::QX, y = c / T::QX;
       const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
       R             u[5], q[8];
       load_hydro<S, R>(m, P, s, u);
-      double bl[3], br[3];
+      R bl[3], br[3];
       // sB x index = global - (c0-1): the Q cell at x has B index x
       bl[0] = B0[(0 * T::BY + y) * T::BX + x];
       bl[1] = B0[(1 * T::BY + y) * T::BX + x];
@@ -353,7 +367,16 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
       br[0] = B0[(0 * T::BY + y) * T::BX + x + 1];
       br[1] = B0[(1 * T::BY + y + 1) * T::BX + x];
       br[2] = B1[(2 * T::BY + y) * T::BX + x];
-      mhd_constoprim<R>(u, bl, br, q, C);
+      const int gi = c0 - 1 + x, gj = d0 - 1 + y;
+      mhd_constoprim<R>(u, bl, br, q, C, [&](double (&a)[3], double (&b)[3]) {
+        // FP64 copies of the face fields for the cancellation island
+        a[0] = load_face<S>(m, P, s, 0);
+        a[1] = load_face<S>(m, P, s, 1);
+        a[2] = load_face<S>(m, P, s, 2);
+        b[0] = load_face<S>(m, P, src_cell(P, gi + 1, gj, gk), 0);
+        b[1] = load_face<S>(m, P, src_cell(P, gi, gj + 1, gk), 1);
+        b[2] = load_face<S>(m, P, src_cell(P, gi, gj, gk + 1), 2);
+      });
 #pragma unroll
       for (int v = 0; v < 8; ++v)
         dst[(v * T::QY + y) * T::QX + x] = q[v];
@@ -366,15 +389,15 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
     R *            dst = sE + slot * T::EP;
     const R *      Qa = sQ + qs0 * T::QP; // k-1
     const R *      Qb = sQ + qs1 * T::QP; // k
-    const double * Ba = sB + bs0 * T::BP;
-    const double * Bb = sB + bs1 * T::BP;
+    const R * Ba = sB + bs0 * T::BP;
+    const R * Bb = sB + bs1 * T::BP;
     for (int c = threadIdx.x; c < T::EX * T::EY; c += NT)
     {
       const int x = c % T::EX, y = c / T::EX; // E cell global = c0 + x
       const int qx = x + 1, qy = y + 1;       // sQ index of the same cell
       const int bx = x + 1, by = y + 1;       // sB index of the same cell
       auto      Q = [&](const R * pl, int v, int xx, int yy) { return pl[(v * T::QY + yy) * T::QX + xx]; };
-      auto      Bf = [&](const double * pl, int comp, int xx, int yy) {
+      auto      Bf = [&](const R * pl, int comp, int xx, int yy) {
         return (R)pl[(comp * T::BY + yy) * T::BX + xx];
       };
       R uu, vv, ww, A, B, Cc;
@@ -687,7 +710,7 @@ template <class R>
 constexpr size_t
 mhd_trace_smem(int TX, int TY)
 {
-  return sizeof(double) * 4 * 3 * (TX + 3) * (TY + 3) + sizeof(R) * (3 * 8 * (TX + 2) * (TY + 2) + 2 * 3 * (TX + 1) * (TY + 1));
+  return sizeof(R) * (4 * 3 * (TX + 3) * (TY + 3) + 3 * 8 * (TX + 2) * (TY + 2) + 2 * 3 * (TX + 1) * (TY + 1));
 }
 template <class R>
 constexpr size_t
@@ -702,19 +725,19 @@ constexpr int MU_TX = 16, MU_TY = 8; // update tile
 
 template <class S, class R>
 cudaError_t
-mhd_step_t(const void * Uin, void * Uout, void * work, const KParams & P, DevClock * clk, int step,
-           cudaStream_t st)
+mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams & P, DevClock * clk,
+           int step, cudaStream_t st)
 {
   // 1. dt of this step into clock slot step % 3
+  if (phase == 0)
   {
     const long long n = (long long)P.nx * P.ny * P.nz;
     const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     mhd_dt_kernel<S, R><<<blocks, 256, 0, st>>>(Uin, P, clk, step, nullptr);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess)
-      return e;
+    return cudaGetLastError();
   }
   // 2. trace
+  if (phase == 1)
   {
     auto       k = mhd_trace_kernel<S, R, MT_TX, MT_TY>;
     const int  sm = (int)mhd_trace_smem<R>(MT_TX, MT_TY);
@@ -724,9 +747,7 @@ mhd_step_t(const void * Uin, void * Uout, void * work, const KParams & P, DevClo
     const int nt = P.nz + 2;
     dim3      grid((P.nx + 2 + MT_TX - 1) / MT_TX, (P.ny + 2 + MT_TY - 1) / MT_TY, (nt + P.kchunk - 1) / P.kchunk);
     k<<<grid, MT_TX * MT_TY, sm, st>>>(Uin, (R *)work, P, clk, step);
-    e = cudaGetLastError();
-    if (e != cudaSuccess)
-      return e;
+    return cudaGetLastError();
   }
   // 3. fluxes, emfs, update
   {
@@ -742,17 +763,17 @@ mhd_step_t(const void * Uin, void * Uout, void * work, const KParams & P, DevClo
 }
 
 cudaError_t
-mhd_step(int prec, const void * Uin, void * Uout, void * work, const KParams & P, DevClock * clk,
-         int step, cudaStream_t st)
+mhd_step(int prec, int phase, const void * Uin, void * Uout, void * work, const KParams & P,
+         DevClock * clk, int step, cudaStream_t st)
 {
 #ifdef EK_EXACT_ONLY
   if (prec != 0)
     return cudaErrorNotSupported;
-  return mhd_step_t<double, double>(Uin, Uout, work, P, clk, step, st);
+  return mhd_step_t<double, double>(phase, Uin, Uout, work, P, clk, step, st);
 #else
   if (prec == 0)
-    return mhd_step_t<double, double>(Uin, Uout, work, P, clk, step, st);
-  return mhd_step_t<float, float>(Uin, Uout, work, P, clk, step, st);
+    return mhd_step_t<double, double>(phase, Uin, Uout, work, P, clk, step, st);
+  return mhd_step_t<float, float>(phase, Uin, Uout, work, P, clk, step, st);
 #endif
 }
 

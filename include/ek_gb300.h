@@ -140,6 +140,17 @@ ek_status ek_solver_synchronize(ek_solver * s);
 /* Number of kernel launches issued by this solver so far. */
 ek_status ek_solver_launch_count(ek_solver * s, long long * n);
 
+/* The CUDA stream (cudaStream_t) all work of the solver is issued on. */
+ek_status ek_solver_stream(ek_solver * s, void ** stream);
+
+/* Kernel timing with CUDA events recorded on the solver's stream around
+ * every launch of the step kernels (no counterpart in the reference, whose
+ * timers wrap whole phases: SolverBase.h:35-45, CudaTimer.h).  Enabling
+ * resets the accumulators.  kernel: 0 the fused step kernel (hydro) or the
+ * flux/emf/update kernel (MHD), 1 the MHD trace kernel, 2 the MHD CFL kernel. */
+ek_status ek_solver_set_profiling(ek_solver * s, int enable);
+ek_status ek_solver_kernel_time(ek_solver * s, int kernel, double * total_ms, long long * launches);
+
 #ifdef __cplusplus
 }
 #endif
