@@ -232,6 +232,63 @@ def cpu_sample(args, seconds=15.0):
                       (n, steps, cores, dt)}
 
 
+def ensemble_workload(ek, P, args, sync, maxt, world):
+    """The batched Kelvin-Helmholtz ensemble: args.ens_n instances with grids
+    from {64,96,128,192,256}^2, own shear / density ratio / dt each, FP32 with
+    FP64 totals, one persistent kernel per step replayed from a CUDA graph."""
+    import torch
+
+    cases = P.kh_ensemble(n_inst=args.ens_n, nsteps=10 ** 6)
+    params = [ek.params_from_ini(ini, precision=ek.EK_PREC_MIXED) for ini, _ in cases]
+    with ek.Ensemble(params) as e:
+        for i, (_, U0) in enumerate(cases):
+            e.set_state(i, U0)
+        info = e.info()
+        e.run(args.ens_steps, graph=True)  # capture, instantiate and warm up
+        e.synchronize()
+        st = torch.cuda.ExternalStream(e.stream())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sync()
+        l0 = e.info()["launches"]
+        e0.record(st)
+        e.run(args.ens_steps, graph=True)  # replay
+        e1.record(st)
+        sync()
+        ms = maxt(e0.elapsed_time(e1))
+        launches = e.info()["launches"] - l0
+        tot = e.totals()
+        t_last = [e.time(i)[0] for i in (0, len(cases) // 2, len(cases) - 1)]
+    cells = info["cells"]
+    value = cells * args.ens_steps / (ms / 1e3) / 1e6 * world
+    # CPU reference on a bounded sample: the first instances, a few steps each
+    cpu = None
+    if not args.no_cpu:
+        ensure_oracle()
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import eko
+
+        t0 = time.perf_counter()
+        done_cells = 0
+        for ini, U0 in cases[:8]:
+            p = eko.params_from_ini(ini)
+            o = eko.Oracle(p, U0)
+            n = len(o.run(10))
+            done_cells += p.nx * p.ny * n
+            o.close()
+        dt = time.perf_counter() - t0
+        cpu = {"value": done_cells / dt / 1e6, "unit": UNIT, "cores": eko.num_threads(), "kind": "port",
+               "sample": "first 8 instances x 10 steps, one after another (%.1f s)" % dt}
+    return {
+        "value": value, "unit": UNIT, "dtype": "f32", "instances": len(cases), "interior_cells": cells,
+        "steps": args.ens_steps, "ms_per_step": ms / args.ens_steps, "tiles_per_step": info["tiles"],
+        "persistent_grid": info["grid"], "gpu_launches": launches, "cuda_graph": True,
+        "fp64_total_mass_first": float(tot[0, 0]), "t_end_samples": t_last,
+        "cpu_baseline": cpu,
+        "config": "%d x Hydro_Muscl_2D Kelvin-Helmholtz, N in {64,96,128,192,256}^2, shear U[0.2,1], "
+                  "density ratio U[1.5,3], periodic x / reflecting y, HLLC, MC, CFL 0.8, own dt" % len(cases),
+    }
+
+
 def run_reference(args):
     """--impl reference: the reference algorithm's CPU restatement (the
     reference's own build cannot be compiled on the GPU host: Kokkos is not
@@ -282,6 +339,9 @@ def main():
     ap.add_argument("--mhd-steps", type=int, default=20)
     ap.add_argument("--no-mhd", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--ens-n", type=int, default=512)
+    ap.add_argument("--ens-steps", type=int, default=200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -375,6 +435,9 @@ def main():
             "roofline_fp64": roofline(m64, ("mhd3d", "fp64")),
             "config": "MHD_Muscl_3D Orszag-Tang %d^3, HLLD + CT, slope_type 2, CFL 0.8, periodic" % args.n,
         }
+
+    if not args.no_ensemble:
+        workloads["kh_ensemble_%d" % args.ens_n] = ensemble_workload(ek, P, args, sync, maxt, world)
 
     line = None
     if rank == 0:

@@ -27,6 +27,7 @@ __all__ = [
     "EkError",
     "Params",
     "Solver",
+    "Ensemble",
     "SolverFactory",
     "params_from_ini",
     "load_library",
@@ -133,6 +134,19 @@ def load_library():
         "ek_solver_set_profiling": (ctypes.c_int, [c_p, ctypes.c_int]),
         "ek_solver_kernel_time": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                                  ctypes.POINTER(ctypes.c_longlong)]),
+        "ek_ensemble_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int, ctypes.POINTER(c_p)]),
+        "ek_ensemble_destroy": (ctypes.c_int, [c_p]),
+        "ek_ensemble_set_state": (ctypes.c_int, [c_p, ctypes.c_int, c_p, ctypes.c_int]),
+        "ek_ensemble_get_state": (ctypes.c_int, [c_p, ctypes.c_int, c_p, ctypes.c_int]),
+        "ek_ensemble_run": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.c_int]),
+        "ek_ensemble_synchronize": (ctypes.c_int, [c_p]),
+        "ek_ensemble_time": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]),
+        "ek_ensemble_dt_history": (ctypes.c_int, [c_p, ctypes.c_int, c_p, ctypes.c_int]),
+        "ek_ensemble_totals": (ctypes.c_int, [c_p, c_p]),
+        "ek_ensemble_info": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int),
+                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong)]),
+        "ek_ensemble_stream": (ctypes.c_int, [c_p, ctypes.POINTER(c_p)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -284,6 +298,85 @@ class Solver:
         ms, n = ctypes.c_double(), ctypes.c_longlong()
         _check(self._L.ek_solver_kernel_time(self._h, kernel, ctypes.byref(ms), ctypes.byref(n)), "kernel_time")
         return ms.value, n.value
+
+
+class Ensemble:
+    """Independent Hydro_Muscl_2D runs stepped together by one persistent
+    kernel per step (optionally replayed from a CUDA graph)."""
+
+    def __init__(self, params_list):
+        L = load_library()
+        self._L = L
+        self.params = [p.copy() for p in params_list]
+        arr = (Params * len(self.params))(*self.params)
+        h = ctypes.c_void_p()
+        _check(L.ek_ensemble_create(arr, len(self.params), ctypes.byref(h)), "ek_ensemble_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ek_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.params)
+
+    def set_state(self, i: int, U: np.ndarray, layout: int = EK_LAYOUT_LEFT):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.size != int(np.prod(self.params[i].shape)):
+            raise ValueError("instance %d: state has %d values, expected %s" % (i, U.size, self.params[i].shape))
+        _check(self._L.ek_ensemble_set_state(self._h, i, U.ctypes.data, layout), "ensemble set_state")
+
+    def get_state(self, i: int) -> np.ndarray:
+        U = np.empty(self.params[i].shape, dtype=np.float64)
+        _check(self._L.ek_ensemble_get_state(self._h, i, U.ctypes.data, EK_LAYOUT_LEFT), "ensemble get_state")
+        return U
+
+    def run(self, nsteps: int, graph: bool = True):
+        _check(self._L.ek_ensemble_run(self._h, nsteps, int(graph)), "ensemble run")
+
+    def synchronize(self):
+        _check(self._L.ek_ensemble_synchronize(self._h), "ensemble synchronize")
+
+    def time(self, i: int):
+        t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        _check(self._L.ek_ensemble_time(self._h, i, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(it)), "time")
+        return t.value, dt.value, it.value
+
+    def dt_history(self, i: int) -> np.ndarray:
+        n = self.time(i)[2]
+        out = np.empty(n, dtype=np.float64)
+        if n:
+            _check(self._L.ek_ensemble_dt_history(self._h, i, out.ctypes.data, n), "dt_history")
+        return out
+
+    def totals(self) -> np.ndarray:
+        out = np.empty((len(self.params), 2), dtype=np.float64)
+        _check(self._L.ek_ensemble_totals(self._h, out.ctypes.data), "totals")
+        return out
+
+    def info(self):
+        c, t, g, l = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        _check(self._L.ek_ensemble_info(self._h, ctypes.byref(c), ctypes.byref(t), ctypes.byref(g),
+                                        ctypes.byref(l)), "info")
+        return {"cells": c.value, "tiles": t.value, "grid": g.value, "launches": l.value}
+
+    def stream(self) -> int:
+        p = ctypes.c_void_p()
+        _check(self._L.ek_ensemble_stream(self._h, ctypes.byref(p)), "stream")
+        return p.value or 0
 
 
 class SolverFactory:

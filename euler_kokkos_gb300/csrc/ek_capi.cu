@@ -60,6 +60,7 @@ struct ek_solver
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
   double                   kernel_ms[3] = { 0, 0, 0 };
   long long                kernel_n[3] = { 0, 0, 0 };
+  bool                     owns = true; // false: a view into an ensemble's buffers
 };
 
 static cudaEvent_t
@@ -138,23 +139,11 @@ ek_last_error(void)
   return ek_internal::g_last_error.c_str();
 }
 
-static size_t
-state_bytes_of(const ek_params & p, const KParams & kp)
+namespace ek_internal
 {
-  if (p.precision == EK_PREC_FP64)
-    return sizeof(double) * (size_t)kp.vstride * p.nbvar;
-  if (!p.mhd)
-    return sizeof(float) * (size_t)kp.vstride * p.nbvar;
-  return ekc::mixed_bfield_offset(kp.vstride) + sizeof(double) * 3 * (size_t)kp.vstride;
-}
-
-extern "C" ek_status
-ek_solver_create(const ek_params * params, ek_solver ** out)
+ek_status
+validate(const ek_params & p)
 {
-  if (!params || !out)
-    return fail(EK_ERR_INVALID, "ek_solver_create: null argument");
-  *out = nullptr;
-  const ek_params & p = *params;
   if (p.dim != 2 && p.dim != 3)
     return fail(EK_ERR_INVALID, "dim must be 2 or 3");
   if (p.nx < 1 || p.ny < 1 || (p.dim == 3 && p.nz < 1))
@@ -183,18 +172,17 @@ ek_solver_create(const ek_params * params, ek_solver ** out)
     return fail(EK_ERR_UNSUPPORTED, "isothermal and shearing-box terms are not implemented");
   if (p.exact_fp && p.precision != EK_PREC_FP64)
     return fail(EK_ERR_INVALID, "exact_fp requires precision fp64");
+  if (p.precision != EK_PREC_FP64 && p.precision != EK_PREC_MIXED)
+    return fail(EK_ERR_INVALID, "precision must be EK_PREC_FP64 or EK_PREC_MIXED");
+  return EK_OK;
+}
 
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
-    return fail(EK_ERR_NO_DEVICE, "no CUDA device available");
-
-  ek_solver * s = new ek_solver();
-  s->p = p;
-  s->prec = p.precision;
-  s->exact = p.exact_fp != 0;
-  cudaGetDevice(&s->device);
-  KParams & k = s->kp;
+ekc::KParams
+make_kparams(const ek_params & p)
+{
+  ekc::KParams k;
   std::memset(&k, 0, sizeof k);
+  const int gw = p.mhd ? 3 : 2;
   k.nx = p.nx;
   k.ny = p.ny;
   k.nz = p.dim == 3 ? p.nz : 1;
@@ -220,8 +208,45 @@ ek_solver_create(const ek_params * params, ek_solver ** out)
   k.cIso = p.cIso;
   k.riemann = p.riemann;
   k.kchunk = p.kchunk > 0 ? p.kchunk : (k.nz <= 64 ? k.nz : 64);
+  return k;
+}
 
-  s->state_bytes = state_bytes_of(p, k);
+size_t
+state_bytes(const ek_params & p, const ekc::KParams & kp)
+{
+  if (p.precision == EK_PREC_FP64)
+    return sizeof(double) * (size_t)kp.vstride * p.nbvar;
+  if (!p.mhd)
+    return sizeof(float) * (size_t)kp.vstride * p.nbvar;
+  return ekc::mixed_bfield_offset(kp.vstride) + sizeof(double) * 3 * (size_t)kp.vstride;
+}
+} // namespace ek_internal
+
+extern "C" ek_status
+ek_solver_create(const ek_params * params, ek_solver ** out)
+{
+  if (!params || !out)
+    return fail(EK_ERR_INVALID, "ek_solver_create: null argument");
+  *out = nullptr;
+  const ek_params & p = *params;
+  {
+    ek_status v = ek_internal::validate(p);
+    if (v != EK_OK)
+      return v;
+  }
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(EK_ERR_NO_DEVICE, "no CUDA device available");
+
+  ek_solver * s = new ek_solver();
+  s->p = p;
+  s->prec = p.precision;
+  s->exact = p.exact_fp != 0;
+  cudaGetDevice(&s->device);
+  s->kp = ek_internal::make_kparams(p);
+  const KParams & k = s->kp;
+  s->state_bytes = ek_internal::state_bytes(p, k);
   cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess)
     e = cudaMalloc(&s->U[0], s->state_bytes);
@@ -259,6 +284,12 @@ ek_solver_destroy(ek_solver * s)
 {
   if (!s)
     return EK_OK;
+  if (!s->owns)
+  {
+    drain_events(s);
+    delete s;
+    return EK_OK;
+  }
   if (s->stream)
     cudaStreamSynchronize(s->stream);
   cudaFree(s->U[0]);
@@ -740,5 +771,336 @@ ek_solver_kernel_time(ek_solver * s, int kernel, double * total_ms, long long * 
     *total_ms = s->kernel_ms[kernel];
   if (launches)
     *launches = s->kernel_n[kernel];
+  return EK_OK;
+}
+
+// ===========================================================================
+// Ensemble of independent 2D hydro runs
+// ===========================================================================
+struct ek_ensemble
+{
+  int                      n = 0;
+  int                      prec = 0;
+  bool                     exact = false;
+  cudaStream_t             stream = nullptr;
+  std::vector<ek_solver *> views; // per-instance views (no own device memory)
+  void *                   states = nullptr; // all ping-pong states
+  DevClock *               clocks = nullptr;
+  double *                 dtlogs = nullptr;
+  ekc::EnsInstance *       d_insts = nullptr;
+  ekc::EnsTile *           d_tiles = nullptr;
+  int *                    d_step = nullptr;
+  double *                 d_totals = nullptr;
+  int                      ntiles = 0;
+  int                      grid = 0;
+  int                      step = 0; // host copy of the device step counter
+  long long                cells = 0;
+  long long                launches = 0;
+  cudaGraph_t              graph = nullptr;
+  cudaGraphExec_t          graph_exec = nullptr;
+  int                      graph_steps = 0;
+};
+
+extern "C" ek_status ek_ensemble_time(ek_ensemble * e, int i, double * t, double * dt, int * iteration);
+
+extern "C" ek_status
+ek_ensemble_destroy(ek_ensemble * e)
+{
+  if (!e)
+    return EK_OK;
+  if (e->stream)
+    cudaStreamSynchronize(e->stream);
+  for (auto v : e->views)
+    ek_solver_destroy(v);
+  if (e->graph_exec)
+    cudaGraphExecDestroy(e->graph_exec);
+  if (e->graph)
+    cudaGraphDestroy(e->graph);
+  cudaFree(e->states);
+  cudaFree(e->clocks);
+  cudaFree(e->dtlogs);
+  cudaFree(e->d_insts);
+  cudaFree(e->d_tiles);
+  cudaFree(e->d_step);
+  cudaFree(e->d_totals);
+  if (e->stream)
+    cudaStreamDestroy(e->stream);
+  delete e;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_ensemble_create(const ek_params * params, int n, ek_ensemble ** out)
+{
+  if (!params || n < 1 || !out)
+    return fail(EK_ERR_INVALID, "ek_ensemble_create: bad argument");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i)
+  {
+    const ek_params & p = params[i];
+    ek_status v = ek_internal::validate(p);
+    if (v != EK_OK)
+      return fail(v, "instance " + std::to_string(i) + ": " + ek_last_error());
+    if (p.dim != 2 || p.mhd)
+      return fail(EK_ERR_UNSUPPORTED, "ensembles hold Hydro_Muscl_2D runs");
+    if (p.precision != params[0].precision || p.exact_fp != params[0].exact_fp)
+      return fail(EK_ERR_INVALID, "all instances of an ensemble share precision and exact_fp");
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(EK_ERR_NO_DEVICE, "no CUDA device available");
+
+  ek_ensemble * e = new ek_ensemble();
+  e->n = n;
+  e->prec = params[0].precision;
+  e->exact = params[0].exact_fp != 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  // layout: instance i owns two states at offsets off[i], off[i] + bytes[i]
+  std::vector<size_t> off(n), bytes(n);
+  size_t              total = 0;
+  int                 dtcap = 1;
+  for (int i = 0; i < n; ++i)
+  {
+    ekc::KParams k = ek_internal::make_kparams(params[i]);
+    bytes[i] = (ek_internal::state_bytes(params[i], k) + 255) / 256 * 256;
+    off[i] = total;
+    total += 2 * bytes[i];
+    const int cap = params[i].nStepmax > 0 ? (params[i].nStepmax < (1 << 20) ? params[i].nStepmax + 1 : (1 << 20)) : 1;
+    dtcap = cap > dtcap ? cap : dtcap;
+    e->cells += (long long)params[i].nx * params[i].ny;
+  }
+  cudaError_t err = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+  if (err == cudaSuccess)
+    err = cudaMalloc(&e->states, total);
+  if (err == cudaSuccess)
+    err = cudaMemsetAsync(e->states, 0, total, e->stream);
+  if (err == cudaSuccess)
+    err = cudaMalloc((void **)&e->clocks, sizeof(DevClock) * n);
+  if (err == cudaSuccess)
+    err = cudaMalloc((void **)&e->dtlogs, sizeof(double) * (size_t)dtcap * n);
+  if (err == cudaSuccess)
+    err = cudaMalloc((void **)&e->d_insts, sizeof(ekc::EnsInstance) * n);
+  if (err == cudaSuccess)
+    err = cudaMalloc((void **)&e->d_step, sizeof(int));
+  if (err == cudaSuccess)
+    err = cudaMemsetAsync(e->d_step, 0, sizeof(int), e->stream);
+  if (err == cudaSuccess)
+    err = cudaMalloc((void **)&e->d_totals, 2 * sizeof(double) * n);
+  std::vector<ekc::EnsInstance> h_insts(n);
+  std::vector<ekc::EnsTile>     tiles;
+  if (err == cudaSuccess)
+  {
+    for (int i = 0; i < n; ++i)
+    {
+      ek_solver * v = new ek_solver();
+      v->owns = false;
+      v->p = params[i];
+      v->kp = ek_internal::make_kparams(params[i]);
+      v->prec = e->prec;
+      v->exact = e->exact;
+      v->device = dev;
+      v->stream = e->stream;
+      v->state_bytes = ek_internal::state_bytes(params[i], v->kp);
+      v->U[0] = (char *)e->states + off[i];
+      v->U[1] = (char *)e->states + off[i] + bytes[i];
+      v->clk = e->clocks + i;
+      v->dtlog = e->dtlogs + (size_t)i * dtcap;
+      v->dtcap = dtcap;
+      v->scratch3 = nullptr;
+      e->views.push_back(v);
+      h_insts[i].P = v->kp;
+      h_insts[i].U[0] = v->U[0];
+      h_insts[i].U[1] = v->U[1];
+      h_insts[i].clk = v->clk;
+      // 32 x 8 tiles of the 2D step kernel, instance-major
+      const int tx = (params[i].nx + 31) / 32, ty = (params[i].ny + 7) / 8;
+      for (int by = 0; by < ty; ++by)
+        for (int bx = 0; bx < tx; ++bx)
+          tiles.push_back({ i, bx, by });
+    }
+    e->ntiles = (int)tiles.size();
+    err = cudaMalloc((void **)&e->d_tiles, sizeof(ekc::EnsTile) * tiles.size());
+  }
+  if (err == cudaSuccess)
+    err = cudaMemcpyAsync(e->d_insts, h_insts.data(), sizeof(ekc::EnsInstance) * n, cudaMemcpyHostToDevice,
+                          e->stream);
+  if (err == cudaSuccess)
+    err = cudaMemcpyAsync(e->d_tiles, tiles.data(), sizeof(ekc::EnsTile) * tiles.size(),
+                          cudaMemcpyHostToDevice, e->stream);
+  if (err == cudaSuccess)
+    err = cudaStreamSynchronize(e->stream);
+  if (err != cudaSuccess)
+  {
+    ek_status st = cuda_fail(err, "ek_ensemble_create");
+    ek_ensemble_destroy(e);
+    return st;
+  }
+  e->grid = e->exact ? ek_exact::ensemble2d_grid(e->prec) : ek_fast::ensemble2d_grid(e->prec);
+  *out = e;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_ensemble_set_state(ek_ensemble * e, int i, const double * U, int layout)
+{
+  if (!e || i < 0 || i >= e->n)
+    return fail(EK_ERR_INVALID, "ek_ensemble_set_state: bad instance");
+  if (e->step != 0)
+    return fail(EK_ERR_INVALID, "ek_ensemble_set_state: states are set before the first step");
+  return ek_solver_set_state(e->views[i], U, layout);
+}
+
+extern "C" ek_status
+ek_ensemble_get_state(ek_ensemble * e, int i, double * U, int layout)
+{
+  if (!e || i < 0 || i >= e->n)
+    return fail(EK_ERR_INVALID, "ek_ensemble_get_state: bad instance");
+  double    t, dt;
+  int       it;
+  ek_status st = ek_ensemble_time(e, i, &t, &dt, &it); // current buffer follows the device clock
+  if (st != EK_OK)
+    return st;
+  return ek_solver_get_state(e->views[i], U, layout);
+}
+
+static ek_status
+ensemble_launch_steps(ek_ensemble * e, int nsteps)
+{
+  for (int k = 0; k < nsteps; ++k)
+  {
+    cudaError_t err = e->exact ? ek_exact::ensemble2d_step(e->prec, e->d_insts, e->d_tiles, e->ntiles,
+                                                           e->d_step, e->grid, e->stream)
+                               : ek_fast::ensemble2d_step(e->prec, e->d_insts, e->d_tiles, e->ntiles,
+                                                          e->d_step, e->grid, e->stream);
+    if (err != cudaSuccess)
+      return cuda_fail(err, "ensemble step");
+  }
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_ensemble_run(ek_ensemble * e, int nsteps, int use_graph)
+{
+  if (!e || nsteps < 0)
+    return fail(EK_ERR_INVALID, "ek_ensemble_run: bad argument");
+  for (auto v : e->views)
+    if (!v->has_state)
+      return fail(EK_ERR_INVALID, "ek_ensemble_run: every instance needs a state");
+  if (nsteps == 0)
+    return EK_OK;
+  if (!use_graph)
+  {
+    ek_status st = ensemble_launch_steps(e, nsteps);
+    if (st != EK_OK)
+      return st;
+  }
+  else
+  {
+    if (!e->graph_exec || e->graph_steps != nsteps)
+    {
+      if (e->graph_exec)
+        cudaGraphExecDestroy(e->graph_exec);
+      if (e->graph)
+        cudaGraphDestroy(e->graph);
+      e->graph_exec = nullptr;
+      e->graph = nullptr;
+      EK_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+      ek_status st = ensemble_launch_steps(e, nsteps);
+      cudaGraph_t g = nullptr;
+      cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+      if (st != EK_OK)
+        return st;
+      EK_CUDA(ce, "graph capture");
+      e->graph = g;
+      EK_CUDA(cudaGraphInstantiate(&e->graph_exec, e->graph, 0), "graph instantiate");
+      e->graph_steps = nsteps;
+    }
+    EK_CUDA(cudaGraphLaunch(e->graph_exec, e->stream), "graph launch");
+  }
+  e->launches += 2LL * nsteps;
+  e->step += nsteps;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_ensemble_synchronize(ek_ensemble * e)
+{
+  if (!e)
+    return fail(EK_ERR_INVALID, "ek_ensemble_synchronize: null ensemble");
+  EK_CUDA(cudaStreamSynchronize(e->stream), "synchronize");
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_ensemble_time(ek_ensemble * e, int i, double * t, double * dt, int * iteration)
+{
+  if (!e || i < 0 || i >= e->n)
+    return fail(EK_ERR_INVALID, "ek_ensemble_time: bad instance");
+  ek_solver * v = e->views[i];
+  DevClock    h;
+  ek_status   st = read_clock(v, &h);
+  if (st != EK_OK)
+    return st;
+  v->iteration = h.iteration;
+  v->t = h.t[h.iteration % 3];
+  if (h.iteration > 0 && h.iteration - 1 < v->dtcap)
+    EK_CUDA(cudaMemcpy(&v->dt, v->dtlog + (h.iteration - 1), sizeof(double), cudaMemcpyDeviceToHost), "dt");
+  return ek_solver_time(v, t, dt, iteration);
+}
+
+extern "C" ek_status
+ek_ensemble_dt_history(ek_ensemble * e, int i, double * dts, int n)
+{
+  if (!e || i < 0 || i >= e->n)
+    return fail(EK_ERR_INVALID, "ek_ensemble_dt_history: bad instance");
+  double t, dt;
+  int    it;
+  ek_status st = ek_ensemble_time(e, i, &t, &dt, &it);
+  if (st != EK_OK)
+    return st;
+  return ek_solver_dt_history(e->views[i], dts, n);
+}
+
+extern "C" ek_status
+ek_ensemble_totals(ek_ensemble * e, double * out)
+{
+  if (!e || !out)
+    return fail(EK_ERR_INVALID, "ek_ensemble_totals: bad argument");
+  EK_CUDA(ek_fast::ensemble_totals(e->prec, e->d_insts, e->n, e->d_step, e->d_totals, e->stream), "totals");
+  EK_CUDA(cudaMemcpyAsync(out, e->d_totals, 2 * sizeof(double) * e->n, cudaMemcpyDeviceToHost, e->stream),
+          "totals");
+  EK_CUDA(cudaStreamSynchronize(e->stream), "totals");
+  for (int i = 0; i < e->n; ++i)
+  {
+    const double cell = e->views[i]->p.dx * e->views[i]->p.dy;
+    out[2 * i] *= cell;
+    out[2 * i + 1] *= cell;
+  }
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_ensemble_info(ek_ensemble * e, long long * interior_cells, int * tiles, int * grid, long long * launches)
+{
+  if (!e)
+    return fail(EK_ERR_INVALID, "ek_ensemble_info: null ensemble");
+  if (interior_cells)
+    *interior_cells = e->cells;
+  if (tiles)
+    *tiles = e->ntiles;
+  if (grid)
+    *grid = e->grid;
+  if (launches)
+    *launches = e->launches;
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_ensemble_stream(ek_ensemble * e, void ** stream)
+{
+  if (!e || !stream)
+    return fail(EK_ERR_INVALID, "ek_ensemble_stream: bad argument");
+  *stream = (void *)e->stream;
   return EK_OK;
 }

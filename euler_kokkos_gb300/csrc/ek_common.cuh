@@ -74,6 +74,18 @@ enum : int
   EK_DEVERR_NONFINITE_DT = 1,
 };
 
+// One instance of an ensemble of independent runs and one tile of work.
+struct EnsInstance
+{
+  KParams    P;
+  void *     U[2]; // ping-pong states
+  DevClock * clk;
+};
+struct EnsTile
+{
+  int inst, bx, by;
+};
+
 // Mixed-precision MHD state: 5 FP32 hydro planes, then (256-byte aligned) the
 // 3 FP64 face-field planes.
 __host__ __device__ inline size_t

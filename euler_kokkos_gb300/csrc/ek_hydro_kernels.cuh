@@ -76,15 +76,16 @@ cell_slopes(const R * q0, const R * qm, const R * qp, int hx, int hy, R st, R (&
 }
 
 // ---------------------------------------------------------------------------
-// 2D: one CTA = one TX x TY tile of interior cells
+// 2D: one CTA = one TX x TY tile of interior cells.  hydro2d_tile is the tile
+// body shared by the single-solver kernel and the ensemble kernel.
 // ---------------------------------------------------------------------------
 template <class S, class R, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY)
-hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
+__device__ __forceinline__ void
+hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & P, DevClock * clk,
+             int step, int bx, int by, unsigned char * smem_raw)
 {
   constexpr int NV = 4, HX = TX + 4, HY = TY + 4, NT = TX * TY;
   constexpr int FX = TX + 2; // face-state rows in x: cells -1..TX
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   R * sQ = reinterpret_cast<R *>(smem_raw);  // [NV][HY][HX]
   R * sXm = sQ + NV * HY * HX;               // XMIN state of cells -1..TX, then x-flux
   R * sXp = sXm + NV * TY * FX;              // XMAX state
@@ -98,7 +99,7 @@ hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   const HydroConst<R> C = hydro_const<R>(P);
   const InvD          ID_ = make_invd(P.dx, P.dy, P.dz);
 
-  const int gi0 = P.gw + blockIdx.x * TX, gj0 = P.gw + blockIdx.y * TY;
+  const int gi0 = P.gw + bx * TX, gj0 = P.gw + by * TY;
   load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, 0, sQ);
   __syncthreads();
 
@@ -237,9 +238,78 @@ hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
     kmax = cand_key(hydro_invdt<R, NV>(us, C, ID_));
   }
   block_max_commit<NT>(kmax, &clk->key[(step + 1) % 3]);
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
+  if (bx == 0 && by == 0 && threadIdx.x == 0)
     step_commit(clk, step, t, dt);
 }
+
+template <class S, class R, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY)
+hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  hydro2d_tile<S, R, TX, TY>(Uin, Uout, P, clk, step, blockIdx.x, blockIdx.y, smem_raw);
+}
+
+// ---------------------------------------------------------------------------
+// Ensemble of independent 2D runs (uneven grids, own dt each): a persistent
+// kernel walks the flat (instance, tile) work list; one launch = one step of
+// every instance.  No inter-block waits.
+// ---------------------------------------------------------------------------
+template <class S, class R, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY)
+ensemble2d_step(const EnsInstance * __restrict__ insts, const EnsTile * __restrict__ tiles, int ntiles,
+                const int * __restrict__ stepc)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // the step number lives in device memory (advanced by ensemble_advance after
+  // every step), so a captured sequence of steps can be replayed as is
+  const int step = *stepc;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
+  {
+    const EnsTile      w = tiles[t];
+    const EnsInstance & in = insts[w.inst];
+    hydro2d_tile<S, R, TX, TY>((const S *)in.U[step % 2], (S *)in.U[(step + 1) % 2], in.P, in.clk, step,
+                               w.bx, w.by, smem_raw);
+    __syncthreads(); // shared tiles are reused by the next work item
+  }
+}
+
+__global__ void
+ensemble_advance(int * stepc)
+{
+  *stepc += 1;
+}
+
+// FP64 mass and total energy of every instance (blockIdx.y = instance)
+template <class S>
+__global__ void
+ensemble_totals_kernel(const EnsInstance * __restrict__ insts, const int * __restrict__ stepc,
+                       double * __restrict__ out)
+{
+  const EnsInstance & in = insts[blockIdx.y];
+  const KParams &     P = in.P;
+  const S *           U = (const S *)in.U[*stepc % 2];
+  const long long     n = (long long)P.nx * P.ny;
+  double              m = 0.0, e = 0.0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x)
+  {
+    const long long off = (long long)(c / P.nx + P.gw) * P.isize + (c % P.nx + P.gw);
+    m += (double)U[off];
+    e += (double)U[P.vstride + off];
+  }
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    m += __shfl_xor_sync(0xffffffffu, m, o);
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+  }
+  if ((threadIdx.x & 31) == 0)
+  {
+    atomicAdd(out + 2 * blockIdx.y, m);
+    atomicAdd(out + 2 * blockIdx.y + 1, e);
+  }
+}
+
 
 // ---------------------------------------------------------------------------
 // 3D: one CTA = a TX x TY column of interior cells marching over kchunk planes

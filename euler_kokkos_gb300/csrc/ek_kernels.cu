@@ -99,6 +99,65 @@ hydro_dt(int dim, int prec, const void * U, const KParams & P, unsigned long lon
 #endif
 }
 
+namespace
+{
+template <class S, class R>
+cudaError_t
+ensemble2d_t(const EnsInstance * insts, const EnsTile * tiles, int ntiles, int * stepc, int grid,
+             cudaStream_t st)
+{
+  auto        k = ensemble2d_step<S, R, H2_TX, H2_TY>;
+  size_t      sm = hydro2d_smem<R>();
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess)
+    return e;
+  k<<<grid, H2_TX * H2_TY, sm, st>>>(insts, tiles, ntiles, stepc);
+  e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return e;
+  ensemble_advance<<<1, 1, 0, st>>>(stepc);
+  return cudaGetLastError();
+}
+template <class S, class R>
+int
+ensemble2d_grid_t()
+{
+  auto   k = ensemble2d_step<S, R, H2_TX, H2_TY>;
+  size_t sm = hydro2d_smem<R>();
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int per_sm = 0, dev = 0, nsm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, H2_TX * H2_TY, sm);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return (per_sm > 0 ? per_sm : 1) * (nsm > 0 ? nsm : 1);
+}
+} // namespace
+
+cudaError_t
+ensemble2d_step(int prec, const EnsInstance * insts, const EnsTile * tiles, int ntiles, int * stepc,
+                int grid, cudaStream_t st)
+{
+#ifdef EK_EXACT_ONLY
+  if (prec != 0)
+    return cudaErrorNotSupported;
+  return ensemble2d_t<double, double>(insts, tiles, ntiles, stepc, grid, st);
+#else
+  if (prec == 0)
+    return ensemble2d_t<double, double>(insts, tiles, ntiles, stepc, grid, st);
+  return ensemble2d_t<float, float>(insts, tiles, ntiles, stepc, grid, st);
+#endif
+}
+
+int
+ensemble2d_grid(int prec)
+{
+#ifdef EK_EXACT_ONLY
+  return ensemble2d_grid_t<double, double>();
+#else
+  return prec == 0 ? ensemble2d_grid_t<double, double>() : ensemble2d_grid_t<float, float>();
+#endif
+}
+
 #ifndef EK_EXACT_ONLY
 namespace
 {
@@ -149,6 +208,21 @@ fill_ghosts(int prec, void * U, const KParams & P, int nbvar, cudaStream_t st)
     fill_ghosts_kernel<float><<<blocks, 256, 0, st>>>((float *)U, P, 5, 0);
     fill_ghosts_kernel<double><<<blocks, 256, 0, st>>>(mixed_bfield(U, P), P, 3, 5);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t
+ensemble_totals(int prec, const EnsInstance * insts, int n, const int * stepc, double * out,
+                cudaStream_t st)
+{
+  cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(double) * n, st);
+  if (e != cudaSuccess)
+    return e;
+  dim3 grid(16, n);
+  if (prec == 0)
+    ensemble_totals_kernel<double><<<grid, 256, 0, st>>>(insts, stepc, out);
+  else
+    ensemble_totals_kernel<float><<<grid, 256, 0, st>>>(insts, stepc, out);
   return cudaGetLastError();
 }
 

@@ -24,6 +24,10 @@
   cudaError_t mhd_step(int prec, int phase, const void * Uin, void * Uout, void * work,             \
                        const KParams & P, DevClock * clk, int step, cudaStream_t st);               \
   size_t      mhd_work_bytes(int prec, const KParams & P);                                          \
+  /* one step of every instance of a 2D hydro ensemble (persistent kernel) */                       \
+  cudaError_t ensemble2d_step(int prec, const ekc::EnsInstance * insts, const ekc::EnsTile * tiles,  \
+                              int ntiles, int * stepc, int grid, cudaStream_t st);                  \
+  int         ensemble2d_grid(int prec);                                                            \
   }
 
 EK_DECLARE_LAUNCHERS(ek_exact)
@@ -36,4 +40,6 @@ using ekc::KParams;
 cudaError_t fill_ghosts(int prec, void * U, const KParams & P, int nbvar, cudaStream_t st);
 cudaError_t totals(int prec, const void * U, const KParams & P, int nbvar, double * out3,
                    cudaStream_t st);
+cudaError_t ensemble_totals(int prec, const ekc::EnsInstance * insts, int n, const int * stepc,
+                            double * out, cudaStream_t st);
 } // namespace ek_fast

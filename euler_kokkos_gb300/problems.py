@@ -27,6 +27,8 @@ __all__ = [
     "orszag_tang_3d",
     "mhd_blast_3d",
     "kelvin_helmholtz_2d",
+    "kh_ensemble",
+    "smooth_random",
     "ini_text",
 ]
 
@@ -336,3 +338,21 @@ def smooth_random(dim=3, mhd=False, nx=16, ny=None, nz=None, seed=1, bc=None, sl
     U[1] = pr / (g - 1.0) + 0.5 * rho * (vel[0] ** 2 + vel[1] ** 2 + vel[2] ** 2) \
         + 0.5 * (bxc ** 2 + byc ** 2 + bzc ** 2)
     return ini, U
+
+
+KH_SIZES = (64, 96, 128, 192, 256)
+
+
+def kh_ensemble(n_inst=512, seed=20261203, nsteps=200, sizes=KH_SIZES):
+    """The batched Kelvin-Helmholtz workload: instance n draws its grid from
+    ``sizes`` (squared), its shear speed from U[0.2, 1.0] and its density ratio
+    from U[1.5, 3] with splitmix64(seed + n); each instance is periodic in x,
+    reflecting in y, with a seeded 1% velocity perturbation."""
+    out = []
+    for n in range(n_inst):
+        r = splitmix_uniform(seed + n, np.arange(3, dtype=np.uint64))  # U[-1, 1)
+        size = sizes[int((r[0] + 1.0) / 2.0 * len(sizes)) % len(sizes)]
+        shear = 0.2 + 0.8 * (r[1] + 1.0) / 2.0
+        ratio = 1.5 + 1.5 * (r[2] + 1.0) / 2.0
+        out.append(kelvin_helmholtz_2d(n=size, shear=shear, ratio=ratio, seed=seed + 7919 * n, nsteps=nsteps))
+    return out

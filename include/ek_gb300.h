@@ -151,6 +151,37 @@ ek_status ek_solver_stream(ek_solver * s, void ** stream);
 ek_status ek_solver_set_profiling(ek_solver * s, int enable);
 ek_status ek_solver_kernel_time(ek_solver * s, int kernel, double * total_ms, long long * launches);
 
+/* ---------------------------------------------------------------------------
+ * Ensembles of independent Hydro_Muscl_2D runs (no counterpart in the
+ * reference, which runs one problem per process): every instance has its own
+ * grid size, parameters, boundary conditions and time step.  One step of all
+ * instances is one persistent kernel over a flat (instance, tile) work list;
+ * ek_ensemble_run can capture the steps in a CUDA graph and replay it.
+ * ------------------------------------------------------------------------- */
+typedef struct ek_ensemble ek_ensemble;
+
+/* n parameter sets (all 2D hydro, same precision and exact_fp) */
+ek_status ek_ensemble_create(const ek_params * params, int n, ek_ensemble ** out);
+ek_status ek_ensemble_destroy(ek_ensemble * e);
+/* inject the state of instance i (before the first step), as ek_solver_set_state */
+ek_status ek_ensemble_set_state(ek_ensemble * e, int i, const double * U, int layout);
+ek_status ek_ensemble_get_state(ek_ensemble * e, int i, double * U, int layout);
+/* nsteps steps of every instance (instances past their tEnd stay put);
+ * use_graph = 1 captures the nsteps launches in one CUDA graph and replays it
+ * on later calls with the same nsteps.  Asynchronous: see ek_ensemble_synchronize. */
+ek_status ek_ensemble_run(ek_ensemble * e, int nsteps, int use_graph);
+ek_status ek_ensemble_synchronize(ek_ensemble * e);
+/* m_t, m_dt and m_iteration of instance i */
+ek_status ek_ensemble_time(ek_ensemble * e, int i, double * t, double * dt, int * iteration);
+ek_status ek_ensemble_dt_history(ek_ensemble * e, int i, double * dts, int n);
+/* FP64 totals per instance: out[2i] mass, out[2i+1] total energy */
+ek_status ek_ensemble_totals(ek_ensemble * e, double * out);
+/* interior cells over all instances, work tiles per step, persistent grid size,
+ * kernel launches issued */
+ek_status ek_ensemble_info(ek_ensemble * e, long long * interior_cells, int * tiles, int * grid,
+                           long long * launches);
+ek_status ek_ensemble_stream(ek_ensemble * e, void ** stream);
+
 #ifdef __cplusplus
 }
 #endif
