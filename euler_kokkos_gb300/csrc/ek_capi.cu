@@ -208,6 +208,14 @@ make_kparams(const ek_params & p)
   k.cIso = p.cIso;
   k.riemann = p.riemann;
   k.kchunk = p.kchunk > 0 ? p.kchunk : (k.nz <= 64 ? k.nz : 64);
+  k.gamma0f = (float)p.gamma0;
+  k.smallrf = (float)p.smallr;
+  k.smallcf = (float)p.smallc;
+  k.smallpf = (float)p.smallp;
+  k.slopef = (float)p.slope_type;
+  k.idx = (float)(1.0 / p.dx);
+  k.idy = (float)(1.0 / p.dy);
+  k.idz = (float)(1.0 / (p.dim == 3 ? p.dz : 1.0));
   return k;
 }
 

@@ -53,6 +53,10 @@ struct KParams
   double    gamma0, smallr, smallc, smallp, slope_type, cfl, tEnd, cIso;
   int       riemann;
   int       kchunk; // interior planes per CTA (3D kernels)
+  // FP32 copies prepared on the host, so that mixed kernels do no per-thread
+  // FP64 arithmetic (one FP64 instruction costs 64 FP32 ones on GB300)
+  float     gamma0f, smallrf, smallcf, smallpf, slopef;
+  float     idx, idy, idz; // 1/dx, 1/dy, 1/dz
 };
 
 // Per-step scalars kept on the device so that consecutive steps need no host
@@ -232,6 +236,33 @@ step_dt(const KParams & P, const DevClock * clk, int step, double * t, double * 
   *t = tt;
   *dt = d;
   return !(tt >= P.tEnd - 1e-14);
+}
+
+// Step scalars computed once per CTA by thread 0 and shared: dt and the
+// dt/dx ratios (the FP64 divisions would otherwise run in every thread).
+template <class R>
+struct StepScalars
+{
+  double t, dt;
+  R      dtdx, dtdy, dtdz;
+  int    active;
+};
+template <class R>
+__device__ __forceinline__ bool
+step_scalars(const KParams & P, const DevClock * clk, int step, StepScalars<R> * sh)
+{
+  if (threadIdx.x == 0)
+  {
+    double t, dt;
+    sh->active = step_dt(P, clk, step, &t, &dt) ? 1 : 0;
+    sh->t = t;
+    sh->dt = dt;
+    sh->dtdx = (R)(dt / P.dx);
+    sh->dtdy = (R)(dt / P.dy);
+    sh->dtdz = (R)(dt / P.dz);
+  }
+  __syncthreads();
+  return sh->active != 0;
 }
 
 // bookkeeping done once per step by block 0, thread 0

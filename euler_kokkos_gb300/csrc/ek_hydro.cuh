@@ -207,27 +207,13 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
 }
 
 // per-cell CFL candidate of ComputeDtFunctor{2D,3D}
-// (HydroRunFunctors2D.h:56-84, HydroRunFunctors3D.h:49-84).  FP64: the
-// reference's expression.  Mixed: the candidate is formed in FP32 with the
-// inverse cell sizes (FP64 arithmetic costs 64 FP32 operations on GB300);
-// the max-reduction and dt = cfl / max stay FP64.
-struct InvD
-{
-  double dx, dy, dz;    // cell sizes (FP64 path)
-  float  idx, idy, idz; // 1/dx, 1/dy, 1/dz (mixed path)
-};
-__host__ __device__ inline InvD
-make_invd(double dx, double dy, double dz)
-{
-  InvD d;
-  d.dx = dx, d.dy = dy, d.dz = dz;
-  d.idx = (float)(1.0 / dx), d.idy = (float)(1.0 / dy), d.idz = (float)(1.0 / dz);
-  return d;
-}
-
+// (HydroRunFunctors2D.h:56-84, HydroRunFunctors3D.h:49-84), in the working
+// precision: FP64 keeps the reference's expression; the mixed form uses the
+// FP32 inverse cell sizes.  Threads keep a NaN-ignoring max (fmax, as the
+// reference's reduction) and convert to the FP64 key once.
 template <class R, int NV>
-__device__ __forceinline__ double
-hydro_invdt(const R (&u)[NV], const HydroConst<R> & C, const InvD & D)
+__device__ __forceinline__ R
+hydro_invdt(const R (&u)[NV], const HydroConst<R> & C, const KParams & P)
 {
   R q[NV];
   hydro_prims<R, NV>(u, q, C);
@@ -237,21 +223,21 @@ hydro_invdt(const R (&u)[NV], const HydroConst<R> & C, const InvD & D)
   if constexpr (sizeof(R) == 8)
   {
     if constexpr (NV == 4)
-      return vx / D.dx + vy / D.dy;
+      return vx / P.dx + vy / P.dy;
     else
     {
       const R vz = c + fabs(q[IW]);
-      return vx / D.dx + vy / D.dy + vz / D.dz;
+      return vx / P.dx + vy / P.dy + vz / P.dz;
     }
   }
   else
   {
     if constexpr (NV == 4)
-      return (double)(vx * D.idx + vy * D.idy);
+      return vx * P.idx + vy * P.idy;
     else
     {
       const R vz = c + fabs(q[IW]);
-      return (double)(vx * D.idx + vy * D.idy + vz * D.idz);
+      return vx * P.idx + vy * P.idy + vz * P.idz;
     }
   }
 }

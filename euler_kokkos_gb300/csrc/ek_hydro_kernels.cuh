@@ -19,11 +19,22 @@ __device__ __forceinline__ HydroConst<R>
 hydro_const(const KParams & P)
 {
   HydroConst<R> C;
-  C.gamma0 = (R)P.gamma0;
-  C.smallr = (R)P.smallr;
-  C.smallp = (R)P.smallp;
-  C.smallc = (R)P.smallc;
-  C.slope_type = (R)P.slope_type;
+  if constexpr (sizeof(R) == 8)
+  {
+    C.gamma0 = P.gamma0;
+    C.smallr = P.smallr;
+    C.smallp = P.smallp;
+    C.smallc = P.smallc;
+    C.slope_type = P.slope_type;
+  }
+  else
+  {
+    C.gamma0 = P.gamma0f;
+    C.smallr = P.smallrf;
+    C.smallp = P.smallpf;
+    C.smallc = P.smallcf;
+    C.slope_type = P.slopef;
+  }
   return C;
 }
 
@@ -92,12 +103,12 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
   R * sYm = sXp + NV * TY * FX;              // YMIN state of cells -1..TY, then y-flux
   R * sYp = sYm + NV * (TY + 2) * TX;        // YMAX state
 
-  double t, dt;
-  if (!step_dt(P, clk, step, &t, &dt))
+  __shared__ StepScalars<R> sc;
+  if (!step_scalars<R>(P, clk, step, &sc))
     return;
-  const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy);
+  const double        t = sc.t, dt = sc.dt;
+  const R             dtdx = sc.dtdx, dtdy = sc.dtdy;
   const HydroConst<R> C = hydro_const<R>(P);
-  const InvD          ID_ = make_invd(P.dx, P.dy, P.dz);
 
   const int gi0 = P.gw + bx * TX, gj0 = P.gw + by * TY;
   load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, 0, sQ);
@@ -214,7 +225,7 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
 
   // update (UpdateFunctor2D, HydroRunFunctors2D.h:809-836), in its order
   const int gi = gi0 + tx, gj = gj0 + ty;
-  unsigned long long kmax = 0ull;
+  R tmax = R(-INFINITY);
   if (gi < P.nx + P.gw && gj < P.ny + P.gw)
   {
     const long long off = (long long)gj * P.isize + gi;
@@ -235,9 +246,9 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       us[v] = (R)(S)u[v];
-    kmax = cand_key(hydro_invdt<R, NV>(us, C, ID_));
+    tmax = fmax(tmax, hydro_invdt<R, NV>(us, C, P));
   }
-  block_max_commit<NT>(kmax, &clk->key[(step + 1) % 3]);
+  block_max_commit<NT>(cand_key((double)tmax), &clk->key[(step + 1) % 3]);
   if (bx == 0 && by == 0 && threadIdx.x == 0)
     step_commit(clk, step, t, dt);
 }
@@ -328,12 +339,12 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   R * sYm = sXp + NV * TY * FX;
   R * sYp = sYm + NV * (TY + 2) * TX;
 
-  double t, dt;
-  if (!step_dt(P, clk, step, &t, &dt))
+  __shared__ StepScalars<R> sc;
+  if (!step_scalars<R>(P, clk, step, &sc))
     return;
-  const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy), dtdz = (R)(dt / P.dz);
+  const double        t = sc.t, dt = sc.dt;
+  const R             dtdx = sc.dtdx, dtdy = sc.dtdy, dtdz = sc.dtdz;
   const HydroConst<R> C = hydro_const<R>(P);
-  const InvD          ID_ = make_invd(P.dx, P.dy, P.dz);
 
   const int gw = P.gw;
   const int gi0 = gw + blockIdx.x * TX, gj0 = gw + blockIdx.y * TY;
@@ -348,9 +359,9 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 2 + gw, sQ + ((k0 + 1) % 3) * QP);
   load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 1 + gw, sQ + ((k0 + 2) % 3) * QP);
 
-  R   zmax_prev[NV]; // ZMAX face state of the cell below
-  R   acc[NV];       // partial update of the cell below, waiting for -Fz(k)
-  unsigned long long kmax = 0ull;
+  R zmax_prev[NV];        // ZMAX face state of the cell below
+  R acc[NV];              // partial update of the cell below, waiting for -Fz(k)
+  R tmax = R(-INFINITY);  // CFL candidate max of the cells this thread wrote
 
   for (int kc = k0 - 1; kc <= k1; ++kc)
   {
@@ -514,8 +525,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
         Uout[v * P.vstride + off] = (S)x;
         us[v] = (R)(S)x;
       }
-      unsigned long long kk = cand_key(hydro_invdt<R, NV>(us, C, ID_));
-      kmax = kk > kmax ? kk : kmax;
+      tmax = fmax(tmax, hydro_invdt<R, NV>(us, C, P));
     }
     if (full && own)
     {
@@ -534,7 +544,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
     }
     __syncthreads(); // ring slot and face buffers are reused next plane
   }
-  block_max_commit<NT>(kmax, &clk->key[(step + 1) % 3]);
+  block_max_commit<NT>(cand_key((double)tmax), &clk->key[(step + 1) % 3]);
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
     step_commit(clk, step, t, dt);
 }
@@ -548,9 +558,8 @@ __global__ void
 hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
 {
   const HydroConst<R> C = hydro_const<R>(P);
-  const InvD          ID_ = make_invd(P.dx, P.dy, P.dz);
   const long long     n = (long long)P.nx * P.ny * (NV == 5 ? P.nz : 1);
-  unsigned long long  kmax = 0ull;
+  R                   tmax = R(-INFINITY);
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
        c += (long long)gridDim.x * blockDim.x)
   {
@@ -564,10 +573,9 @@ hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       u[v] = (R)ldg(U + v * P.vstride + off);
-    unsigned long long kk = cand_key(hydro_invdt<R, NV>(u, C, ID_));
-    kmax = kk > kmax ? kk : kmax;
+    tmax = fmax(tmax, hydro_invdt<R, NV>(u, C, P));
   }
-  block_max_commit<256>(kmax, key);
+  block_max_commit<256>(cand_key((double)tmax), key);
 }
 
 // Fill the ghost cells of a state in memory (make_boundaries_serial result,

@@ -32,7 +32,7 @@ mhd_speed_fast(const R (&q)[8], R gamma0)
 // expression; mixed: the candidate is formed in FP32 with 1/dx (the
 // max-reduction and dt stay FP64).
 template <class R>
-__device__ __forceinline__ double
+__device__ __forceinline__ R
 mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz, float idx, float idy, float idz)
 {
   const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
@@ -48,7 +48,7 @@ mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz, float idx,
   if constexpr (sizeof(R) == 8)
     return vx / dx + vy / dy + vz / dz;
   else
-    return (double)(vx * idx + vy * idy + vz * idz);
+    return vx * idx + vy * idy + vz * idz;
 }
 
 // constoprim_mhd (MHDBaseFunctor3D.h:194-242).  u: hydro variables of the

@@ -23,11 +23,22 @@ __device__ __forceinline__ MhdConst<R>
 mhd_const(const KParams & P)
 {
   MhdConst<R> C;
-  C.gamma0 = (R)P.gamma0;
-  C.smallr = (R)P.smallr;
-  C.smallp = (R)P.smallp;
-  C.smallc = (R)P.smallc;
-  C.slope_type = (R)P.slope_type;
+  if constexpr (sizeof(R) == 8)
+  {
+    C.gamma0 = P.gamma0;
+    C.smallr = P.smallr;
+    C.smallp = P.smallp;
+    C.smallc = P.smallc;
+    C.slope_type = P.slope_type;
+  }
+  else
+  {
+    C.gamma0 = P.gamma0f;
+    C.smallr = P.smallrf;
+    C.smallp = P.smallpf;
+    C.smallc = P.smallcf;
+    C.slope_type = P.slopef;
+  }
   return C;
 }
 
@@ -120,10 +131,10 @@ mhd_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step,
     if (clk->sid[s] != step || clk->t[s] >= P.tEnd - 1e-14)
       return;
   }
-  const MhdState<S>  m = mhd_state<S>(U, P);
-  const MhdConst<R>  C = mhd_const<R>(P);
-  const long long    n = (long long)P.nx * P.ny * P.nz;
-  unsigned long long kmax = 0ull;
+  const MhdState<S> m = mhd_state<S>(U, P);
+  const MhdConst<R> C = mhd_const<R>(P);
+  const long long   n = (long long)P.nx * P.ny * P.nz;
+  R                 tmax = R(-INFINITY);
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
        c += (long long)gridDim.x * blockDim.x)
   {
@@ -133,10 +144,9 @@ mhd_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step,
     const int       k = (int)(r / P.ny) + P.gw;
     R               q[8];
     cell_prims_global<S, R>(m, P, C, i, j, k, q);
-    const unsigned long long kk = cand_key(mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz, (float)(1.0 / P.dx), (float)(1.0 / P.dy), (float)(1.0 / P.dz)));
-    kmax = kk > kmax ? kk : kmax;
+    tmax = fmax(tmax, mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz, P.idx, P.idy, P.idz));
   }
-  block_max_commit<256>(kmax, key ? key : &clk->key[step % 3]);
+  block_max_commit<256>(cand_key((double)tmax), key ? key : &clk->key[step % 3]);
 }
 
 // ---------------------------------------------------------------------------
@@ -323,12 +333,12 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
   R * sQ = sB + 4 * T::BP;                  // [3][8][QY][QX]
   R *      sE = sQ + 3 * T::QP;                                // [2][3][EY][EX]
 
-  double t, dt;
-  if (!step_dt(P, clk, step, &t, &dt))
+  __shared__ StepScalars<R> sc;
+  if (!step_scalars<R>(P, clk, step, &sc))
     return;
-  const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy), dtdz = (R)(dt / P.dz);
-  const MhdConst<R>  C = mhd_const<R>(P);
-  const MhdState<S>  m = mhd_state<S>(U, P);
+  const R           dtdx = sc.dtdx, dtdy = sc.dtdy, dtdz = sc.dtdz;
+  const MhdConst<R> C = mhd_const<R>(P);
+  const MhdState<S> m = mhd_state<S>(U, P);
   const int gw = P.gw;
   // trace cells span global [gw-1, n+gw] in each direction
   const int c0 = gw - 1 + blockIdx.x * TX, d0 = gw - 1 + blockIdx.y * TY;
@@ -462,26 +472,53 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
 // ---------------------------------------------------------------------------
 // 3. fluxes, emfs and update
 // ---------------------------------------------------------------------------
+// Output tile [i0, i0+TX) x [j0, j0+TY) marching over planes [k0, k1).  The
+// compact trace of the cells [i0-1, i0+TX] x [j0-1, j0+TY] of planes k-1 and k
+// is staged in shared memory (coalesced loads).  Per plane, every face and
+// edge quantity the tile needs forms one flat work list (x/y/z fluxes, z-, y-
+// and x-edge emfs), so no warp idles between item kinds.
+template <int TX, int TY>
+struct UpdTile
+{
+  static constexpr int XE = TX + 2, YE = TY + 2, PL = XE * YE; // trace cells per plane
+  static constexpr int FXS = (TX + 1) * TY, FYS = TX * (TY + 1), FZS = TX * TY;
+  static constexpr int EZS = (TX + 1) * (TY + 1), EYS = (TX + 1) * TY, EXS = TX * (TY + 1);
+  static constexpr int ITEMS = FXS + FYS + FZS + EZS + EYS + EXS;
+};
+
 template <class S, class R, int TX, int TY>
 __global__ void __launch_bounds__(TX * TY)
 mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
                   KParams P, DevClock * clk, int step)
 {
+  using T = UpdTile<TX, TY>;
   constexpr int NT = TX * TY;
-  constexpr int FXS = (TX + 1) * TY, FYS = TX * (TY + 1);
-  constexpr int EZS = (TX + 1) * (TY + 1), EYS = (TX + 1) * TY, EXS = TX * (TY + 1);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R * sFx = reinterpret_cast<R *>(smem_raw); // [5][TY][TX+1]
-  R * sFy = sFx + 5 * FXS;                   // [5][TY+1][TX]
-  R * sEz = sFy + 5 * FYS;                   // [2][TY+1][TX+1]
-  R * sEy = sEz + 2 * EZS;                   // [2][TY][TX+1]
-  R * sEx = sEy + 2 * EYS;                   // [2][TY+1][TX]
+  R * sT = reinterpret_cast<R *>(smem_raw); // [2][T_N][YE][XE] trace planes
+  R * sFx = sT + 2 * T_N * T::PL;           // [5][TY][TX+1]
+  R * sFy = sFx + 5 * T::FXS;               // [5][TY+1][TX]
+  R * sFz = sFy + 5 * T::FYS;               // [5][TY][TX]
+  R * sEz = sFz + 5 * T::FZS;               // [2][TY+1][TX+1]
+  R * sEy = sEz + 2 * T::EZS;               // [2][TY][TX+1]
+  R * sEx = sEy + 2 * T::EYS;               // [2][TY+1][TX]
 
-  double t, dt;
-  if (!step_dt(P, clk, step, &t, &dt))
+  __shared__ StepScalars<R> sc;
+  __shared__ double         sdd[3]; // FP64 dt/dx, dt/dy, dt/dz of the CT update
+  if (threadIdx.x == 0)
+  {
+    double t0, dt0;
+    if (step_dt(P, clk, step, &t0, &dt0))
+    {
+      sdd[0] = dt0 / P.dx;
+      sdd[1] = dt0 / P.dy;
+      sdd[2] = dt0 / P.dz;
+    }
+  }
+  if (!step_scalars<R>(P, clk, step, &sc))
     return;
-  const R dtdx = (R)(dt / P.dx), dtdy = (R)(dt / P.dy), dtdz = (R)(dt / P.dz);
-  const double ddtdx = dt / P.dx, ddtdy = dt / P.dy, ddtdz = dt / P.dz;
+  const double      t = sc.t, dt = sc.dt;
+  const R           dtdx = sc.dtdx, dtdy = sc.dtdy, dtdz = sc.dtdz;
+  const double      ddtdx = sdd[0], ddtdy = sdd[1], ddtdz = sdd[2];
   const MhdConst<R> C = mhd_const<R>(P);
   const int         gw = P.gw;
   const int         i0 = gw + blockIdx.x * TX, j0 = gw + blockIdx.y * TY;
@@ -495,45 +532,67 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
   S *               hout = (S *)Uout;
   double *          bout = sizeof(S) == 8 ? (double *)Uout + 5 * P.vstride : mixed_bfield(Uout, P);
   const R           sr = C.smallr, sp = C.smallp;
+  // the trace buffer holds cells [gw-1, n+gw] in each direction
+  const int ihi = P.nx + gw, jhi = P.ny + gw;
 
-  auto T = [&](int i, int j, int k) { return trace + (long long)k * P.plane + (long long)j * P.isize + i; };
-  auto esl = [](int k) { return (k + 4) % 2; };
+  auto load_plane = [&](int k) {
+    R * dst = sT + (k & 1) * T_N * T::PL;
+    for (int c = threadIdx.x; c < T_N * T::PL; c += NT)
+    {
+      const int f = c / T::PL, r = c - f * T::PL;
+      const int x = r % T::XE, y = r / T::XE;
+      const int i = min(i0 - 1 + x, ihi), j = min(j0 - 1 + y, jhi);
+      dst[c] = ldg(trace + f * st + (long long)k * P.plane + (long long)j * P.isize + i);
+    }
+  };
+  // trace pointer of cell (i, j) (global indices) of plane k in shared memory
+  auto TS = [&](int i, int j, int k) {
+    return sT + (k & 1) * T_N * T::PL + (j - (j0 - 1)) * T::XE + (i - (i0 - 1));
+  };
+  const long long tst = T::PL; // field stride in shared memory
 
-  R                  acc[5];
-  unsigned long long kmax = 0ull;
-  (void)kmax;
+  R acc[5];
+  load_plane(k0 - 1);
   for (int k = k0; k <= k1; ++k)
   {
-    const bool plane = k < k1; // cells of plane k are updated (partially) this iteration
-    const int  es = esl(k);
-    R *        Ez = sEz + es * EZS;
-    R *        Ey = sEy + es * EYS;
-    R *        Ex = sEx + es * EXS;
-    if (plane)
+    const bool plane = k < k1; // cells of plane k get their in-plane fluxes this iteration
+    load_plane(k);
+    __syncthreads();
+    R * Ez = sEz + (k & 1) * T::EZS;
+    R * Ey = sEy + (k & 1) * T::EYS;
+    R * Ex = sEx + (k & 1) * T::EXS;
+    for (int w = threadIdx.x; w < T::ITEMS; w += NT)
     {
-      // x-faces i in [i0, i0+TX], rows j in [j0, j0+TY): HLLD (MHDRunFunctors3D.h:1839-1846)
-      for (int f = threadIdx.x; f < FXS; f += NT)
+      int f = w;
+      if (f < T::FXS)
       {
+        // x-face i (MHDRunFunctors3D.h:1839-1846)
+        if (!plane)
+          continue;
         const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
-        if (i > P.nx + gw || j >= P.ny + gw)
-          continue; // padding of a partial tile
+        if (i > ihi || j >= jhi)
+          continue;
         R ql[8], qr[8], fl[5];
-        face_state<R, 0, true>(T(i - 1, j, k), st, ql, sr, sp);
-        face_state<R, 0, false>(T(i, j, k), st, qr, sr, sp);
+        face_state<R, 0, true>(TS(i - 1, j, k), tst, ql, sr, sp);
+        face_state<R, 0, false>(TS(i, j, k), tst, qr, sr, sp);
         mhd_hlld<R>(ql, qr, fl, C.gamma0);
 #pragma unroll
         for (int v = 0; v < 5; ++v)
-          sFx[v * FXS + f] = fl[v];
+          sFx[v * T::FXS + f] = fl[v];
+        continue;
       }
-      // y-faces, swap IU<->IV, IA<->IB (MHDRunFunctors3D.h:1848-1860)
-      for (int f = threadIdx.x; f < FYS; f += NT)
+      f -= T::FXS;
+      if (f < T::FYS)
       {
+        // y-face, swap IU<->IV and IA<->IB (MHDRunFunctors3D.h:1848-1860)
+        if (!plane)
+          continue;
         const int i = i0 + f % TX, j = j0 + f / TX;
-        if (i >= P.nx + gw || j > P.ny + gw)
+        if (i >= ihi || j > jhi)
           continue;
         R ql[8], qr[8], fl[5], x;
-        face_state<R, 1, true>(T(i, j - 1, k), st, ql, sr, sp);
-        face_state<R, 1, false>(T(i, j, k), st, qr, sr, sp);
+        face_state<R, 1, true>(TS(i, j - 1, k), tst, ql, sr, sp);
+        face_state<R, 1, false>(TS(i, j, k), tst, qr, sr, sp);
         x = ql[IU], ql[IU] = ql[IV], ql[IV] = x;
         x = ql[IA], ql[IA] = ql[IB], ql[IB] = x;
         x = qr[IU], qr[IU] = qr[IV], qr[IV] = x;
@@ -541,83 +600,97 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
         mhd_hlld<R>(ql, qr, fl, C.gamma0);
 #pragma unroll
         for (int v = 0; v < 5; ++v)
-          sFy[v * FYS + f] = fl[v];
+          sFy[v * T::FYS + f] = fl[v];
+        continue;
       }
-      // z-edge emfs of plane k: edges (i, j) i in [i0, i0+TX], j in [j0, j0+TY]
-      for (int f = threadIdx.x; f < EZS; f += NT)
+      f -= T::FYS;
+      if (f < T::FZS)
       {
+        // z-face at level k, swap IU<->IW and IA<->IC (MHDRunFunctors3D.h:1862-1874)
+        const int i = i0 + f % TX, j = j0 + f / TX;
+        if (i >= ihi || j >= jhi)
+          continue;
+        R ql[8], qr[8], fl[5], x;
+        face_state<R, 2, true>(TS(i, j, k - 1), tst, ql, sr, sp);
+        face_state<R, 2, false>(TS(i, j, k), tst, qr, sr, sp);
+        x = ql[IU], ql[IU] = ql[IW], ql[IW] = x;
+        x = ql[IA], ql[IA] = ql[IC], ql[IC] = x;
+        x = qr[IU], qr[IU] = qr[IW], qr[IW] = x;
+        x = qr[IA], qr[IA] = qr[IC], qr[IC] = x;
+        mhd_hlld<R>(ql, qr, fl, C.gamma0);
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          sFz[v * T::FZS + f] = fl[v];
+        continue;
+      }
+      f -= T::FZS;
+      if (f < T::EZS)
+      {
+        // z-edge emf of plane k, corners RT3(i-1,j-1), RB3(i-1,j), LT3(i,j-1), LB3(i,j)
+        if (!plane)
+          continue;
         const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
-        if (i > P.nx + gw || j > P.ny + gw)
+        if (i > ihi || j > jhi)
           continue;
         R a[8], b[8], c[8], d[8];
-        edge_state<R, 2, 0>(T(i - 1, j - 1, k), st, a, sr, sp);
-        edge_state<R, 2, 1>(T(i - 1, j, k), st, b, sr, sp);
-        edge_state<R, 2, 2>(T(i, j - 1, k), st, c, sr, sp);
-        edge_state<R, 2, 3>(T(i, j, k), st, d, sr, sp);
+        edge_state<R, 2, 0>(TS(i - 1, j - 1, k), tst, a, sr, sp);
+        edge_state<R, 2, 1>(TS(i - 1, j, k), tst, b, sr, sp);
+        edge_state<R, 2, 2>(TS(i, j - 1, k), tst, c, sr, sp);
+        edge_state<R, 2, 3>(TS(i, j, k), tst, d, sr, sp);
         Ez[f] = mhd_compute_emf<R, 2>(a, b, c, d, C.gamma0, C.smallc);
+        continue;
       }
-    }
-    // y-edge emfs at level k: edges (i, j) i in [i0, i0+TX], j in [j0, j0+TY)
-    // corners RT2(i-1,k-1), LT2(i,k-1), RB2(i-1,k), LB2(i,k) (MHDRunFunctors3D.h:2212-2217)
-    for (int f = threadIdx.x; f < EYS; f += NT)
-    {
-      const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
-      if (i > P.nx + gw || j >= P.ny + gw)
+      f -= T::EZS;
+      if (f < T::EYS)
+      {
+        // y-edge emf at level k: RT2(i-1,k-1), LT2(i,k-1), RB2(i-1,k), LB2(i,k)
+        // (MHDRunFunctors3D.h:2212-2217)
+        const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
+        if (i > ihi || j >= jhi)
+          continue;
+        R a[8], b[8], c[8], d[8];
+        edge_state<R, 1, 0>(TS(i - 1, j, k - 1), tst, a, sr, sp);
+        edge_state<R, 1, 2>(TS(i, j, k - 1), tst, b, sr, sp);
+        edge_state<R, 1, 1>(TS(i - 1, j, k), tst, c, sr, sp);
+        edge_state<R, 1, 3>(TS(i, j, k), tst, d, sr, sp);
+        Ey[f] = mhd_compute_emf<R, 1>(a, b, c, d, C.gamma0, C.smallc);
         continue;
-      R a[8], b[8], c[8], d[8];
-      edge_state<R, 1, 0>(T(i - 1, j, k - 1), st, a, sr, sp);
-      edge_state<R, 1, 2>(T(i, j, k - 1), st, b, sr, sp);
-      edge_state<R, 1, 1>(T(i - 1, j, k), st, c, sr, sp);
-      edge_state<R, 1, 3>(T(i, j, k), st, d, sr, sp);
-      Ey[f] = mhd_compute_emf<R, 1>(a, b, c, d, C.gamma0, C.smallc);
-    }
-    // x-edge emfs at level k: edges (i, j) i in [i0, i0+TX), j in [j0, j0+TY]
-    for (int f = threadIdx.x; f < EXS; f += NT)
-    {
-      const int i = i0 + f % TX, j = j0 + f / TX;
-      if (i >= P.nx + gw || j > P.ny + gw)
-        continue;
-      R a[8], b[8], c[8], d[8];
-      edge_state<R, 0, 0>(T(i, j - 1, k - 1), st, a, sr, sp);
-      edge_state<R, 0, 1>(T(i, j - 1, k), st, b, sr, sp);
-      edge_state<R, 0, 2>(T(i, j, k - 1), st, c, sr, sp);
-      edge_state<R, 0, 3>(T(i, j, k), st, d, sr, sp);
-      Ex[f] = mhd_compute_emf<R, 0>(a, b, c, d, C.gamma0, C.smallc);
-    }
-    // z-face flux at level k of the own column: swap IU<->IW, IA<->IC
-    R fz[5];
-    if (own)
-    {
-      R ql[8], qr[8], x;
-      face_state<R, 2, true>(T(gi, gj, k - 1), st, ql, sr, sp);
-      face_state<R, 2, false>(T(gi, gj, k), st, qr, sr, sp);
-      x = ql[IU], ql[IU] = ql[IW], ql[IW] = x;
-      x = ql[IA], ql[IA] = ql[IC], ql[IC] = x;
-      x = qr[IU], qr[IU] = qr[IW], qr[IW] = x;
-      x = qr[IA], qr[IA] = qr[IC], qr[IC] = x;
-      mhd_hlld<R>(ql, qr, fz, C.gamma0);
+      }
+      f -= T::EYS;
+      {
+        // x-edge emf at level k: RT(j-1,k-1), RB(j-1,k), LT(j,k-1), LB(j,k)
+        const int i = i0 + f % TX, j = j0 + f / TX;
+        if (i >= ihi || j > jhi)
+          continue;
+        R a[8], b[8], c[8], d[8];
+        edge_state<R, 0, 0>(TS(i, j - 1, k - 1), tst, a, sr, sp);
+        edge_state<R, 0, 1>(TS(i, j - 1, k), tst, b, sr, sp);
+        edge_state<R, 0, 2>(TS(i, j, k - 1), tst, c, sr, sp);
+        edge_state<R, 0, 3>(TS(i, j, k), tst, d, sr, sp);
+        Ex[f] = mhd_compute_emf<R, 0>(a, b, c, d, C.gamma0, C.smallc);
+      }
     }
     __syncthreads();
 
+    const int fz0 = ty * TX + tx;
     if (own && k > k0)
     {
       // finish cell k-1: hydro (UpdateFunctor3D_MHD, MHDRunFunctors3D.h:2488-2527)
       const long long off = (long long)(k - 1) * P.plane + (long long)gj * P.isize + gi;
-      acc[ID] -= fz[ID] * dtdz;
-      acc[IP] -= fz[IP] * dtdz;
-      acc[IU] -= fz[IW] * dtdz;
-      acc[IV] -= fz[IV] * dtdz;
-      acc[IW] -= fz[IU] * dtdz;
+      acc[ID] -= sFz[ID * T::FZS + fz0] * dtdz;
+      acc[IP] -= sFz[IP * T::FZS + fz0] * dtdz;
+      acc[IU] -= sFz[IW * T::FZS + fz0] * dtdz;
+      acc[IV] -= sFz[IV * T::FZS + fz0] * dtdz;
+      acc[IW] -= sFz[IU * T::FZS + fz0] * dtdz;
 #pragma unroll
       for (int v = 0; v < 5; ++v)
         hout[v * st + off] = (S)acc[v];
       // CT update of the face fields (UpdateEmfFunctor3D, MHDRunFunctors3D.h:2590-2613)
-      const int  pe = esl(k - 1);
-      const R *  Ezp = sEz + pe * EZS;
-      const R *  Eyp = sEy + pe * EYS;
-      const R *  Exp = sEx + pe * EXS;
-      const int  ezi = ty * (TX + 1) + tx, eyi = ty * (TX + 1) + tx, exi = ty * TX + tx;
-      double     bx = mi.b[0 * st + off], by = mi.b[1 * st + off], bz = mi.b[2 * st + off];
+      const R * Ezp = sEz + ((k - 1) & 1) * T::EZS;
+      const R * Eyp = sEy + ((k - 1) & 1) * T::EYS;
+      const R * Exp = sEx + ((k - 1) & 1) * T::EXS;
+      const int ezi = ty * (TX + 1) + tx, eyi = ty * (TX + 1) + tx, exi = ty * TX + tx;
+      double    bx = mi.b[0 * st + off], by = mi.b[1 * st + off], bz = mi.b[2 * st + off];
       if constexpr (sizeof(R) == 8)
       {
         bx += (Ezp[ezi + (TX + 1)] - Ezp[ezi]) * dtdy;
@@ -652,30 +725,30 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       const int fx0 = ty * (TX + 1) + tx, fy0 = ty * TX + tx;
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        u[v] += sFx[v * FXS + fx0] * dtdx;
+        u[v] += sFx[v * T::FXS + fx0] * dtdx;
 #pragma unroll
       for (int v = 0; v < 5; ++v)
-        u[v] -= sFx[v * FXS + fx0 + 1] * dtdx;
-      u[ID] += sFy[ID * FYS + fy0] * dtdy;
-      u[IP] += sFy[IP * FYS + fy0] * dtdy;
-      u[IU] += sFy[IV * FYS + fy0] * dtdy;
-      u[IV] += sFy[IU * FYS + fy0] * dtdy;
-      u[IW] += sFy[IW * FYS + fy0] * dtdy;
-      u[ID] -= sFy[ID * FYS + fy0 + TX] * dtdy;
-      u[IP] -= sFy[IP * FYS + fy0 + TX] * dtdy;
-      u[IU] -= sFy[IV * FYS + fy0 + TX] * dtdy;
-      u[IV] -= sFy[IU * FYS + fy0 + TX] * dtdy;
-      u[IW] -= sFy[IW * FYS + fy0 + TX] * dtdy;
-      u[ID] += fz[ID] * dtdz;
-      u[IP] += fz[IP] * dtdz;
-      u[IU] += fz[IW] * dtdz;
-      u[IV] += fz[IV] * dtdz;
-      u[IW] += fz[IU] * dtdz;
+        u[v] -= sFx[v * T::FXS + fx0 + 1] * dtdx;
+      u[ID] += sFy[ID * T::FYS + fy0] * dtdy;
+      u[IP] += sFy[IP * T::FYS + fy0] * dtdy;
+      u[IU] += sFy[IV * T::FYS + fy0] * dtdy;
+      u[IV] += sFy[IU * T::FYS + fy0] * dtdy;
+      u[IW] += sFy[IW * T::FYS + fy0] * dtdy;
+      u[ID] -= sFy[ID * T::FYS + fy0 + TX] * dtdy;
+      u[IP] -= sFy[IP * T::FYS + fy0 + TX] * dtdy;
+      u[IU] -= sFy[IV * T::FYS + fy0 + TX] * dtdy;
+      u[IV] -= sFy[IU * T::FYS + fy0 + TX] * dtdy;
+      u[IW] -= sFy[IW * T::FYS + fy0 + TX] * dtdy;
+      u[ID] += sFz[ID * T::FZS + fz0] * dtdz;
+      u[IP] += sFz[IP * T::FZS + fz0] * dtdz;
+      u[IU] += sFz[IW * T::FZS + fz0] * dtdz;
+      u[IV] += sFz[IV * T::FZS + fz0] * dtdz;
+      u[IW] += sFz[IU * T::FZS + fz0] * dtdz;
 #pragma unroll
       for (int v = 0; v < 5; ++v)
         acc[v] = u[v];
     }
-    __syncthreads(); // flux buffers and the older emf planes are reused
+    __syncthreads(); // trace slot, flux buffers and the older emf planes are reused
   }
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
     step_commit(clk, step, t, dt);
@@ -716,8 +789,8 @@ template <class R>
 constexpr size_t
 mhd_update_smem(int TX, int TY)
 {
-  return sizeof(R) * (5 * (TX + 1) * TY + 5 * TX * (TY + 1) + 2 * (TX + 1) * (TY + 1) + 2 * (TX + 1) * TY +
-                      2 * TX * (TY + 1));
+  return sizeof(R) * (2 * T_N * (TX + 2) * (TY + 2) + 5 * (TX + 1) * TY + 5 * TX * (TY + 1) + 5 * TX * TY +
+                      2 * (TX + 1) * (TY + 1) + 2 * (TX + 1) * TY + 2 * TX * (TY + 1));
 }
 
 constexpr int MT_TX = 32, MT_TY = 4; // trace tile

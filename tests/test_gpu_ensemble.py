@@ -71,7 +71,7 @@ def test_ensemble_instances_stop_at_their_tend():
         e.synchronize()
         ta, _, ia = e.time(0)
         tb, _, ib = e.time(1)
-        assert ia == 20 and ib < 20 and abs(tb - 0.004) < 1e-15
+        assert ia == 20 and ib < 20 and tb == float(np.float32(0.004))  # tEnd read through strtof
         o = eko.Oracle(eko.params_from_ini(ini_b), b[1])
         do = o.run(20)
         assert len(do) == ib and np.array_equal(e.dt_history(1), do)
