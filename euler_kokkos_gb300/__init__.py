@@ -63,6 +63,7 @@ class Params(ctypes.Structure):
         ("nStepmax", ctypes.c_int), ("tEnd", ctypes.c_double), ("tCurrent", ctypes.c_double),
         ("nOutput", ctypes.c_int), ("nlog", ctypes.c_int),
         ("precision", ctypes.c_int), ("exact_fp", ctypes.c_int), ("kchunk", ctypes.c_int),
+        ("mhd_stage", ctypes.c_int),
         ("solver_name_", ctypes.c_char * 32), ("problem_", ctypes.c_char * 32),
     ]
 

@@ -207,7 +207,7 @@ make_kparams(const ek_params & p)
   k.tEnd = p.tEnd;
   k.cIso = p.cIso;
   k.riemann = p.riemann;
-  k.kchunk = p.kchunk > 0 ? p.kchunk : (k.nz <= 64 ? k.nz : 64);
+  k.kchunk = p.kchunk > 0 ? p.kchunk : (k.nz <= 32 ? k.nz : 32);
   k.gamma0f = (float)p.gamma0;
   k.smallrf = (float)p.smallr;
   k.smallcf = (float)p.smallc;
@@ -216,6 +216,7 @@ make_kparams(const ek_params & p)
   k.idx = (float)(1.0 / p.dx);
   k.idy = (float)(1.0 / p.dy);
   k.idz = (float)(1.0 / (p.dim == 3 ? p.dz : 1.0));
+  k.mhd_stage = p.mhd_stage;
   return k;
 }
 

@@ -57,6 +57,7 @@ struct KParams
   // FP64 arithmetic (one FP64 instruction costs 64 FP32 ones on GB300)
   float     gamma0f, smallrf, smallcf, smallpf, slopef;
   float     idx, idy, idz; // 1/dx, 1/dy, 1/dz
+  int       mhd_stage;     // MHD update: stage the trace planes in shared memory
 };
 
 // Per-step scalars kept on the device so that consecutive steps need no host

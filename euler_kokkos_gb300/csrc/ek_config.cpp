@@ -213,6 +213,7 @@ ek_params_from_ini(const char * text, size_t len, ek_params * out)
   p.precision = (prec == "mixed" || prec == "fp32") ? EK_PREC_MIXED : EK_PREC_FP64;
   p.exact_fp = (int)get_integer(ini, "gb300", "exact", 0);
   p.kchunk = (int)get_integer(ini, "gb300", "kchunk", 0);
+  p.mhd_stage = (int)get_integer(ini, "gb300", "mhd_stage", 0);
   *out = p;
   return EK_OK;
 }

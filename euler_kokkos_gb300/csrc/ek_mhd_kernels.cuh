@@ -486,7 +486,7 @@ struct UpdTile
   static constexpr int ITEMS = FXS + FYS + FZS + EZS + EYS + EXS;
 };
 
-template <class S, class R, int TX, int TY>
+template <class S, class R, int TX, int TY, bool STAGE>
 __global__ void __launch_bounds__(TX * TY)
 mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
                   KParams P, DevClock * clk, int step)
@@ -494,8 +494,8 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
   using T = UpdTile<TX, TY>;
   constexpr int NT = TX * TY;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R * sT = reinterpret_cast<R *>(smem_raw); // [2][T_N][YE][XE] trace planes
-  R * sFx = sT + 2 * T_N * T::PL;           // [5][TY][TX+1]
+  R * sT = reinterpret_cast<R *>(smem_raw); // [2][T_N][YE][XE] trace planes (STAGE)
+  R * sFx = sT + (STAGE ? 2 * T_N * T::PL : 0); // [5][TY][TX+1]
   R * sFy = sFx + 5 * T::FXS;               // [5][TY+1][TX]
   R * sFz = sFy + 5 * T::FYS;               // [5][TY][TX]
   R * sEz = sFz + 5 * T::FZS;               // [2][TY+1][TX+1]
@@ -536,6 +536,8 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
   const int ihi = P.nx + gw, jhi = P.ny + gw;
 
   auto load_plane = [&](int k) {
+    if (!STAGE)
+      return;
     R * dst = sT + (k & 1) * T_N * T::PL;
     for (int c = threadIdx.x; c < T_N * T::PL; c += NT)
     {
@@ -545,11 +547,14 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       dst[c] = ldg(trace + f * st + (long long)k * P.plane + (long long)j * P.isize + i);
     }
   };
-  // trace pointer of cell (i, j) (global indices) of plane k in shared memory
-  auto TS = [&](int i, int j, int k) {
-    return sT + (k & 1) * T_N * T::PL + (j - (j0 - 1)) * T::XE + (i - (i0 - 1));
+  // trace pointer of cell (i, j) (global indices) of plane k: shared memory
+  // (STAGE) or the trace buffer itself (read through L1)
+  auto TS = [&](int i, int j, int k) -> const R * {
+    if (STAGE)
+      return sT + (k & 1) * T_N * T::PL + (j - (j0 - 1)) * T::XE + (i - (i0 - 1));
+    return trace + (long long)k * P.plane + (long long)j * P.isize + i;
   };
-  const long long tst = T::PL; // field stride in shared memory
+  const long long tst = STAGE ? (long long)T::PL : st; // field stride
 
   R acc[5];
   load_plane(k0 - 1);
@@ -787,9 +792,9 @@ mhd_trace_smem(int TX, int TY)
 }
 template <class R>
 constexpr size_t
-mhd_update_smem(int TX, int TY)
+mhd_update_smem(int TX, int TY, bool stage)
 {
-  return sizeof(R) * (2 * T_N * (TX + 2) * (TY + 2) + 5 * (TX + 1) * TY + 5 * TX * (TY + 1) + 5 * TX * TY +
+  return sizeof(R) * ((stage ? 2 * T_N * (TX + 2) * (TY + 2) : 0) + 5 * (TX + 1) * TY + 5 * TX * (TY + 1) + 5 * TX * TY +
                       2 * (TX + 1) * (TY + 1) + 2 * (TX + 1) * TY + 2 * TX * (TY + 1));
 }
 
@@ -822,10 +827,11 @@ mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams 
     k<<<grid, MT_TX * MT_TY, sm, st>>>(Uin, (R *)work, P, clk, step);
     return cudaGetLastError();
   }
-  // 3. fluxes, emfs, update
+  // 3. fluxes, emfs, update (trace read through L1, or staged in shared memory)
   {
-    auto       k = mhd_update_kernel<S, R, MU_TX, MU_TY>;
-    const int  sm = (int)mhd_update_smem<R>(MU_TX, MU_TY);
+    auto       k = P.mhd_stage ? mhd_update_kernel<S, R, MU_TX, MU_TY, true>
+                               : mhd_update_kernel<S, R, MU_TX, MU_TY, false>;
+    const int  sm = (int)mhd_update_smem<R>(MU_TX, MU_TY, P.mhd_stage != 0);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e != cudaSuccess)
       return e;

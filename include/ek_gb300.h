@@ -78,6 +78,7 @@ typedef struct ek_params
   int    precision; /* ek_precision; [gb300] precision = fp64 | mixed */
   int    exact_fp;  /* 1: FP64 kernels built without FMA contraction ([gb300] exact = 1) */
   int    kchunk;    /* 3D planes per CTA column (0: automatic; [gb300] kchunk) */
+  int    mhd_stage; /* MHD update kernel stages the trace planes in shared memory ([gb300] mhd_stage) */
   char   solver_name[32];
   char   problem[32];
 } ek_params;
