@@ -5,6 +5,7 @@ Translation units (compiled in parallel, one -gencode):
                         namespace ek_fast  (FP64 with FMA contraction + mixed FP32)
   ek_capi.cu         -- C ABI host implementation
   ek_config.cpp      -- .ini front end
+  ek_noalloc.cu      -- the MHD 3D step on a static device scratch (no allocation)
 Usage: python -m euler_kokkos_gb300.build   (or build() from Python)
 """
 
@@ -45,6 +46,7 @@ def _units():
                                   "--prec-div=false", "--prec-sqrt=false"]),
         ("ek_capi.o", os.path.join(CSRC, "ek_capi.cu"), []),
         ("ek_config.o", os.path.join(CSRC, "ek_config.cpp"), ["-x", "cu"]),
+        ("ek_noalloc.o", os.path.join(CSRC, "ek_noalloc.cu"), []),
     ]
 
 

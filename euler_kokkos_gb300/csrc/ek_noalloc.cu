@@ -1,0 +1,172 @@
+// ek_mhd3d_step_noalloc: one MHD_Muscl_3D time step that allocates no device
+// memory.
+//
+// It is the GPU form of SolverMHDMuscl<3>::godunov_unsplit_impl(data_in,
+// data_out) (SolverMHDMuscl.cpp:463-568): boundaries of data_in, dt of the
+// state (compute_dt), trace, fluxes, emfs and update into data_out.
+//
+// Which callers cannot allocate, and why: a host code that hands the library
+// only the two state arrays of the step -- as that function receives only its
+// two DataArrays -- and keeps every other byte of device memory in its own
+// pool (Kokkos memory space, an embedding code that budgets the whole HBM).
+// Such a caller cannot give the library a trace buffer, and a cudaMalloc /
+// cudaFree pair per step would synchronise the device twice per step.  The
+// step's only temporary, the 47-value compact trace of the z-marching trace
+// kernel, therefore lives in a fixed file-scope device array.
+//
+// Limits and rules:
+//   * the array is EK_NOALLOC_SCRATCH_BYTES (64 MiB); every GPU context that
+//     loads this library holds it until the process exits;
+//   * FP64 trace = 47 * 8 bytes per cell of the ghosted grid, so grids with
+//     (nx+6)(ny+6)(nz+6) above (64 MiB - 512) / 376 = 178,479 cells (a 50^3
+//     interior is the largest cube) are rejected with EK_ERR_INVALID;
+//   * the first call on each device resolves the array's address with
+//     cudaGetSymbolAddress (that device current); make that first call before
+//     any stream capture;
+//   * calls on one device share the array: two calls in flight at once
+//     (different streams or host threads) race on it and must be serialised
+//     by the caller, e.g. by issuing them on one stream;
+//   * nothing in the array has to start at zero: each call writes the clock
+//     slots itself (a one-thread kernel, before the step's kernels) and the
+//     trace kernel writes every trace value the update kernel reads.
+#include <cmath>
+#include <mutex>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ek_gb300.h"
+#include "ek_internal.h"
+#include "ek_launch.h"
+
+// the scratch: file scope, fixed size, one copy per device context
+static __device__ __align__(256) unsigned char g_noalloc_scratch[EK_NOALLOC_SCRATCH_BYTES];
+
+namespace
+{
+
+// [0, 256): the step's device clock; [256, 512): the dt of the step;
+// [512, EK_NOALLOC_SCRATCH_BYTES): the compact trace
+constexpr size_t kClockOffset = 0;
+constexpr size_t kDtOffset = 256;
+constexpr size_t kTraceOffset = 512;
+static_assert(sizeof(ekc::DevClock) <= kDtOffset - kClockOffset, "clock region too small");
+
+constexpr int kMaxDevices = 64;
+std::mutex    g_setup_mutex;
+void *        g_scratch_addr[kMaxDevices] = {};
+
+// once per device, with that device current
+ek_status
+scratch_address(int dev, unsigned char ** out)
+{
+  if (dev < 0 || dev >= kMaxDevices)
+    return ek_internal::fail(EK_ERR_UNSUPPORTED, "ek_mhd3d_step_noalloc: device ordinal " + std::to_string(dev) +
+                                                     " beyond the " + std::to_string(kMaxDevices) + " supported");
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (!g_scratch_addr[dev])
+  {
+    void *      ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess)
+      return ek_internal::fail(EK_ERR_CUDA, std::string("ek_mhd3d_step_noalloc: cudaGetSymbolAddress: ") +
+                                                cudaGetErrorString(e));
+    g_scratch_addr[dev] = ptr;
+  }
+  *out = static_cast<unsigned char *>(g_scratch_addr[dev]);
+  return EK_OK;
+}
+
+// the clock of a single step starting at t0 (slot 0 committed, CFL slot at
+// the lowest key, dt slot NaN until the update kernel writes it)
+__global__ void
+noalloc_clock_init(ekc::DevClock * clk, double t0, double * dt_slot)
+{
+  for (int s = 0; s < 3; ++s)
+  {
+    clk->key[s] = EK_KEY_LOWEST;
+    clk->t[s] = 0.0;
+    clk->sid[s] = -1;
+  }
+  clk->sid[0] = 0;
+  clk->t[0] = t0;
+  clk->iteration = 0;
+  clk->error = 0;
+  clk->dtlog = dt_slot;
+  clk->dtcap = 1;
+  *dt_slot = __longlong_as_double(0x7ff8000000000000ll);
+}
+
+} // namespace
+
+extern "C" ek_status
+ek_mhd3d_step_noalloc(const ek_params * params, const double * U_in, double * U_out, double t,
+                      double * dt_out, void * stream)
+{
+  using ek_internal::fail;
+  if (!params || !U_in || !U_out)
+    return fail(EK_ERR_INVALID, "ek_mhd3d_step_noalloc: null argument");
+  const ek_params & p = *params;
+  {
+    ek_status v = ek_internal::validate(p);
+    if (v != EK_OK)
+      return v;
+  }
+  if (!p.mhd || p.dim != 3)
+    return fail(EK_ERR_UNSUPPORTED, "ek_mhd3d_step_noalloc: MHD_Muscl_3D only");
+  if (p.precision != EK_PREC_FP64)
+    return fail(EK_ERR_UNSUPPORTED, "ek_mhd3d_step_noalloc: the state arrays are FP64 (precision must be fp64)");
+  const ekc::KParams kp = ek_internal::make_kparams(p);
+  const size_t       trace_bytes = ek_exact::mhd_work_bytes(0, kp);
+  const size_t       cell_bytes = trace_bytes / (size_t)kp.vstride;
+  if (trace_bytes > EK_NOALLOC_SCRATCH_BYTES - kTraceOffset)
+    return fail(EK_ERR_INVALID,
+                "ek_mhd3d_step_noalloc: grid too large for the static scratch: the trace needs " +
+                    std::to_string(trace_bytes) + " bytes, the scratch holds " +
+                    std::to_string(EK_NOALLOC_SCRATCH_BYTES - kTraceOffset) + " (at most " +
+                    std::to_string((EK_NOALLOC_SCRATCH_BYTES - kTraceOffset) / cell_bytes) +
+                    " cells including ghosts)");
+  const size_t state = ek_internal::state_bytes(p, kp);
+  const char * a = reinterpret_cast<const char *>(U_in);
+  const char * b = reinterpret_cast<const char *>(U_out);
+  if (a < b + state && b < a + state)
+    return fail(EK_ERR_INVALID, "ek_mhd3d_step_noalloc: U_in and U_out overlap");
+  if (!(t < p.tEnd - 1e-14))
+    return fail(EK_ERR_INVALID, "ek_mhd3d_step_noalloc: t >= tEnd, the run is finished");
+
+  int dev = 0;
+  {
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+      return fail(EK_ERR_NO_DEVICE, std::string("ek_mhd3d_step_noalloc: ") + cudaGetErrorString(e));
+  }
+  unsigned char * scratch = nullptr;
+  {
+    ek_status s = scratch_address(dev, &scratch);
+    if (s != EK_OK)
+      return s;
+  }
+  ekc::DevClock * clk = reinterpret_cast<ekc::DevClock *>(scratch + kClockOffset);
+  double *        dt_slot = reinterpret_cast<double *>(scratch + kDtOffset);
+  void *          trace = scratch + kTraceOffset;
+  cudaStream_t    st = static_cast<cudaStream_t>(stream);
+
+  noalloc_clock_init<<<1, 1, 0, st>>>(clk, t, dt_slot);
+  cudaError_t e = cudaGetLastError();
+  for (int phase = 0; phase < 3 && e == cudaSuccess; ++phase)
+    e = p.exact_fp ? ek_exact::mhd_step(0, phase, U_in, U_out, trace, kp, clk, 0, st)
+                   : ek_fast::mhd_step(0, phase, U_in, U_out, trace, kp, clk, 0, st);
+  if (e != cudaSuccess)
+    return fail(EK_ERR_CUDA, std::string("ek_mhd3d_step_noalloc: launch: ") + cudaGetErrorString(e));
+  if (!dt_out)
+    return EK_OK;
+  e = cudaMemcpyAsync(dt_out, dt_slot, sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess)
+    return fail(EK_ERR_CUDA, std::string("ek_mhd3d_step_noalloc: dt read: ") + cudaGetErrorString(e));
+  if (!(*dt_out > 0.0) || !std::isfinite(*dt_out))
+    return fail(EK_ERR_NONFINITE, "ek_mhd3d_step_noalloc: time step is not finite and positive (dt = " +
+                                      std::to_string(*dt_out) + ")");
+  return EK_OK;
+}

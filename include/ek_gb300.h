@@ -183,6 +183,41 @@ ek_status ek_ensemble_info(ek_ensemble * e, long long * interior_cells, int * ti
                            long long * launches);
 ek_status ek_ensemble_stream(ek_ensemble * e, void ** stream);
 
+/* ---------------------------------------------------------------------------
+ * One MHD_Muscl_3D step that allocates no device memory (no counterpart in
+ * the reference).  For callers that own every byte of device memory in their
+ * own pool and hand the step only its two state arrays -- as the reference's
+ * SolverMHDMuscl<3>::godunov_unsplit_impl(data_in, data_out)
+ * (SolverMHDMuscl.cpp:463-568), which this call computes, receives only two
+ * DataArrays -- and for which a cudaMalloc / cudaFree pair per step (each
+ * synchronising the device) is not acceptable.
+ *
+ * The step's temporary (the 47 x FP64 per-cell compact trace) lives in one
+ * static device array of EK_NOALLOC_SCRATCH_BYTES, held by every GPU context
+ * that loads this library until the process exits.  Grids whose ghosted cell
+ * count (nx+6)(ny+6)(nz+6) exceeds (EK_NOALLOC_SCRATCH_BYTES - 512) / 376 =
+ * 178,479 (a 50^3 interior is the largest cube) are rejected: EK_ERR_INVALID.
+ *
+ * U_in, U_out: device pointers, FP64 EK_LAYOUT_LEFT, ghost-inclusive, not
+ * overlapping.  The step reads U_in's interior (ghost values follow the
+ * boundary conditions by index mapping, so U_in's ghost cells are not read)
+ * and writes U_out's interior cells only.  t: time at the start of the step.
+ * dt is computed on the device from U_in as the solver's step does (CFL of the
+ * state, clamped at tEnd); params->precision must be EK_PREC_FP64,
+ * params->exact_fp selects the bitwise-parity build.
+ * dt_out: NULL (the call is asynchronous on `stream`) or a host pointer that
+ * receives the step's dt (the call then synchronises `stream`;
+ * EK_ERR_NONFINITE if dt is not finite and positive).
+ * stream: a cudaStream_t, NULL for the default stream.
+ *
+ * The first call on each device (that device current) resolves the array's
+ * address with cudaGetSymbolAddress: make it before any stream capture.
+ * Calls on one device share the array, so calls in flight at the same time
+ * (other streams, other host threads) race: serialise them (one stream). */
+#define EK_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+ek_status ek_mhd3d_step_noalloc(const ek_params * params, const double * U_in, double * U_out, double t,
+                                double * dt_out, void * stream);
+
 #ifdef __cplusplus
 }
 #endif
