@@ -142,6 +142,53 @@ namespace EK_NS
 {
 using namespace ekc;
 
+// FP64 <-> FP32 conversions on the integer pipes.  The hardware conversion
+// instructions run on the FP64 unit, which issues at 1/64 of the FP32 rate on
+// this GPU, so the mixed kernels convert the FP64 face fields this way.
+// Normal results and zeros take the integer path and equal the hardware
+// round-to-nearest-even conversion bit for bit; subnormal, overflowing,
+// infinite and NaN values fall back to the hardware instruction.
+__device__ __forceinline__ float
+d2f_rn(double x)
+{
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned           hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned           e = (hi >> 20) & 0x7ffu;
+  if (e - 897u <= 253u)
+  {
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    unsigned       f = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
+    f += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float(f);
+  }
+  if ((b << 1) == 0ull)
+    return __uint_as_float(hi & 0x80000000u);
+  return __double2float_rn(x);
+}
+__device__ __forceinline__ double
+f2d(float x)
+{
+  const unsigned b = __float_as_uint(x);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e - 1u < 254u)
+    return __hiloint2double((int)((b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3)),
+                            (int)(b << 29));
+  if ((b << 1) == 0u)
+    return __hiloint2double((int)(b & 0x80000000u), 0);
+  return (double)x;
+}
+// FP64 value in the working precision R
+template <class R>
+__device__ __forceinline__ R
+to_r(double x)
+{
+  if constexpr (sizeof(R) == 4)
+    return d2f_rn(x);
+  else
+    return x;
+}
+
 // Map a (possibly ghost) coordinate g in [0, n+2gw) of one dimension to the
 // interior coordinate the boundary fill copies from; *flip is set when the
 // reflecting wall flips the sign of the normal components.

@@ -401,32 +401,35 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
 }
 
 // compute_emf<emfDir> (RiemannSolvers_MHD.h:648-871) on the four corner
-// states (qRT, qRB, qLT, qLB) of an edge.  iu/iv: parallel velocities,
-// ia/ib: parallel fields, ic: orthogonal field, per emfDir.
-template <class R, int EMF>
-__device__ __forceinline__ R
-mhd_compute_emf(const R (&qRT)[8], const R (&qRB)[8], const R (&qLT)[8], const R (&qLB)[8], R gamma0,
-                R smallc)
+// states of an edge.  Each corner carries the components compute_emf reads
+// for the edge direction: the velocities and face fields along the two
+// transverse directions (u, a along the first, v, b along the second) and the
+// field along the edge (c).
+template <class R>
+struct EdgeCorner
 {
-  constexpr int iu = EMF == 2 ? IU : (EMF == 1 ? IW : IV);
-  constexpr int iv = EMF == 2 ? IV : (EMF == 1 ? IU : IW);
-  constexpr int ia = EMF == 2 ? IA : (EMF == 1 ? IC : IB);
-  constexpr int ib = EMF == 2 ? IB : (EMF == 1 ? IA : IC);
-  constexpr int ic = EMF == 2 ? IC : (EMF == 1 ? IB : IA);
+  R r, p, u, v, a, b, c;
+};
+
+template <class R>
+__device__ __forceinline__ R
+mhd_emf_corners(const EdgeCorner<R> & RT, const EdgeCorner<R> & RB, const EdgeCorner<R> & LT,
+                const EdgeCorner<R> & LB, R gamma0, R smallc)
+{
   EdgeQ<R> LL, RL, LR, RR;
-  LL.r = qRT[ID], RL.r = qLT[ID], LR.r = qRB[ID], RR.r = qLB[ID];
-  LL.p = qRT[IP], RL.p = qLT[IP], LR.p = qRB[IP], RR.p = qLB[IP];
-  LL.u = qRT[iu], RL.u = qLT[iu], LR.u = qRB[iu], RR.u = qLB[iu];
-  LL.v = qRT[iv], RL.v = qLT[iv], LR.v = qRB[iv], RR.v = qLB[iv];
-  LL.a = R(0.5) * (qRT[ia] + qLT[ia]);
-  RL.a = R(0.5) * (qRT[ia] + qLT[ia]);
-  LR.a = R(0.5) * (qRB[ia] + qLB[ia]);
-  RR.a = R(0.5) * (qRB[ia] + qLB[ia]);
-  LL.b = R(0.5) * (qRT[ib] + qRB[ib]);
-  RL.b = R(0.5) * (qLT[ib] + qLB[ib]);
-  LR.b = R(0.5) * (qRT[ib] + qRB[ib]);
-  RR.b = R(0.5) * (qLT[ib] + qLB[ib]);
-  LL.c = qRT[ic], RL.c = qLT[ic], LR.c = qRB[ic], RR.c = qLB[ic];
+  LL.r = RT.r, RL.r = LT.r, LR.r = RB.r, RR.r = LB.r;
+  LL.p = RT.p, RL.p = LT.p, LR.p = RB.p, RR.p = LB.p;
+  LL.u = RT.u, RL.u = LT.u, LR.u = RB.u, RR.u = LB.u;
+  LL.v = RT.v, RL.v = LT.v, LR.v = RB.v, RR.v = LB.v;
+  LL.a = R(0.5) * (RT.a + LT.a);
+  RL.a = R(0.5) * (RT.a + LT.a);
+  LR.a = R(0.5) * (RB.a + LB.a);
+  RR.a = R(0.5) * (RB.a + LB.a);
+  LL.b = R(0.5) * (RT.b + RB.b);
+  RL.b = R(0.5) * (LT.b + LB.b);
+  LR.b = R(0.5) * (RT.b + RB.b);
+  RR.b = R(0.5) * (LT.b + LB.b);
+  LL.c = RT.c, RL.c = LT.c, LR.c = RB.c, RR.c = LB.c;
   const R ELL = LL.u * LL.b - LL.v * LL.a;
   const R ERL = RL.u * RL.b - RL.v * RL.a;
   const R ELR = LR.u * LR.b - LR.v * LR.a;
@@ -462,103 +465,85 @@ floor_state(R (&q)[8], R smallr, R smallp)
   q[IP] = fmax(smallp, q[IP]);
 }
 
-// face states (qm: left state at the right face, qp: right state at the left face)
-template <class R, int DIR, bool PLUS>
-__device__ __forceinline__ void
-face_state(const R * t, long long st, R (&q)[8], R smallr, R smallp)
+// Trace field indices as functions of a direction (0 x, 1 y, 2 z), so one
+// code path serves the faces and edges of every direction:
+//   hydro half slope of variable f (T_R..T_W) along e
+//   half slope of the cell-centred field f along e (f != e)
+//   face value of field f on the left (0) / right (1) face
+//   half slope of that face value along e (e != f)
+__device__ __forceinline__ int
+t_hslope(int e, int f)
 {
-  constexpr int dr = DIR == 0 ? T_DRX : (DIR == 1 ? T_DRY : T_DRZ);
-  const R r = t[T_R * st], p = t[T_P * st], u = t[T_U * st], v = t[T_V * st], w = t[T_W * st];
-  const R d_r = t[dr * st], d_p = t[(dr + 1) * st], d_u = t[(dr + 2) * st], d_v = t[(dr + 3) * st],
-          d_w = t[(dr + 4) * st];
-  if (PLUS)
-  {
-    q[ID] = r + d_r, q[IU] = u + d_u, q[IV] = v + d_v, q[IW] = w + d_w, q[IP] = p + d_p;
-  }
-  else
-  {
-    q[ID] = r - d_r, q[IU] = u - d_u, q[IV] = v - d_v, q[IW] = w - d_w, q[IP] = p - d_p;
-  }
-  if constexpr (DIR == 0)
-  {
-    q[IA] = PLUS ? t[T_AR * st] : t[T_AL * st];
-    q[IB] = PLUS ? t[T_B * st] + t[T_DBX * st] : t[T_B * st] - t[T_DBX * st];
-    q[IC] = PLUS ? t[T_C * st] + t[T_DCX * st] : t[T_C * st] - t[T_DCX * st];
-  }
-  else if constexpr (DIR == 1)
-  {
-    q[IA] = PLUS ? t[T_A * st] + t[T_DAY * st] : t[T_A * st] - t[T_DAY * st];
-    q[IB] = PLUS ? t[T_BR * st] : t[T_BL * st];
-    q[IC] = PLUS ? t[T_C * st] + t[T_DCY * st] : t[T_C * st] - t[T_DCY * st];
-  }
-  else
-  {
-    q[IA] = PLUS ? t[T_A * st] + t[T_DAZ * st] : t[T_A * st] - t[T_DAZ * st];
-    q[IB] = PLUS ? t[T_B * st] + t[T_DBZ * st] : t[T_B * st] - t[T_DBZ * st];
-    q[IC] = PLUS ? t[T_CR * st] : t[T_CL * st];
-  }
+  return T_DRX + 7 * e + f;
+}
+__device__ __forceinline__ int
+t_bslope(int e, int f)
+{
+  return T_DRX + 7 * e + 5 + (f < e ? f : f - 1);
+}
+__device__ __forceinline__ int
+t_bface(int f, int right)
+{
+  return T_AL + 2 * f + right;
+}
+__device__ __forceinline__ int
+t_bfslope(int f, int right, int e)
+{
+  return T_DALY + 6 * right + 2 * f + (e < f ? e : e - 1);
+}
+
+// Face state of a cell on its face normal to d (PLUS: the right face, the
+// left state of that face; otherwise the left face), in the face frame the
+// flux functor hands to the Riemann solver: normal velocity in IU and normal
+// field in IA, with the reference's component swaps for y (IU<->IV, IA<->IB)
+// and z (IU<->IW, IA<->IC) faces (trace_unsplit_mhd_3d_simpler,
+// MHDBaseFunctor3D.h:905-955; MHDRunFunctors3D.h:1839-1874).
+template <class R, bool PLUS>
+__device__ __forceinline__ void
+face_state_dir(const R * t, long long st, int d, R (&q)[8], R smallr, R smallp)
+{
+  auto h = [&](int f) {
+    const R c = t[f * st], s = t[t_hslope(d, f) * st];
+    return PLUS ? c + s : c - s;
+  };
+  auto tb = [&](int f) {
+    const R c = t[(T_A + f) * st], s = t[t_bslope(d, f) * st];
+    return PLUS ? c + s : c - s;
+  };
+  q[ID] = h(T_R);
+  q[IP] = h(T_P);
+  q[IU] = h(T_U + d);
+  q[IV] = h(d == 1 ? T_U : T_V);
+  q[IW] = h(d == 2 ? T_U : T_W);
+  q[IA] = t[t_bface(d, PLUS ? 1 : 0) * st];
+  q[IB] = tb(d == 1 ? 0 : 1);
+  q[IC] = tb(d == 2 ? 0 : 2);
   floor_state(q, smallr, smallp);
 }
 
-// edge states: E = 0 RT, 1 RB, 2 LT, 3 LB; DIR = edge direction
-template <class R, int DIR, int E>
-__device__ __forceinline__ void
-edge_state(const R * t, long long st, R (&q)[8], R smallr, R smallp)
+// One corner of an edge along d (MHDBaseFunctor3D.h:957-1113).  The
+// transverse directions are p1 = (d+1)%3 and p2 = (d+2)%3, the order in which
+// compute_emf<emfDir> reads them; S1/S2 are the sides (+1 right, -1 left) of
+// the corner along p1/p2.  Each sum keeps the reference's operands, so the
+// result is bit-identical to the per-direction expressions.
+template <class R, int S1, int S2>
+__device__ __forceinline__ EdgeCorner<R>
+edge_corner(const R * t, long long st, int d, int p1, int p2, R smallr, R smallp)
 {
-  // the two transverse directions (a, b) of the edge and the signs of their
-  // slopes: RT (+,+), RB (+,-), LT (-,+), LB (-,-)
-  constexpr int da = DIR == 0 ? T_DRY : T_DRX;
-  constexpr int db = DIR == 2 ? T_DRY : T_DRZ;
-  constexpr bool pa = (E == 0 || E == 1), pb = (E == 0 || E == 2);
-  const R r = t[T_R * st], p = t[T_P * st], u = t[T_U * st], v = t[T_V * st], w = t[T_W * st];
-  auto comb = [&](R c0, int off) {
-    const R x = t[(da + off) * st], y = t[(db + off) * st];
-    R       s;
-    if (pa && pb)
-      s = (+x + y);
-    else if (pa)
-      s = (+x - y);
-    else if (pb)
-      s = (-x + y);
-    else
-      s = (-x - y);
-    return c0 + s;
+  auto sg1 = [](R x) { return S1 > 0 ? x : -x; };
+  auto sg2 = [](R x) { return S2 > 0 ? x : -x; };
+  auto hyd = [&](int f) {
+    return t[f * st] + (sg1(t[t_hslope(p1, f) * st]) + sg2(t[t_hslope(p2, f) * st]));
   };
-  q[ID] = comb(r, 0);
-  q[IP] = comb(p, 1);
-  q[IU] = comb(u, 2);
-  q[IV] = comb(v, 3);
-  q[IW] = comb(w, 4);
-  // face-field components (MHDBaseFunctor3D.h:957-1113)
-  if constexpr (DIR == 0)
-  {
-    // IA = A + (+-dAy +- dAz); IB from BR/BL with dBRz/dBLz; IC from CR/CL with dCRy/dCLy
-    const R A = t[T_A * st], dAy = t[T_DAY * st], dAz = t[T_DAZ * st];
-    q[IA] = A + (pa && pb ? (+dAy + dAz) : pa ? (+dAy - dAz) : pb ? (-dAy + dAz) : (-dAy - dAz));
-    q[IB] = pa ? t[T_BR * st] + (pb ? +t[T_DBRZ * st] : -t[T_DBRZ * st])
-               : t[T_BL * st] + (pb ? +t[T_DBLZ * st] : -t[T_DBLZ * st]);
-    q[IC] = pb ? t[T_CR * st] + (pa ? +t[T_DCRY * st] : -t[T_DCRY * st])
-               : t[T_CL * st] + (pa ? +t[T_DCLY * st] : -t[T_DCLY * st]);
-  }
-  else if constexpr (DIR == 1)
-  {
-    q[IA] = pa ? t[T_AR * st] + (pb ? +t[T_DARZ * st] : -t[T_DARZ * st])
-               : t[T_AL * st] + (pb ? +t[T_DALZ * st] : -t[T_DALZ * st]);
-    const R B = t[T_B * st], dBx = t[T_DBX * st], dBz = t[T_DBZ * st];
-    q[IB] = B + (pa && pb ? (+dBx + dBz) : pa ? (+dBx - dBz) : pb ? (-dBx + dBz) : (-dBx - dBz));
-    q[IC] = pb ? t[T_CR * st] + (pa ? +t[T_DCRX * st] : -t[T_DCRX * st])
-               : t[T_CL * st] + (pa ? +t[T_DCLX * st] : -t[T_DCLX * st]);
-  }
-  else
-  {
-    q[IA] = pa ? t[T_AR * st] + (pb ? +t[T_DARY * st] : -t[T_DARY * st])
-               : t[T_AL * st] + (pb ? +t[T_DALY * st] : -t[T_DALY * st]);
-    q[IB] = pb ? t[T_BR * st] + (pa ? +t[T_DBRX * st] : -t[T_DBRX * st])
-               : t[T_BL * st] + (pa ? +t[T_DBLX * st] : -t[T_DBLX * st]);
-    const R C = t[T_C * st], dCx = t[T_DCX * st], dCy = t[T_DCY * st];
-    q[IC] = C + (pa && pb ? (+dCx + dCy) : pa ? (+dCx - dCy) : pb ? (-dCx + dCy) : (-dCx - dCy));
-  }
-  floor_state(q, smallr, smallp);
+  EdgeCorner<R> e;
+  e.r = fmax(smallr, hyd(T_R));
+  e.p = fmax(smallp, hyd(T_P));
+  e.u = hyd(T_U + p1);
+  e.v = hyd(T_U + p2);
+  e.a = t[t_bface(p1, S1 > 0) * st] + sg2(t[t_bfslope(p1, S1 > 0, p2) * st]);
+  e.b = t[t_bface(p2, S2 > 0) * st] + sg1(t[t_bfslope(p2, S2 > 0, p1) * st]);
+  e.c = t[(T_A + d) * st] + (sg1(t[t_bslope(p1, d) * st]) + sg2(t[t_bslope(p2, d) * st]));
+  return e;
 }
 
 } // namespace EK_NS

@@ -103,8 +103,8 @@ cell_prims_global(const MhdState<S> & m, const KParams & P, const MhdConst<R> & 
 #pragma unroll
   for (int c = 0; c < 3; ++c)
   {
-    blr[c] = (R)bl[c];
-    brr[c] = (R)br[c];
+    blr[c] = to_r<R>(bl[c]);
+    brr[c] = to_r<R>(br[c]);
   }
   mhd_constoprim<R>(u, blr, brr, q, C, [&](double (&a)[3], double (&b)[3]) {
 #pragma unroll
@@ -354,7 +354,7 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
       const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
 #pragma unroll
       for (int comp = 0; comp < 3; ++comp)
-        dst[(comp * T::BY + y) * T::BX + x] = (R)load_face<S>(m, P, s, comp);
+        dst[(comp * T::BY + y) * T::BX + x] = to_r<R>(load_face<S>(m, P, s, comp));
     }
   };
   // primitives of plane gk from the hydro variables and the face planes
@@ -474,16 +474,17 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
 // ---------------------------------------------------------------------------
 // Output tile [i0, i0+TX) x [j0, j0+TY) marching over planes [k0, k1).  The
 // compact trace of the cells [i0-1, i0+TX] x [j0-1, j0+TY] of planes k-1 and k
-// is staged in shared memory (coalesced loads).  Per plane, every face and
-// edge quantity the tile needs forms one flat work list (x/y/z fluxes, z-, y-
-// and x-edge emfs), so no warp idles between item kinds.
+// is read through L1, or staged in shared memory (STAGE).  Per plane, the
+// faces and edges the tile needs form one flat work list: all faces first
+// (one code path for the three directions, the HLLD solver), then all edges
+// (one code path, the 2D HLLD emf), so a warp runs at most two item kinds
+// and the kernel holds one copy of each solver.
 template <int TX, int TY>
 struct UpdTile
 {
   static constexpr int XE = TX + 2, YE = TY + 2, PL = XE * YE; // trace cells per plane
   static constexpr int FXS = (TX + 1) * TY, FYS = TX * (TY + 1), FZS = TX * TY;
   static constexpr int EZS = (TX + 1) * (TY + 1), EYS = (TX + 1) * TY, EXS = TX * (TY + 1);
-  static constexpr int ITEMS = FXS + FYS + FZS + EZS + EYS + EXS;
 };
 
 template <class S, class R, int TX, int TY, bool STAGE>
@@ -566,114 +567,67 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
     R * Ez = sEz + (k & 1) * T::EZS;
     R * Ey = sEy + (k & 1) * T::EYS;
     R * Ex = sEx + (k & 1) * T::EXS;
-    for (int w = threadIdx.x; w < T::ITEMS; w += NT)
+    // faces (z, x, y; padded to whole warps) then edges (y, x, z); plane k1
+    // only needs its z-faces and its y- and x-edges
+    const int nf = plane ? T::FZS + T::FXS + T::FYS : T::FZS;
+    const int nfp = (nf + 31) & ~31;
+    const int ne = plane ? T::EYS + T::EXS + T::EZS : T::EYS + T::EXS;
+    for (int w = threadIdx.x; w < nfp + ne; w += NT)
     {
-      int f = w;
-      if (f < T::FXS)
+      if (w < nfp)
       {
-        // x-face i (MHDRunFunctors3D.h:1839-1846)
-        if (!plane)
+        if (w >= nf)
           continue;
-        const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
-        if (i > ihi || j >= jhi)
+        int f = w, d = 2;
+        if (f >= T::FZS)
+        {
+          f -= T::FZS;
+          d = 0;
+          if (f >= T::FXS)
+            f -= T::FXS, d = 1;
+        }
+        // face normal to d between cell (i,j,k) - e_d and cell (i,j,k)
+        // (MHDRunFunctors3D.h:1839-1874)
+        const int ex = TX + (d == 0 ? 1 : 0);
+        const int i = i0 + f % ex, j = j0 + f / ex;
+        if (i > ihi - (d != 0 ? 1 : 0) || j > jhi - (d != 1 ? 1 : 0))
           continue;
         R ql[8], qr[8], fl[5];
-        face_state<R, 0, true>(TS(i - 1, j, k), tst, ql, sr, sp);
-        face_state<R, 0, false>(TS(i, j, k), tst, qr, sr, sp);
+        face_state_dir<R, true>(TS(i - (d == 0), j - (d == 1), k - (d == 2)), tst, d, ql, sr, sp);
+        face_state_dir<R, false>(TS(i, j, k), tst, d, qr, sr, sp);
         mhd_hlld<R>(ql, qr, fl, C.gamma0);
+        R *       dst = d == 0 ? sFx : (d == 1 ? sFy : sFz);
+        const int nd = d == 0 ? T::FXS : (d == 1 ? T::FYS : T::FZS);
 #pragma unroll
         for (int v = 0; v < 5; ++v)
-          sFx[v * T::FXS + f] = fl[v];
+          dst[v * nd + f] = fl[v];
         continue;
       }
-      f -= T::FXS;
-      if (f < T::FYS)
+      int f = w - nfp, d = 1;
+      if (f >= T::EYS)
       {
-        // y-face, swap IU<->IV and IA<->IB (MHDRunFunctors3D.h:1848-1860)
-        if (!plane)
-          continue;
-        const int i = i0 + f % TX, j = j0 + f / TX;
-        if (i >= ihi || j > jhi)
-          continue;
-        R ql[8], qr[8], fl[5], x;
-        face_state<R, 1, true>(TS(i, j - 1, k), tst, ql, sr, sp);
-        face_state<R, 1, false>(TS(i, j, k), tst, qr, sr, sp);
-        x = ql[IU], ql[IU] = ql[IV], ql[IV] = x;
-        x = ql[IA], ql[IA] = ql[IB], ql[IB] = x;
-        x = qr[IU], qr[IU] = qr[IV], qr[IV] = x;
-        x = qr[IA], qr[IA] = qr[IB], qr[IB] = x;
-        mhd_hlld<R>(ql, qr, fl, C.gamma0);
-#pragma unroll
-        for (int v = 0; v < 5; ++v)
-          sFy[v * T::FYS + f] = fl[v];
+        f -= T::EYS;
+        d = 0;
+        if (f >= T::EXS)
+          f -= T::EXS, d = 2;
+      }
+      // edge along d at the low corner of cell (i,j,k); corners RT, RB, LT, LB
+      // lie at -1 along (p1,p2), p1, p2 and nowhere (z-edge: RT(i-1,j-1),
+      // RB(i-1,j), LT(i,j-1), LB(i,j); MHDRunFunctors3D.h:2180-2230)
+      const int ex = TX + (d != 0 ? 1 : 0);
+      const int i = i0 + f % ex, j = j0 + f / ex;
+      if (i > ihi - (d == 0 ? 1 : 0) || j > jhi - (d == 1 ? 1 : 0))
         continue;
-      }
-      f -= T::FYS;
-      if (f < T::FZS)
-      {
-        // z-face at level k, swap IU<->IW and IA<->IC (MHDRunFunctors3D.h:1862-1874)
-        const int i = i0 + f % TX, j = j0 + f / TX;
-        if (i >= ihi || j >= jhi)
-          continue;
-        R ql[8], qr[8], fl[5], x;
-        face_state<R, 2, true>(TS(i, j, k - 1), tst, ql, sr, sp);
-        face_state<R, 2, false>(TS(i, j, k), tst, qr, sr, sp);
-        x = ql[IU], ql[IU] = ql[IW], ql[IW] = x;
-        x = ql[IA], ql[IA] = ql[IC], ql[IC] = x;
-        x = qr[IU], qr[IU] = qr[IW], qr[IW] = x;
-        x = qr[IA], qr[IA] = qr[IC], qr[IC] = x;
-        mhd_hlld<R>(ql, qr, fl, C.gamma0);
-#pragma unroll
-        for (int v = 0; v < 5; ++v)
-          sFz[v * T::FZS + f] = fl[v];
-        continue;
-      }
-      f -= T::FZS;
-      if (f < T::EZS)
-      {
-        // z-edge emf of plane k, corners RT3(i-1,j-1), RB3(i-1,j), LT3(i,j-1), LB3(i,j)
-        if (!plane)
-          continue;
-        const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
-        if (i > ihi || j > jhi)
-          continue;
-        R a[8], b[8], c[8], d[8];
-        edge_state<R, 2, 0>(TS(i - 1, j - 1, k), tst, a, sr, sp);
-        edge_state<R, 2, 1>(TS(i - 1, j, k), tst, b, sr, sp);
-        edge_state<R, 2, 2>(TS(i, j - 1, k), tst, c, sr, sp);
-        edge_state<R, 2, 3>(TS(i, j, k), tst, d, sr, sp);
-        Ez[f] = mhd_compute_emf<R, 2>(a, b, c, d, C.gamma0, C.smallc);
-        continue;
-      }
-      f -= T::EZS;
-      if (f < T::EYS)
-      {
-        // y-edge emf at level k: RT2(i-1,k-1), LT2(i,k-1), RB2(i-1,k), LB2(i,k)
-        // (MHDRunFunctors3D.h:2212-2217)
-        const int i = i0 + f % (TX + 1), j = j0 + f / (TX + 1);
-        if (i > ihi || j >= jhi)
-          continue;
-        R a[8], b[8], c[8], d[8];
-        edge_state<R, 1, 0>(TS(i - 1, j, k - 1), tst, a, sr, sp);
-        edge_state<R, 1, 2>(TS(i, j, k - 1), tst, b, sr, sp);
-        edge_state<R, 1, 1>(TS(i - 1, j, k), tst, c, sr, sp);
-        edge_state<R, 1, 3>(TS(i, j, k), tst, d, sr, sp);
-        Ey[f] = mhd_compute_emf<R, 1>(a, b, c, d, C.gamma0, C.smallc);
-        continue;
-      }
-      f -= T::EYS;
-      {
-        // x-edge emf at level k: RT(j-1,k-1), RB(j-1,k), LT(j,k-1), LB(j,k)
-        const int i = i0 + f % TX, j = j0 + f / TX;
-        if (i >= ihi || j > jhi)
-          continue;
-        R a[8], b[8], c[8], d[8];
-        edge_state<R, 0, 0>(TS(i, j - 1, k - 1), tst, a, sr, sp);
-        edge_state<R, 0, 1>(TS(i, j - 1, k), tst, b, sr, sp);
-        edge_state<R, 0, 2>(TS(i, j, k - 1), tst, c, sr, sp);
-        edge_state<R, 0, 3>(TS(i, j, k), tst, d, sr, sp);
-        Ex[f] = mhd_compute_emf<R, 0>(a, b, c, d, C.gamma0, C.smallc);
-      }
+      const int p1 = d == 2 ? 0 : d + 1, p2 = d == 0 ? 2 : d - 1;
+      const int i1 = p1 == 0, j1 = p1 == 1, k1s = p1 == 2;
+      const int i2 = p2 == 0, j2 = p2 == 1, k2s = p2 == 2;
+      const EdgeCorner<R> cRT =
+        edge_corner<R, 1, 1>(TS(i - i1 - i2, j - j1 - j2, k - k1s - k2s), tst, d, p1, p2, sr, sp);
+      const EdgeCorner<R> cRB = edge_corner<R, 1, -1>(TS(i - i1, j - j1, k - k1s), tst, d, p1, p2, sr, sp);
+      const EdgeCorner<R> cLT = edge_corner<R, -1, 1>(TS(i - i2, j - j2, k - k2s), tst, d, p1, p2, sr, sp);
+      const EdgeCorner<R> cLB = edge_corner<R, -1, -1>(TS(i, j, k), tst, d, p1, p2, sr, sp);
+      const R             e = mhd_emf_corners<R>(cRT, cRB, cLT, cLB, C.gamma0, C.smallc);
+      (d == 0 ? Ex : (d == 1 ? Ey : Ez))[f] = e;
     }
     __syncthreads();
 
@@ -708,12 +662,12 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       else
       {
         // FP64 island: the CT update keeps div B at FP64 round-off
-        bx += ((double)Ezp[ezi + (TX + 1)] - (double)Ezp[ezi]) * ddtdy;
-        by -= ((double)Ezp[ezi + 1] - (double)Ezp[ezi]) * ddtdx;
-        bx -= ((double)Ey[eyi] - (double)Eyp[eyi]) * ddtdz;
-        by += ((double)Ex[exi] - (double)Exp[exi]) * ddtdz;
-        bz += ((double)Eyp[eyi + 1] - (double)Eyp[eyi]) * ddtdx;
-        bz -= ((double)Exp[exi + TX] - (double)Exp[exi]) * ddtdy;
+        bx += (f2d(Ezp[ezi + (TX + 1)]) - f2d(Ezp[ezi])) * ddtdy;
+        by -= (f2d(Ezp[ezi + 1]) - f2d(Ezp[ezi])) * ddtdx;
+        bx -= (f2d(Ey[eyi]) - f2d(Eyp[eyi])) * ddtdz;
+        by += (f2d(Ex[exi]) - f2d(Exp[exi])) * ddtdz;
+        bz += (f2d(Eyp[eyi + 1]) - f2d(Eyp[eyi])) * ddtdx;
+        bz -= (f2d(Exp[exi + TX]) - f2d(Exp[exi])) * ddtdy;
       }
       bout[0 * st + off] = bx;
       bout[1 * st + off] = by;
