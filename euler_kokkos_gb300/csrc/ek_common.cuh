@@ -178,6 +178,32 @@ f2d(float x)
     return __hiloint2double((int)(b & 0x80000000u), 0);
   return (double)x;
 }
+// Approximate FP32 reciprocal, reciprocal square root and square root (one
+// special-function-unit instruction each, about 1 ulp).  The mixed form uses
+// them where the reference divides several numbers by one denominator or
+// divides by a square root; the FP64 forms keep the reference's divisions.
+__device__ __forceinline__ float
+rcp_a(float x)
+{
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float
+rsqrt_a(float x)
+{
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float
+sqrt_a(float x)
+{
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // FP64 value in the working precision R
 template <class R>
 __device__ __forceinline__ R

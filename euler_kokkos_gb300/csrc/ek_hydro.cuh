@@ -41,20 +41,31 @@ __device__ __forceinline__ void
 hydro_prims(const R (&u)[NV], R (&q)[NV], const HydroConst<R> & C)
 {
   const R d = fmax(u[ID], C.smallr);
-  const R ux = u[IU] / d;
-  const R uy = u[IV] / d;
+  // FP32: one reciprocal of the density for the four quotients
+  R id = R(0);
+  if constexpr (sizeof(R) == 4)
+    id = rcp_a(d);
+  auto over_d = [&](R x) {
+    if constexpr (sizeof(R) == 4)
+      return x * id;
+    else
+      return x / d;
+  };
+  const R ux = over_d(u[IU]);
+  const R uy = over_d(u[IV]);
   R       eken, uz = R(0);
   if constexpr (NV == 4)
     eken = R(0.5) * (ux * ux + uy * uy);
   else
   {
-    uz = u[IW] / d;
+    uz = over_d(u[IW]);
     eken = R(0.5) * (ux * ux + uy * uy + uz * uz);
   }
-  R e = u[IP] / d - eken;
+  const R ed = over_d(u[IP]);
+  R       e = ed - eken;
   if constexpr (sizeof(R) == 4)
   {
-    if (e < R(1.0 / 128.0) * (u[IP] / d))
+    if (e < R(1.0 / 128.0) * ed)
     {
       // FP64 island: cancellation between total and kinetic energy
       const double dd = (double)d;
@@ -82,7 +93,10 @@ template <class R>
 __device__ __forceinline__ R
 hydro_sound(R d, R p, const HydroConst<R> & C)
 {
-  return sqrt(C.gamma0 * (p) / d);
+  if constexpr (sizeof(R) == 4)
+    return sqrt_a(C.gamma0 * p * rcp_a(d));
+  else
+    return sqrt(C.gamma0 * (p) / d);
 }
 
 // Per-cell source terms of trace_unsplit_{2d,3d}_along_dir
@@ -94,21 +108,30 @@ hydro_sources(const R (&q)[NV], const R (&dx)[NV], const R (&dy)[NV], const R (&
               const HydroConst<R> & C)
 {
   const R r = q[ID], p = q[IP], u = q[IU], v = q[IV];
+  R       ir = R(0);
+  if constexpr (sizeof(R) == 4)
+    ir = rcp_a(r);
+  auto over_r = [&](R x) {
+    if constexpr (sizeof(R) == 4)
+      return x * ir;
+    else
+      return x / r;
+  };
   if constexpr (NV == 4)
   {
     s[ID] = -u * dx[ID] - v * dy[ID] - (dx[IU] + dy[IV]) * r;
     s[IP] = -u * dx[IP] - v * dy[IP] - (dx[IU] + dy[IV]) * C.gamma0 * p;
-    s[IU] = -u * dx[IU] - v * dy[IU] - (dx[IP]) / r;
-    s[IV] = -u * dx[IV] - v * dy[IV] - (dy[IP]) / r;
+    s[IU] = -u * dx[IU] - v * dy[IU] - over_r(dx[IP]);
+    s[IV] = -u * dx[IV] - v * dy[IV] - over_r(dy[IP]);
   }
   else
   {
     const R w = q[IW];
     s[ID] = -u * dx[ID] - v * dy[ID] - w * dz[ID] - (dx[IU] + dy[IV] + dz[IW]) * r;
     s[IP] = -u * dx[IP] - v * dy[IP] - w * dz[IP] - (dx[IU] + dy[IV] + dz[IW]) * C.gamma0 * p;
-    s[IU] = -u * dx[IU] - v * dy[IU] - w * dz[IU] - (dx[IP]) / r;
-    s[IV] = -u * dx[IV] - v * dy[IV] - w * dz[IV] - (dy[IP]) / r;
-    s[IW] = -u * dx[IW] - v * dy[IW] - w * dz[IW] - (dz[IP]) / r;
+    s[IU] = -u * dx[IU] - v * dy[IU] - w * dz[IU] - over_r(dx[IP]);
+    s[IV] = -u * dx[IV] - v * dy[IV] - w * dz[IV] - over_r(dy[IP]);
+    s[IW] = -u * dx[IW] - v * dy[IW] - w * dz[IW] - over_r(dz[IP]);
   }
 }
 
@@ -157,8 +180,17 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
   const R etotr = pr * entho + ecinr;
   const R ptotr = pr;
 
-  const R cfastl = sqrt(fmax(C.gamma0 * pl / rl, C.smallc * C.smallc));
-  const R cfastr = sqrt(fmax(C.gamma0 * pr / rr, C.smallc * C.smallc));
+  R cfastl, cfastr;
+  if constexpr (sizeof(R) == 4)
+  {
+    cfastl = sqrt_a(fmax(C.gamma0 * pl * rcp_a(rl), C.smallc * C.smallc));
+    cfastr = sqrt_a(fmax(C.gamma0 * pr * rcp_a(rr), C.smallc * C.smallc));
+  }
+  else
+  {
+    cfastl = sqrt(fmax(C.gamma0 * pl / rl, C.smallc * C.smallc));
+    cfastr = sqrt(fmax(C.gamma0 * pr / rr, C.smallc * C.smallc));
+  }
 
   const R SL = fmin(ul, ur) - fmax(cfastl, cfastr);
   const R SR = fmax(ul, ur) + fmax(cfastl, cfastr);
@@ -166,8 +198,18 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
   const R rcl = rl * (ul - SL);
   const R rcr = rr * (SR - ur);
 
-  const R ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
-  const R ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+  R ustar, ptotstar;
+  if constexpr (sizeof(R) == 4)
+  {
+    const float irc = rcp_a(rcr + rcl);
+    ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc;
+    ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc;
+  }
+  else
+  {
+    ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
+    ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+  }
 
   R ro, uo, ptoto, etoto;
   if (SL > R(0))
@@ -179,17 +221,35 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
   }
   else if (ustar > R(0))
   {
-    ro = rl * (SL - ul) / (SL - ustar);
     uo = ustar;
     ptoto = ptotstar;
-    etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) / (SL - ustar);
+    if constexpr (sizeof(R) == 4)
+    {
+      const float is = rcp_a(SL - ustar);
+      ro = rl * (SL - ul) * is;
+      etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) * is;
+    }
+    else
+    {
+      ro = rl * (SL - ul) / (SL - ustar);
+      etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) / (SL - ustar);
+    }
   }
   else if (SR > R(0))
   {
-    ro = rr * (SR - ur) / (SR - ustar);
     uo = ustar;
     ptoto = ptotstar;
-    etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) / (SR - ustar);
+    if constexpr (sizeof(R) == 4)
+    {
+      const float is = rcp_a(SR - ustar);
+      ro = rr * (SR - ur) * is;
+      etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) * is;
+    }
+    else
+    {
+      ro = rr * (SR - ur) / (SR - ustar);
+      etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) / (SR - ustar);
+    }
   }
   else
   {

@@ -41,22 +41,34 @@ hydro_const(const KParams & P)
 // Load one (TX+4) x (TY+4) plane of U (global plane gk), convert to primitive
 // variables and store into sQ[NV][HY][HX]; halo cells are mapped through the
 // boundary conditions.
+// When the whole (TX+4) x (TY+4) halo of the tile and plane gk lie inside the
+// interior (direct), the boundary mapping is the identity and is skipped.
 template <class S, class R, int NV, int TX, int TY>
 __device__ __forceinline__ void
 load_q_plane(const S * __restrict__ U, const KParams & P, const HydroConst<R> & C, int gi0, int gj0,
-             int gk, R * sQ)
+             int gk, R * sQ, bool direct = false)
 {
   constexpr int HX = TX + 4, HY = TY + 4, NT = TX * TY;
   for (int c = threadIdx.x; c < HX * HY; c += NT)
   {
-    const int     hx = c % HX, hy = c / HX;
-    const SrcCell s = src_cell(P, gi0 - 2 + hx, gj0 - 2 + hy, gk);
-    R             u[NV], q[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v)
+    const int hx = c % HX, hy = c / HX;
+    R         u[NV], q[NV];
+    if (direct)
     {
-      R x = (R)ldg(U + v * P.vstride + s.off);
-      u[v] = flips(s, v, 0) ? -x : x;
+      const long long off = (long long)gk * P.plane + (long long)(gj0 - 2 + hy) * P.isize + (gi0 - 2 + hx);
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        u[v] = (R)ldg(U + v * P.vstride + off);
+    }
+    else
+    {
+      const SrcCell s = src_cell(P, gi0 - 2 + hx, gj0 - 2 + hy, gk);
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+      {
+        R x = (R)ldg(U + v * P.vstride + s.off);
+        u[v] = flips(s, v, 0) ? -x : x;
+      }
     }
     hydro_prims<R, NV>(u, q, C);
 #pragma unroll
@@ -326,7 +338,7 @@ ensemble_totals_kernel(const EnsInstance * __restrict__ insts, const int * __res
 // 3D: one CTA = a TX x TY column of interior cells marching over kchunk planes
 // ---------------------------------------------------------------------------
 template <class S, class R, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY)
+__global__ void __launch_bounds__(TX * TY, sizeof(R) == 4 ? 4 : 2)
 hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
 {
   constexpr int NV = 5, HX = TX + 4, HY = TY + 4, NT = TX * TY;
@@ -355,9 +367,15 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   const bool own = gi < P.nx + gw && gj < P.ny + gw;
   const long long own_off = (long long)gj * P.isize + gi;
 
+  // tile halo inside the interior in x and y: no boundary mapping needed
+  const bool xy_in = gi0 - 2 >= gw && gi0 + TX + 1 < P.nx + gw && gj0 - 2 >= gw && gj0 + TY + 1 < P.ny + gw;
+  auto       plane_in = [&](int gk) { return xy_in && gk >= gw && gk < P.nz + gw; };
+
   // prologue: planes k0-2, k0-1
-  load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 2 + gw, sQ + ((k0 + 1) % 3) * QP);
-  load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 1 + gw, sQ + ((k0 + 2) % 3) * QP);
+  load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 2 + gw, sQ + ((k0 + 1) % 3) * QP,
+                                 plane_in(k0 - 2 + gw));
+  load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 1 + gw, sQ + ((k0 + 2) % 3) * QP,
+                                 plane_in(k0 - 1 + gw));
 
   R zmax_prev[NV];        // ZMAX face state of the cell below
   R acc[NV];              // partial update of the cell below, waiting for -Fz(k)
@@ -366,7 +384,8 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   for (int kc = k0 - 1; kc <= k1; ++kc)
   {
     // plane kc+1 into ring slot (kc+1)%3  [(kc+1+3)%3 to stay non-negative]
-    load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, kc + 1 + gw, sQ + ((kc + 4) % 3) * QP);
+    load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, kc + 1 + gw, sQ + ((kc + 4) % 3) * QP,
+                                   plane_in(kc + 1 + gw));
     __syncthreads();
     const R * q0 = sQ + ((kc + 3) % 3) * QP;
     const R * qm = sQ + ((kc + 2) % 3) * QP;
@@ -470,44 +489,44 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
 
     if (full)
     {
-      for (int fidx = threadIdx.x; fidx < (TX + 1) * TY; fidx += NT)
+      // x- and y-faces of the plane as one work list (one HLLC code path;
+      // the y-faces swap IU and IV around the solver)
+      constexpr int NFX = (TX + 1) * TY, NFY = TX * (TY + 1);
+      for (int fidx = threadIdx.x; fidx < NFX + NFY; fidx += NT)
       {
-        const int i = fidx % (TX + 1), j = fidx / (TX + 1);
-        R         ql[NV], qr[NV], fl[NV];
+        const bool ydir = fidx >= NFX;
+        const int  g = ydir ? fidx - NFX : fidx;
+        const int  i = ydir ? g % TX : g % (TX + 1), j = ydir ? g / TX : g / (TX + 1);
+        const R *  lsrc = ydir ? sYp + j * TX + i : sXp + j * FX + i;
+        R *        rsrc = ydir ? sYm + (j + 1) * TX + i : sXm + j * FX + i + 1;
+        const int  vs = ydir ? (TY + 2) * TX : TY * FX; // variable stride
+        R          ql[NV], qr[NV], fl[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v)
         {
-          ql[v] = sXp[(v * TY + j) * FX + i];
-          qr[v] = sXm[(v * TY + j) * FX + i + 1];
+          ql[v] = lsrc[v * vs];
+          qr[v] = rsrc[v * vs];
         }
-        hllc<R, NV>(ql, qr, fl, C);
-#pragma unroll
-        for (int v = 0; v < NV; ++v)
-          sXm[(v * TY + j) * FX + i + 1] = fl[v] * dtdx;
-      }
-      for (int fidx = threadIdx.x; fidx < TX * (TY + 1); fidx += NT)
-      {
-        const int i = fidx % TX, j = fidx / TX;
-        R         ql[NV], qr[NV], fl[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v)
+        if (ydir)
         {
-          ql[v] = sYp[(v * (TY + 2) + j) * TX + i];
-          qr[v] = sYm[(v * (TY + 2) + j + 1) * TX + i];
+          R tmp = ql[IU];
+          ql[IU] = ql[IV];
+          ql[IV] = tmp;
+          tmp = qr[IU];
+          qr[IU] = qr[IV];
+          qr[IV] = tmp;
         }
-        R tmp = ql[IU];
-        ql[IU] = ql[IV];
-        ql[IV] = tmp;
-        tmp = qr[IU];
-        qr[IU] = qr[IV];
-        qr[IV] = tmp;
         hllc<R, NV>(ql, qr, fl, C);
-        tmp = fl[IU];
-        fl[IU] = fl[IV];
-        fl[IV] = tmp;
+        if (ydir)
+        {
+          R tmp = fl[IU];
+          fl[IU] = fl[IV];
+          fl[IV] = tmp;
+        }
+        const R dtd = ydir ? dtdy : dtdx;
 #pragma unroll
         for (int v = 0; v < NV; ++v)
-          sYm[(v * (TY + 2) + j + 1) * TX + i] = fl[v] * dtdy;
+          rsrc[v * vs] = fl[v] * dtd;
       }
       __syncthreads();
     }

@@ -37,6 +37,17 @@ mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz, float idx,
 {
   const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
   const R b2 = a * a + b * b + c * c;
+  if constexpr (sizeof(R) == 4)
+  {
+    const float id = rcp_a(d);
+    const float c2 = gamma0 * p * id;
+    const float d2 = 0.5f * (b2 * id + c2);
+    const float dd = d2 * d2, cr = c2 * id;
+    const float cfx = sqrt_a(d2 + sqrt_a(dd - cr * a * a));
+    const float cfy = sqrt_a(d2 + sqrt_a(dd - cr * b * b));
+    const float cfz = sqrt_a(d2 + sqrt_a(dd - cr * c * c));
+    return (cfx + fabsf(q[IU])) * idx + (cfy + fabsf(q[IV])) * idy + (cfz + fabsf(q[IW])) * idz;
+  }
   const R c2 = gamma0 * p / d;
   const R d2 = R(0.5) * (b2 / d + c2);
   const R cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d));
@@ -62,15 +73,30 @@ mhd_constoprim(const R (&u)[5], const R (&bl)[3], const R (&br)[3], R (&q)[8], c
                FB && fp64_faces)
 {
   q[ID] = fmax(u[ID], C.smallr);
-  q[IU] = u[IU] / q[ID];
-  q[IV] = u[IV] / q[ID];
-  q[IW] = u[IW] / q[ID];
+  R id = R(0);
+  if constexpr (sizeof(R) == 4)
+  {
+    id = rcp_a(q[ID]);
+    q[IU] = u[IU] * id;
+    q[IV] = u[IV] * id;
+    q[IW] = u[IW] * id;
+  }
+  else
+  {
+    q[IU] = u[IU] / q[ID];
+    q[IV] = u[IV] / q[ID];
+    q[IW] = u[IW] / q[ID];
+  }
   q[IA] = R(0.5) * (bl[0] + br[0]);
   q[IB] = R(0.5) * (bl[1] + br[1]);
   q[IC] = R(0.5) * (bl[2] + br[2]);
   const R eken = R(0.5) * (q[IU] * q[IU] + q[IV] * q[IV] + q[IW] * q[IW]);
   const R emag = R(0.5) * (q[IA] * q[IA] + q[IB] * q[IB] + q[IC] * q[IC]);
-  R       eint = (u[IP] - emag) / q[ID] - eken;
+  R       eint;
+  if constexpr (sizeof(R) == 4)
+    eint = (u[IP] - emag) * id - eken;
+  else
+    eint = (u[IP] - emag) / q[ID] - eken;
   if constexpr (sizeof(R) == 4)
   {
     // FP64 island: E - emag - rho*eken cancels (low beta or high Mach)
@@ -89,12 +115,155 @@ mhd_constoprim(const R (&u)[5], const R (&bl)[3], const R (&br)[3], R (&q)[8], c
   q[IP] = fmax((C.gamma0 - R(1.0)) * q[ID] * eint, q[ID] * C.smallp);
 }
 
+// riemann_hlld in FP32 for the mixed form: the reference's solver with each
+// shared denominator inverted once (rcp_a) and |B_n| / sqrt(rho*) as a
+// reciprocal square root; same branches and degeneracy test.
+__device__ __forceinline__ float
+mhd_speed_fast_f32(float d, float p, float a, float b, float c, float bn, float gamma0)
+{
+  const float id = rcp_a(d);
+  const float c2 = gamma0 * p * id;
+  const float d2 = 0.5f * ((a * a + b * b + c * c) * id + c2);
+  return sqrt_a(d2 + sqrt_a(d2 * d2 - c2 * bn * bn * id));
+}
+
+__device__ __forceinline__ void
+mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[5], float gamma0)
+{
+  const float entho = rcp_a(gamma0 - 1.0f);
+  const float a = 0.5f * (ql[IA] + qr[IA]);
+  const float sgnm = (a >= 0.f) ? 1.f : -1.f;
+  const float a2 = a * a;
+  const float rl = ql[ID], pl = ql[IP], ul = ql[IU], vl = ql[IV], wl = ql[IW], bl = ql[IB], cl = ql[IC];
+  const float ecinl = 0.5f * (ul * ul + vl * vl + wl * wl) * rl;
+  const float emagl = 0.5f * (a2 + bl * bl + cl * cl);
+  const float etotl = pl * entho + ecinl + emagl;
+  const float ptotl = pl + emagl;
+  const float vdotbl = ul * a + vl * bl + wl * cl;
+  const float rr = qr[ID], pr = qr[IP], ur = qr[IU], vr = qr[IV], wr = qr[IW], br = qr[IB], cr = qr[IC];
+  const float ecinr = 0.5f * (ur * ur + vr * vr + wr * wr) * rr;
+  const float emagr = 0.5f * (a2 + br * br + cr * cr);
+  const float etotr = pr * entho + ecinr + emagr;
+  const float ptotr = pr + emagr;
+  const float vdotbr = ur * a + vr * br + wr * cr;
+
+  const float cfastl = mhd_speed_fast_f32(rl, pl, a, bl, cl, a, gamma0);
+  const float cfastr = mhd_speed_fast_f32(rr, pr, a, br, cr, a, gamma0);
+  const float sl = fminf(ul, ur) - fmaxf(cfastl, cfastr);
+  const float sr = fmaxf(ul, ur) + fmaxf(cfastl, cfastr);
+  const float rcl = rl * (ul - sl);
+  const float rcr = rr * (sr - ur);
+  const float irc = rcp_a(rcr + rcl);
+  const float ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc;
+  const float ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc;
+  const float ia2 = rcp_a(a2);
+
+  const float isl = rcp_a(sl - ustar);
+  const float rstarl = rl * (sl - ul) * isl;
+  float       estar = rl * (sl - ul) * (sl - ustar) - a2;
+  const float el = rl * (sl - ul) * (sl - ul) - a2;
+  float       vstarl, wstarl, bstarl, cstarl;
+  if (a2 > 0.f && fabsf(estar * ia2 - 1.f) <= 1e-8f)
+  {
+    vstarl = vl, bstarl = bl, wstarl = wl, cstarl = cl;
+  }
+  else
+  {
+    const float ie = rcp_a(estar);
+    vstarl = vl - a * bl * (ustar - ul) * ie;
+    bstarl = bl * el * ie;
+    wstarl = wl - a * cl * (ustar - ul) * ie;
+    cstarl = cl * el * ie;
+  }
+  const float vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
+  const float etotstarl = ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) * isl;
+  const float sqrrstarl = sqrt_a(rstarl);
+  const float sal = ustar - fabsf(a) * rsqrt_a(rstarl);
+
+  const float isr = rcp_a(sr - ustar);
+  const float rstarr = rr * (sr - ur) * isr;
+  estar = rr * (sr - ur) * (sr - ustar) - a2;
+  const float er = rr * (sr - ur) * (sr - ur) - a2;
+  float       vstarr, wstarr, bstarr, cstarr;
+  if (a2 > 0.f && fabsf(estar * ia2 - 1.f) <= 1e-8f)
+  {
+    vstarr = vr, bstarr = br, wstarr = wr, cstarr = cr;
+  }
+  else
+  {
+    const float ie = rcp_a(estar);
+    vstarr = vr - a * br * (ustar - ur) * ie;
+    bstarr = br * er * ie;
+    wstarr = wr - a * cr * (ustar - ur) * ie;
+    cstarr = cr * er * ie;
+  }
+  const float vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
+  const float etotstarr = ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) * isr;
+  const float sqrrstarr = sqrt_a(rstarr);
+  const float sar = ustar + fabsf(a) * rsqrt_a(rstarr);
+
+  float ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
+  if (sl > 0.f)
+  {
+    ro = rl, uo = ul, vo = vl, wo = wl, bo = bl, co = cl;
+    ptoto = ptotl, etoto = etotl, vdotbo = vdotbl;
+  }
+  else if (sal > 0.f)
+  {
+    ro = rstarl, uo = ustar, vo = vstarl, wo = wstarl, bo = bstarl, co = cstarl;
+    ptoto = ptotstar, etoto = etotstarl, vdotbo = vdotbstarl;
+  }
+  else if (sr > 0.f && !(ustar > 0.f) && !(sar > 0.f))
+  {
+    ro = rstarr, uo = ustar, vo = vstarr, wo = wstarr, bo = bstarr, co = cstarr;
+    ptoto = ptotstar, etoto = etotstarr, vdotbo = vdotbstarr;
+  }
+  else if (!(sr > 0.f) && !(ustar > 0.f) && !(sar > 0.f))
+  {
+    ro = rr, uo = ur, vo = vr, wo = wr, bo = br, co = cr;
+    ptoto = ptotr, etoto = etotr, vdotbo = vdotbr;
+  }
+  else
+  {
+    const float iss = rcp_a(sqrrstarl + sqrrstarr);
+    const float vss = (sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl)) * iss;
+    const float wss = (sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl)) * iss;
+    const float bss = (sqrrstarl * bstarr + sqrrstarr * bstarl + sgnm * sqrrstarl * sqrrstarr * (vstarr - vstarl)) * iss;
+    const float css = (sqrrstarl * cstarr + sqrrstarr * cstarl + sgnm * sqrrstarl * sqrrstarr * (wstarr - wstarl)) * iss;
+    const float vdotbss = ustar * a + vss * bss + wss * css;
+    vo = vss, wo = wss, bo = bss, co = css;
+    uo = ustar, ptoto = ptotstar, vdotbo = vdotbss;
+    if (ustar > 0.f)
+    {
+      ro = rstarl;
+      etoto = etotstarl - sgnm * sqrrstarl * (vdotbstarl - vdotbss);
+    }
+    else
+    {
+      ro = rstarr;
+      etoto = etotstarr + sgnm * sqrrstarr * (vdotbstarr - vdotbss);
+    }
+  }
+  flux[ID] = ro * uo;
+  flux[IP] = (etoto + ptoto) * uo - a * vdotbo;
+  flux[IU] = ro * uo * uo - a2 + ptoto;
+  flux[IV] = ro * uo * vo - a * bo;
+  flux[IW] = ro * uo * wo - a * co;
+}
+
 // riemann_hlld (RiemannSolvers_MHD.h:130-364), states in the face frame.
 // Only the five hydro components of the flux are used by the 3D update.
 template <class R>
 __device__ __forceinline__ void
 mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[5], R gamma0)
 {
+  if constexpr (sizeof(R) == 4)
+  {
+    mhd_hlld_f32(ql, qr, flux, gamma0);
+    return;
+  }
+  else
+  {
   const R entho = R(1.0) / (gamma0 - R(1.0));
   const R a = R(0.5) * (ql[IA] + qr[IA]);
   const R sgnm = (a >= R(0)) ? R(1) : R(-1);
@@ -226,6 +395,7 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[5], R gamma0)
   flux[IU] = ro * uo * uo - a * a + ptoto;
   flux[IV] = ro * uo * vo - a * bo;
   flux[IW] = ro * uo * wo - a * co;
+  }
 }
 
 template <class R>
@@ -269,12 +439,133 @@ struct EdgeQ
   R r, p, u, v, a, b, c;
 };
 
+// mag_riemann2d_hlld in FP32 for the mixed form: one reciprocal per corner
+// density and per shared denominator, |B| / sqrt(rho*) as reciprocal square
+// roots; the reference's branch-free selection of the emf.
+__device__ __forceinline__ float
+mag_riemann2d_hlld_f32(const EdgeQ<float> & LL, const EdgeQ<float> & RL, const EdgeQ<float> & LR,
+                       const EdgeQ<float> & RR, float ELL, float ERL, float ELR, float ERR, float gamma0,
+                       float smallc)
+{
+  auto fast2 = [gamma0](const EdgeQ<float> & q, float & cx, float & cy) {
+    const float ir = rcp_a(q.r);
+    const float c2 = gamma0 * q.p * ir;
+    const float d2 = 0.5f * ((q.a * q.a + q.b * q.b + q.c * q.c) * ir + c2);
+    const float dd = d2 * d2, cr = c2 * ir;
+    cx = sqrt_a(d2 + sqrt_a(dd - cr * q.a * q.a));
+    cy = sqrt_a(d2 + sqrt_a(dd - cr * q.b * q.b));
+  };
+  const float rLL = LL.r, pLL = LL.p, uLL = LL.u, vLL = LL.v, aLL = LL.a, bLL = LL.b, cLL = LL.c;
+  const float rLR = LR.r, pLR = LR.p, uLR = LR.u, vLR = LR.v, aLR = LR.a, bLR = LR.b, cLR = LR.c;
+  const float rRL = RL.r, pRL = RL.p, uRL = RL.u, vRL = RL.v, aRL = RL.a, bRL = RL.b, cRL = RL.c;
+  const float rRR = RR.r, pRR = RR.p, uRR = RR.u, vRR = RR.v, aRR = RR.a, bRR = RR.b, cRR = RR.c;
+  float cLLx, cLLy, cLRx, cLRy, cRLx, cRLy, cRRx, cRRy;
+  fast2(LL, cLLx, cLLy);
+  fast2(LR, cLRx, cLRy);
+  fast2(RL, cRLx, cRLy);
+  fast2(RR, cRRx, cRRy);
+  const float cmx = fmax4(cLLx, cLRx, cRLx, cRRx), cmy = fmax4(cLLy, cLRy, cRLy, cRRy);
+  const float SL = fmin4(uLL, uLR, uRL, uRR) - cmx;
+  const float SR = fmax4(uLL, uLR, uRL, uRR) + cmx;
+  const float SB = fmin4(vLL, vLR, vRL, vRR) - cmy;
+  const float ST = fmax4(vLL, vLR, vRL, vRR) + cmy;
+
+  const float PtotLL = pLL + 0.5f * (aLL * aLL + bLL * bLL + cLL * cLL);
+  const float PtotLR = pLR + 0.5f * (aLR * aLR + bLR * bLR + cLR * cLR);
+  const float PtotRL = pRL + 0.5f * (aRL * aRL + bRL * bRL + cRL * cRL);
+  const float PtotRR = pRR + 0.5f * (aRR * aRR + bRR * bRR + cRR * cRR);
+
+  const float rcLLx = rLL * (uLL - SL), rcRLx = rRL * (SR - uRL);
+  const float rcLRx = rLR * (uLR - SL), rcRRx = rRR * (SR - uRR);
+  const float rcLLy = rLL * (vLL - SB), rcLRy = rLR * (ST - vLR);
+  const float rcRLy = rRL * (vRL - SB), rcRRy = rRR * (ST - vRR);
+
+  const float ustar = (rcLLx * uLL + rcLRx * uLR + rcRLx * uRL + rcRRx * uRR + (PtotLL - PtotRL + PtotLR - PtotRR)) *
+                      rcp_a(rcLLx + rcLRx + rcRLx + rcRRx);
+  const float vstar = (rcLLy * vLL + rcLRy * vLR + rcRLy * vRL + rcRRy * vRR + (PtotLL - PtotLR + PtotRL - PtotRR)) *
+                      rcp_a(rcLLy + rcLRy + rcRLy + rcRRy);
+  const float iL = rcp_a(SL - ustar), iR = rcp_a(SR - ustar), iB = rcp_a(SB - vstar), iT = rcp_a(ST - vstar);
+
+  // star states of corner (r, u, v, a, b) against the x-side factor fx and y-side factor fy
+  const float fxLL = (SL - uLL) * iL, fyLL = (SB - vLL) * iB;
+  const float fxLR = (SL - uLR) * iL, fyLR = (ST - vLR) * iT;
+  const float fxRL = (SR - uRL) * iR, fyRL = (SB - vRL) * iB;
+  const float fxRR = (SR - uRR) * iR, fyRR = (ST - vRR) * iT;
+
+  const float rstarLLx = rLL * fxLL, BstarLL = bLL * fxLL, rstarLLy = rLL * fyLL, AstarLL = aLL * fyLL;
+  const float rstarLL = rstarLLx * fyLL;
+  const float EstarLLx = ustar * BstarLL - vLL * aLL, EstarLLy = uLL * bLL - vstar * AstarLL;
+  const float EstarLL = ustar * BstarLL - vstar * AstarLL;
+  const float rstarLRx = rLR * fxLR, BstarLR = bLR * fxLR, rstarLRy = rLR * fyLR, AstarLR = aLR * fyLR;
+  const float rstarLR = rstarLRx * fyLR;
+  const float EstarLRx = ustar * BstarLR - vLR * aLR, EstarLRy = uLR * bLR - vstar * AstarLR;
+  const float EstarLR = ustar * BstarLR - vstar * AstarLR;
+  const float rstarRLx = rRL * fxRL, BstarRL = bRL * fxRL, rstarRLy = rRL * fyRL, AstarRL = aRL * fyRL;
+  const float rstarRL = rstarRLx * fyRL;
+  const float EstarRLx = ustar * BstarRL - vRL * aRL, EstarRLy = uRL * bRL - vstar * AstarRL;
+  const float EstarRL = ustar * BstarRL - vstar * AstarRL;
+  const float rstarRRx = rRR * fxRR, BstarRR = bRR * fxRR, rstarRRy = rRR * fyRR, AstarRR = aRR * fyRR;
+  const float rstarRR = rstarRRx * fyRR;
+  const float EstarRRx = ustar * BstarRR - vRR * aRR, EstarRRy = uRR * bRR - vstar * AstarRR;
+  const float EstarRR = ustar * BstarRR - vstar * AstarRR;
+
+  const float qLL = rsqrt_a(rstarLL), qLR = rsqrt_a(rstarLR), qRL = rsqrt_a(rstarRL), qRR = rsqrt_a(rstarRR);
+  const float calfvenL = fmax5(fabsf(aLR) * rsqrt_a(rstarLRx), fabsf(AstarLR) * qLR,
+                               fabsf(aLL) * rsqrt_a(rstarLLx), fabsf(AstarLL) * qLL, smallc);
+  const float calfvenR = fmax5(fabsf(aRR) * rsqrt_a(rstarRRx), fabsf(AstarRR) * qRR,
+                               fabsf(aRL) * rsqrt_a(rstarRLx), fabsf(AstarRL) * qRL, smallc);
+  const float calfvenB = fmax5(fabsf(bLL) * rsqrt_a(rstarLLy), fabsf(BstarLL) * qLL,
+                               fabsf(bRL) * rsqrt_a(rstarRLy), fabsf(BstarRL) * qRL, smallc);
+  const float calfvenT = fmax5(fabsf(bLR) * rsqrt_a(rstarLRy), fabsf(BstarLR) * qLR,
+                               fabsf(bRR) * rsqrt_a(rstarRRy), fabsf(BstarRR) * qRR, smallc);
+
+  const float SAL = fminf(ustar - calfvenL, 0.f);
+  const float SAR = fmaxf(ustar + calfvenR, 0.f);
+  const float SAB = fminf(vstar - calfvenB, 0.f);
+  const float SAT = fmaxf(vstar + calfvenT, 0.f);
+  const float iAx = rcp_a(SAR - SAL), iAy = rcp_a(SAT - SAB);
+
+  const float AstarT = (SAR * AstarRR - SAL * AstarLR) * iAx;
+  const float AstarB = (SAR * AstarRL - SAL * AstarLL) * iAx;
+  const float BstarR = (SAT * BstarRR - SAB * BstarRL) * iAy;
+  const float BstarL = (SAT * BstarLR - SAB * BstarLL) * iAy;
+
+  float     E = 0.f, tmpE;
+  const int SB_pos = (int)(1 + copysignf(1.f, SB)) / 2, SB_neg = 1 - SB_pos;
+  const int ST_pos = (int)(1 + copysignf(1.f, ST)) / 2, ST_neg = 1 - ST_pos;
+  const int SL_pos = (int)(1 + copysignf(1.f, SL)) / 2, SL_neg = 1 - SL_pos;
+  const int SR_pos = (int)(1 + copysignf(1.f, SR)) / 2, SR_neg = 1 - SR_pos;
+
+  tmpE = (SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL) * iAx * iAy -
+         SAT * SAB * iAy * (AstarT - AstarB) + SAR * SAL * iAx * (BstarR - BstarL);
+  E += (float)(SB_neg * ST_pos * SL_neg * SR_pos) * tmpE;
+
+  tmpE = (SAR * EstarLLx - SAL * EstarRLx + SAR * SAL * (bRL - bLL)) * iAx;
+  tmpE = (float)SL_pos * ELL + (float)(SL_neg * SR_neg) * ERL + (float)(SL_neg * SR_pos) * tmpE;
+  E += (float)SB_pos * tmpE;
+
+  tmpE = (SAR * EstarLRx - SAL * EstarRRx + SAR * SAL * (bRR - bLR)) * iAx;
+  tmpE = (float)SL_pos * ELR + (float)(SL_neg * SR_neg) * ERR + (float)(SL_neg * SR_pos) * tmpE;
+  E += (float)(SB_neg * ST_neg) * tmpE;
+
+  tmpE = (SAT * EstarLLy - SAB * EstarLRy - SAT * SAB * (aLR - aLL)) * iAy;
+  E += (float)(SB_neg * ST_pos * SL_pos) * tmpE;
+
+  tmpE = (SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL)) * iAy;
+  E += (float)(SB_neg * ST_pos * SL_neg * SR_neg) * tmpE;
+  return E;
+}
+
 // mag_riemann2d_hlld (RiemannSolvers_MHD.h:395-627); corners LL, RL, LR, RR
 template <class R>
 __device__ __forceinline__ R
 mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR,
                    const EdgeQ<R> & RR, R ELL, R ERL, R ELR, R ERR, R gamma0, R smallc)
 {
+  if constexpr (sizeof(R) == 4)
+    return mag_riemann2d_hlld_f32(LL, RL, LR, RR, ELL, ERL, ELR, ERR, gamma0, smallc);
+  else
+  {
   auto fast = [gamma0](const EdgeQ<R> & q, bool ydir) {
     const R b2 = q.a * q.a + q.b * q.b + q.c * q.c;
     const R c2 = gamma0 * q.p / q.r;
@@ -398,6 +689,7 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
   tmpE = (SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL)) / (SAT - SAB);
   E += (R)(SB_neg * ST_pos * SL_neg * SR_neg) * tmpE;
   return E;
+  }
 }
 
 // compute_emf<emfDir> (RiemannSolvers_MHD.h:648-871) on the four corner

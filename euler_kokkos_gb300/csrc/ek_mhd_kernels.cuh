@@ -273,12 +273,26 @@ trace_cell_compact(const R * sB, int bslot[4], const R * sQ, int qslot[3], const
   const R gamma = C.gamma0;
   const R C_ = Cc;
   const R sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
-  const R su0 = (-u * dux - (dpx + B * dBx + C_ * dCx) / r) * dtdx + (-v * duy + B * dAy / r) * dtdy +
-                (-w * duz + C_ * dAz / r) * dtdz;
-  const R sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - (dpy + A * dAy + C_ * dCy) / r) * dtdy +
-                (-w * dvz + C_ * dBz / r) * dtdz;
-  const R sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + B * dCy / r) * dtdy +
-                (-w * dwz - (dpz + A * dAz + B * dBz) / r) * dtdz;
+  R su0, sv0, sw0;
+  if constexpr (sizeof(R) == 4)
+  {
+    const float ir = rcp_a(r);
+    su0 = (-u * dux - (dpx + B * dBx + C_ * dCx) * ir) * dtdx + (-v * duy + B * dAy * ir) * dtdy +
+          (-w * duz + C_ * dAz * ir) * dtdz;
+    sv0 = (-u * dvx + A * dBx * ir) * dtdx + (-v * dvy - (dpy + A * dAy + C_ * dCy) * ir) * dtdy +
+          (-w * dvz + C_ * dBz * ir) * dtdz;
+    sw0 = (-u * dwx + A * dCx * ir) * dtdx + (-v * dwy + B * dCy * ir) * dtdy +
+          (-w * dwz - (dpz + A * dAz + B * dBz) * ir) * dtdz;
+  }
+  else
+  {
+    su0 = (-u * dux - (dpx + B * dBx + C_ * dCx) / r) * dtdx + (-v * duy + B * dAy / r) * dtdy +
+          (-w * duz + C_ * dAz / r) * dtdz;
+    sv0 = (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - (dpy + A * dAy + C_ * dCy) / r) * dtdy +
+          (-w * dvz + C_ * dBz / r) * dtdz;
+    sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + B * dCy / r) * dtdy +
+          (-w * dwz - (dpz + A * dAz + B * dBz) / r) * dtdz;
+  }
   const R sp0 = (-u * dpx - dux * gamma * p) * dtdx + (-v * dpy - dvy * gamma * p) * dtdy +
                 (-w * dpz - dwz * gamma * p) * dtdz;
   const R sA0 = (u * dBy + B * duy - v * dAy - A * dvy) * dtdy + (u * dCz + C_ * duz - w * dAz - A * dwz) * dtdz;
