@@ -387,6 +387,7 @@ class SolverFactory:
     _registry = {
         "Hydro_Muscl_2D": Solver,
         "Hydro_Muscl_3D": Solver,
+        "MHD_Muscl_2D": Solver,
         "MHD_Muscl_3D": Solver,
     }
 

@@ -158,8 +158,6 @@ validate(const ek_params & p)
   for (int f = 0; f < 2 * p.dim; ++f)
     if (p.bc[f] < 1 || p.bc[f] > 3)
       return fail(EK_ERR_INVALID, "boundary types must be 1 (reflect), 2 (outflow) or 3 (periodic)");
-  if (p.mhd && p.dim == 2)
-    return fail(EK_ERR_UNSUPPORTED, "MHD_Muscl_2D is not implemented by this library");
   if (!p.mhd && p.riemann != 3)
     return fail(EK_ERR_UNSUPPORTED, "hydro: only riemann=hllc is implemented");
   if (p.mhd && p.riemann != 4)
@@ -268,7 +266,7 @@ ek_solver_create(const ek_params * params, ek_solver ** out)
     e = cudaMalloc((void **)&s->dtlog, sizeof(double) * s->dtcap);
   if (e == cudaSuccess)
     e = cudaMalloc((void **)&s->scratch3, 3 * sizeof(double));
-  if (e == cudaSuccess && p.mhd)
+  if (e == cudaSuccess && p.mhd && p.dim == 3)
   {
     s->work_bytes = s->exact ? ek_exact::mhd_work_bytes(s->prec, k) : ek_fast::mhd_work_bytes(s->prec, k);
     if (s->work_bytes)
@@ -410,7 +408,10 @@ static ek_status
 launch_dt(ek_solver * s, const void * U, unsigned long long * key)
 {
   cudaError_t e;
-  if (s->p.mhd)
+  if (s->p.mhd && s->p.dim == 2)
+    e = s->exact ? ek_exact::mhd2d_dt(s->prec, U, s->kp, key, s->stream)
+                 : ek_fast::mhd2d_dt(s->prec, U, s->kp, key, s->stream);
+  else if (s->p.mhd)
     e = s->exact ? ek_exact::mhd_dt(s->prec, U, s->kp, key, s->stream)
                  : ek_fast::mhd_dt(s->prec, U, s->kp, key, s->stream);
   else
@@ -542,7 +543,10 @@ launch_one(ek_solver * s, int kernel_id, int phase, int step)
     cudaEventRecord(e0, s->stream);
   }
   cudaError_t e;
-  if (s->p.mhd)
+  if (s->p.mhd && s->p.dim == 2)
+    e = s->exact ? ek_exact::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, s->stream)
+                 : ek_fast::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, s->stream);
+  else if (s->p.mhd)
     e = s->exact ? ek_exact::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream)
                  : ek_fast::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream);
   else
@@ -565,6 +569,13 @@ launch_step(ek_solver * s, int step)
 {
   if (!s->p.mhd)
     return launch_one(s, 0, 0, step);
+  if (s->p.dim == 2)
+  {
+    ek_status st = launch_one(s, 2, 0, step); // CFL of the step
+    if (st == EK_OK)
+      st = launch_one(s, 0, 1, step); // trace, fluxes, emf, update
+    return st;
+  }
   ek_status st = launch_one(s, 2, 0, step); // CFL of the step
   if (st == EK_OK)
     st = launch_one(s, 1, 1, step); // trace

@@ -4,6 +4,7 @@
 #include "ek_launch.h"
 #include "ek_hydro_kernels.cuh"
 #include "ek_mhd_kernels.cuh"
+#include "ek_mhd2d_kernels.cuh"
 
 namespace EK_NS
 {

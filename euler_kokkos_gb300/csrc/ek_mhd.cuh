@@ -127,8 +127,9 @@ mhd_speed_fast_f32(float d, float p, float a, float b, float c, float bn, float 
   return sqrt_a(d2 + sqrt_a(d2 * d2 - c2 * bn * bn * id));
 }
 
+template <int NF>
 __device__ __forceinline__ void
-mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[5], float gamma0)
+mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], float gamma0)
 {
   const float entho = rcp_a(gamma0 - 1.0f);
   const float a = 0.5f * (ql[IA] + qr[IA]);
@@ -249,17 +250,20 @@ mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[5], float
   flux[IU] = ro * uo * uo - a2 + ptoto;
   flux[IV] = ro * uo * vo - a * bo;
   flux[IW] = ro * uo * wo - a * co;
+  if constexpr (NF > 5)
+    flux[5] = co * uo - a * wo;
 }
 
 // riemann_hlld (RiemannSolvers_MHD.h:130-364), states in the face frame.
-// Only the five hydro components of the flux are used by the 3D update.
-template <class R>
+// The 3D update uses the five hydro components of the flux (NF = 5); the 2D
+// update also uses the Bz component, returned in flux[5] when NF = 6.
+template <class R, int NF = 5>
 __device__ __forceinline__ void
-mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[5], R gamma0)
+mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
 {
   if constexpr (sizeof(R) == 4)
   {
-    mhd_hlld_f32(ql, qr, flux, gamma0);
+    mhd_hlld_f32<NF>(ql, qr, flux, gamma0);
     return;
   }
   else
@@ -395,6 +399,8 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[5], R gamma0)
   flux[IU] = ro * uo * uo - a * a + ptoto;
   flux[IV] = ro * uo * vo - a * bo;
   flux[IW] = ro * uo * wo - a * co;
+  if constexpr (NF > 5)
+    flux[5] = co * uo - a * wo;
   }
 }
 

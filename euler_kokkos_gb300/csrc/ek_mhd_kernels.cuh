@@ -741,11 +741,13 @@ mhd_divb_kernel(const void * __restrict__ U, KParams P, unsigned long long * key
     const int       i = (int)(c % P.nx) + P.gw;
     const long long r = c / P.nx;
     const int       j = (int)(r % P.ny) + P.gw;
-    const int       k = (int)(r / P.ny) + P.gw;
+    const int       k = P.ksize > 1 ? (int)(r / P.ny) + P.gw : 0;
     const SrcCell   s0 = src_cell(P, i, j, k);
-    const double    d = (load_face<S>(m, P, src_cell(P, i + 1, j, k), 0) - load_face<S>(m, P, s0, 0)) / P.dx +
-                     (load_face<S>(m, P, src_cell(P, i, j + 1, k), 1) - load_face<S>(m, P, s0, 1)) / P.dy +
-                     (load_face<S>(m, P, src_cell(P, i, j, k + 1), 2) - load_face<S>(m, P, s0, 2)) / P.dz;
+    double          d = (load_face<S>(m, P, src_cell(P, i + 1, j, k), 0) - load_face<S>(m, P, s0, 0)) / P.dx +
+                     (load_face<S>(m, P, src_cell(P, i, j + 1, k), 1) - load_face<S>(m, P, s0, 1)) / P.dy;
+    // 2D: Bz is not a face field (no z derivative)
+    if (P.ksize > 1)
+      d += (load_face<S>(m, P, src_cell(P, i, j, k + 1), 2) - load_face<S>(m, P, s0, 2)) / P.dz;
     const unsigned long long kk = cand_key(fabs(d));
     kmax = kk > kmax ? kk : kmax;
   }

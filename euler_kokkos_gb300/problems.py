@@ -25,6 +25,7 @@ __all__ = [
     "implode_2d",
     "blast_3d",
     "orszag_tang_3d",
+    "orszag_tang_2d",
     "mhd_blast_3d",
     "kelvin_helmholtz_2d",
     "kh_ensemble",
@@ -180,6 +181,44 @@ def orszag_tang_3d(n=256, nsteps=100, seed=0x0257A6, vz_noise=1e-3, slope_type=2
     e[:-1, :-1, :-1] = (p0 / (g - 1.0) + ekin[:-1, :-1, :-1]
                         + 0.5 * (bxc[:-1, :-1, :] ** 2 + byc[:-1, :, :-1] ** 2 + bzc[:, :-1, :-1] ** 2))
     U[1] = e
+    return ini, U
+
+
+def orszag_tang_2d(n=512, ny=None, nsteps=100, seed=0x0257A6, vz_noise=0.0, slope_type=2.0, cfl=0.8,
+                   gamma0=5.0 / 3.0, riemann="hlld"):
+    """2D Orszag-Tang: MHDInitFunctors2D.h:345-470.  rho = gamma p0, p0 =
+    gamma/(4 pi), v = (-sin 2 pi y, sin 2 pi x, vz_noise*u), B = (-B0 sin 2 pi y,
+    B0 sin 4 pi x, 0) at cell centres (each component constant along its own
+    direction, so the discrete div B is exactly zero), B0 = 1/sqrt(4 pi); the
+    total energy uses the face-averaged B for cells i, j < size-1."""
+    ny = n if ny is None else ny
+    gw = 3
+    ini = _deck("MHD_Muscl_2D", n, ny, 1, (3, 3, 3, 3, 3, 3), gamma0, cfl, slope_type, riemann,
+                "orszag_tang", nsteps, {"OrszagTang": {"kt": 0.0, "vortex_dir": 2}})
+    g = _f(gamma0)
+    twopi = 2 * math.pi
+    B0 = 1.0 / math.sqrt(2 * twopi)
+    p0 = g / (2 * twopi)
+    d0 = g * p0
+    X = _centres(n, gw, 0.0, 1.0 / n)[None, :]
+    Y = _centres(ny, gw, 0.0, 1.0 / ny)[:, None]
+    sy, sx = ny + 2 * gw, n + 2 * gw
+    idx = np.arange(sx * sy, dtype=np.uint64).reshape(sy, sx)
+    U = np.zeros((8, 1, sy, sx))
+    U[0, 0] = d0
+    U[2, 0] = np.broadcast_to(-d0 * np.sin(Y * twopi), (sy, sx))
+    U[3, 0] = np.broadcast_to(d0 * np.sin(X * twopi), (sy, sx))
+    U[4, 0] = d0 * vz_noise * splitmix_uniform(seed, idx) if vz_noise else 0.0
+    U[5, 0] = np.broadcast_to(-B0 * np.sin(Y * twopi), (sy, sx))
+    U[6, 0] = np.broadcast_to(B0 * np.sin(2.0 * X * twopi), (sy, sx))
+    U[7, 0] = 0.0
+    u0 = U[:, 0]
+    e = np.zeros((sy, sx))
+    e[:-1, :-1] = (p0 / (g - 1.0)
+                   + 0.5 * (u0[2, :-1, :-1] ** 2 / u0[0, :-1, :-1] + u0[3, :-1, :-1] ** 2 / u0[0, :-1, :-1])
+                   + 0.5 * (((u0[5, :-1, :-1] + u0[5, :-1, 1:]) / 2) ** 2
+                            + ((u0[6, :-1, :-1] + u0[6, 1:, :-1]) / 2) ** 2))
+    U[1, 0] = e
     return ini, U
 
 

@@ -98,7 +98,7 @@ ek_status ek_params_from_ini(const char * text, size_t len, ek_params * out);
 
 /* Create a solver on the current CUDA device.  Replaces
  * SolverFactory::Instance().create(name, params, configMap)
- * (SolverFactory.h:83-116) for the names Hydro_Muscl_2D/3D, MHD_Muscl_3D;
+ * (SolverFactory.h:83-116) for the names Hydro_Muscl_2D/3D, MHD_Muscl_2D/3D;
  * the initial condition is not computed here but injected with
  * ek_solver_set_state (the reference's init(U) becomes the caller's). */
 ek_status ek_solver_create(const ek_params * params, ek_solver ** out);

@@ -1439,6 +1439,338 @@ mhd3d_godunov(eko_solver * s, double * in, double * out)
 }
 
 /* ===================================================================== */
+/* MHD 2D                                                                 */
+/* ===================================================================== */
+
+/* ConvertToPrimitivesFunctor2D_MHD: MHDRunFunctors2D.h:85-160 (i,j < size-1).
+ * The z neighbour field is 0 (MHDRunFunctors2D.h:133), so the cell-centred Bz
+ * is half the stored value. */
+static void
+mhd2d_convert_prims(eko_solver * s, const double * U)
+{
+  const eko_params * p = &s->p;
+  const int is = p->isize, js = p->jsize;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < js - 1; ++j)
+    for (int i = 0; i < is - 1; ++i)
+    {
+      long   c = IDX(s, i, j, 0);
+      double u[8], q[8], bnb[3];
+      for (int v = 0; v < 8; ++v)
+        u[v] = AT(U, s, v, c);
+      bnb[0] = AT(U, s, EKO_IA, c + 1);
+      bnb[1] = AT(U, s, EKO_IB, c + is);
+      bnb[2] = 0.0;
+      mhd_constoprim(u, bnb, q, p);
+      for (int v = 0; v < 8; ++v)
+        AT(s->Q, s, v, c) = q[v];
+    }
+}
+
+/* ComputeDtFunctor2D_MHD: MHDRunFunctors2D.h:16-80, find_speed_info<TWO_D>
+ * (mhd_utils.h:319-366) */
+static double
+mhd2d_compute_dt_local(eko_solver * s)
+{
+  const eko_params * p = &s->p;
+  const int gw = p->gw;
+  double    invDt = -DBL_MAX;
+#pragma omp parallel
+  {
+    double local = -DBL_MAX;
+#pragma omp for schedule(static)
+    for (int j = gw; j < p->jsize - gw; ++j)
+      for (int i = gw; i < p->isize - gw; ++i)
+      {
+        long   c = IDX(s, i, j, 0);
+        double q[8], f[3];
+        for (int v = 0; v < 8; ++v)
+          q[v] = AT(s->Q, s, v, c);
+        speed_info3(q, f, p->gamma0);
+        local = fmax(local, f[0] / p->dx + f[1] / p->dy);
+      }
+#pragma omp critical
+    invDt = local > invDt ? local : invDt;
+  }
+  return p->cfl / invDt;
+}
+
+/* slope_unsplit_mhd_2d: MHDBaseFunctor2D.h:455-518.  bfn = bfx, bfx_yplus,
+ * bfx_yminus, bfy, bfy_xplus, bfy_xminus; returns dbfY[IX] and dbfX[IY]. */
+static void
+mhd2d_bslopes(const double * bfn, double st, double * dbfy_x, double * dbfx_y)
+{
+  *dbfy_x = slope1(bfn[0], bfn[1], bfn[2], st);
+  *dbfx_y = slope1(bfn[3], bfn[4], bfn[5], st);
+}
+
+/* trace_unsplit_mhd_2d: MHDBaseFunctor2D.h:775-1114.  qNb: primitive states
+ * of the 3x3 neighbourhood, bfNb: face fields of the 4x4 neighbourhood (the
+ * cell at [1][1]); qE in the order RT, RB, LT, LB. */
+static void
+mhd_trace2d(double qNb[3][3][8], double bfNb[4][4][3], double dtdx, double dtdy, double qm[2][8],
+            double qp[2][8], double qE[4][8], const eko_params * p)
+{
+  const double smallR = p->smallr, smallp = p->smallp, gamma = p->gamma0, st = p->slope_type;
+  double       Ez[2][2];
+  for (int di = 0; di < 2; di++)
+    for (int dj = 0; dj < 2; dj++)
+    {
+      int    cx = 1 + di, cy = 1 + dj;
+      double u = 0.25 * (qNb[cx - 1][cy - 1][EKO_IU] + qNb[cx - 1][cy][EKO_IU] + qNb[cx][cy - 1][EKO_IU] +
+                         qNb[cx][cy][EKO_IU]);
+      double v = 0.25 * (qNb[cx - 1][cy - 1][EKO_IV] + qNb[cx - 1][cy][EKO_IV] + qNb[cx][cy - 1][EKO_IV] +
+                         qNb[cx][cy][EKO_IV]);
+      double A = 0.5 * (bfNb[cx][cy - 1][0] + bfNb[cx][cy][0]);
+      double B = 0.5 * (bfNb[cx - 1][cy][1] + bfNb[cx][cy][1]);
+      Ez[di][dj] = u * B - v * A;
+    }
+  const double ELL = Ez[0][0], ELR = Ez[0][1], ERL = Ez[1][0], ERR = Ez[1][1];
+  const double * q = qNb[1][1];
+  double r = q[EKO_ID], pp = q[EKO_IP], u = q[EKO_IU], v = q[EKO_IV], w = q[EKO_IW], A = q[EKO_IA],
+         B = q[EKO_IB], C = q[EKO_IC];
+  double AL = bfNb[1][1][0], AR = bfNb[2][1][0], BL = bfNb[1][1][1], BR = bfNb[1][2][1];
+
+  /* slope_unsplit_hydro_2d (MHDBaseFunctor2D.h:346-404), slope_type 1 or 2 */
+  double dq[2][8];
+  for (int var = 0; var < 8; ++var)
+  {
+    dq[0][var] = slope1(q[var], qNb[2][1][var], qNb[0][1][var], st);
+    dq[1][var] = slope1(q[var], qNb[1][2][var], qNb[1][0][var], st);
+  }
+  double drx = dq[0][EKO_ID] * 0.5, dpx = dq[0][EKO_IP] * 0.5, dux = dq[0][EKO_IU] * 0.5,
+         dvx = dq[0][EKO_IV] * 0.5, dwx = dq[0][EKO_IW] * 0.5, dCx = dq[0][EKO_IC] * 0.5,
+         dBx = dq[0][EKO_IB] * 0.5;
+  double dry = dq[1][EKO_ID] * 0.5, dpy = dq[1][EKO_IP] * 0.5, duy = dq[1][EKO_IU] * 0.5,
+         dvy = dq[1][EKO_IV] * 0.5, dwy = dq[1][EKO_IW] * 0.5, dCy = dq[1][EKO_IC] * 0.5,
+         dAy = dq[1][EKO_IA] * 0.5;
+
+  double bfn[6], dbfy_x, dbfx_y;
+  bfn[0] = bfNb[1][1][0], bfn[1] = bfNb[1][2][0], bfn[2] = bfNb[1][0][0];
+  bfn[3] = bfNb[1][1][1], bfn[4] = bfNb[2][1][1], bfn[5] = bfNb[0][1][1];
+  mhd2d_bslopes(bfn, st, &dbfy_x, &dbfx_y);
+  const double dALy = 0.5 * dbfy_x, dBLx = 0.5 * dbfx_y;
+  bfn[0] = bfNb[2][1][0], bfn[1] = bfNb[2][2][0], bfn[2] = bfNb[2][0][0];
+  bfn[3] = bfNb[2][1][1], bfn[4] = bfNb[3][1][1], bfn[5] = bfNb[1][1][1];
+  mhd2d_bslopes(bfn, st, &dbfy_x, &dbfx_y);
+  const double dARy = 0.5 * dbfy_x;
+  bfn[0] = bfNb[1][2][0], bfn[1] = bfNb[1][3][0], bfn[2] = bfNb[1][1][0];
+  bfn[3] = bfNb[1][2][1], bfn[4] = bfNb[2][2][1], bfn[5] = bfNb[0][2][1];
+  mhd2d_bslopes(bfn, st, &dbfy_x, &dbfx_y);
+  const double dBRx = 0.5 * dbfx_y;
+
+  const double dAx = 0.5 * (AR - AL);
+  const double dBy = 0.5 * (BR - BL);
+
+  /* source terms (cartesian), MHDBaseFunctor2D.h:969-995 */
+  const double sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy;
+  const double su0 =
+    (-u * dux - dpx / r - B * dBx / r - C * dCx / r) * dtdx + (-v * duy + B * dAy / r) * dtdy;
+  const double sv0 =
+    (-u * dvx + A * dBx / r) * dtdx + (-v * dvy - dpy / r - A * dAy / r - C * dCy / r) * dtdy;
+  const double sw0 = (-u * dwx + A * dCx / r) * dtdx + (-v * dwy + B * dCy / r) * dtdy;
+  const double sp0 = (-u * dpx - dux * gamma * pp) * dtdx + (-v * dpy - dvy * gamma * pp) * dtdy;
+  const double sA0 = (u * dBy + B * duy - v * dAy - A * dvy) * dtdy;
+  const double sB0 = (-u * dBx - B * dux + v * dAx + A * dvx) * dtdx;
+  const double sC0 =
+    (w * dAx + A * dwx - u * dCx - C * dux) * dtdx + (-v * dCy - C * dvy + w * dBy + B * dwy) * dtdy;
+  const double sAL0 = +(ELR - ELL) * 0.5 * dtdy;
+  const double sAR0 = +(ERR - ERL) * 0.5 * dtdy;
+  const double sBL0 = -(ERL - ELL) * 0.5 * dtdx;
+  const double sBR0 = -(ERR - ELR) * 0.5 * dtdx;
+
+  r = r + sr0;
+  u = u + su0;
+  v = v + sv0;
+  w = w + sw0;
+  pp = pp + sp0;
+  A = A + sA0;
+  B = B + sB0;
+  C = C + sC0;
+  AL = AL + sAL0;
+  AR = AR + sAR0;
+  BL = BL + sBL0;
+  BR = BR + sBR0;
+
+#define EKO_FLOOR2(st_)                                                                            \
+  do                                                                                               \
+  {                                                                                                \
+    (st_)[EKO_ID] = fmax(smallR, (st_)[EKO_ID]);                                                   \
+    (st_)[EKO_IP] = fmax(smallp * (st_)[EKO_ID], (st_)[EKO_IP]);                                   \
+  } while (0)
+  qp[0][EKO_ID] = r - drx, qp[0][EKO_IU] = u - dux, qp[0][EKO_IV] = v - dvx, qp[0][EKO_IW] = w - dwx;
+  qp[0][EKO_IP] = pp - dpx, qp[0][EKO_IA] = AL, qp[0][EKO_IB] = B - dBx, qp[0][EKO_IC] = C - dCx;
+  EKO_FLOOR2(qp[0]);
+  qm[0][EKO_ID] = r + drx, qm[0][EKO_IU] = u + dux, qm[0][EKO_IV] = v + dvx, qm[0][EKO_IW] = w + dwx;
+  qm[0][EKO_IP] = pp + dpx, qm[0][EKO_IA] = AR, qm[0][EKO_IB] = B + dBx, qm[0][EKO_IC] = C + dCx;
+  EKO_FLOOR2(qm[0]);
+  qp[1][EKO_ID] = r - dry, qp[1][EKO_IU] = u - duy, qp[1][EKO_IV] = v - dvy, qp[1][EKO_IW] = w - dwy;
+  qp[1][EKO_IP] = pp - dpy, qp[1][EKO_IA] = A - dAy, qp[1][EKO_IB] = BL, qp[1][EKO_IC] = C - dCy;
+  EKO_FLOOR2(qp[1]);
+  qm[1][EKO_ID] = r + dry, qm[1][EKO_IU] = u + duy, qm[1][EKO_IV] = v + dvy, qm[1][EKO_IW] = w + dwy;
+  qm[1][EKO_IP] = pp + dpy, qm[1][EKO_IA] = A + dAy, qm[1][EKO_IB] = BR, qm[1][EKO_IC] = C + dCy;
+  EKO_FLOOR2(qm[1]);
+
+  double * qRT = qE[0];
+  double * qRB = qE[1];
+  double * qLT = qE[2];
+  double * qLB = qE[3];
+  qRT[EKO_ID] = r + (+drx + dry), qRT[EKO_IU] = u + (+dux + duy), qRT[EKO_IV] = v + (+dvx + dvy);
+  qRT[EKO_IW] = w + (+dwx + dwy), qRT[EKO_IP] = pp + (+dpx + dpy), qRT[EKO_IA] = AR + (+dARy);
+  qRT[EKO_IB] = BR + (+dBRx), qRT[EKO_IC] = C + (+dCx + dCy);
+  EKO_FLOOR2(qRT);
+  qRB[EKO_ID] = r + (+drx - dry), qRB[EKO_IU] = u + (+dux - duy), qRB[EKO_IV] = v + (+dvx - dvy);
+  qRB[EKO_IW] = w + (+dwx - dwy), qRB[EKO_IP] = pp + (+dpx - dpy), qRB[EKO_IA] = AR + (-dARy);
+  qRB[EKO_IB] = BL + (+dBLx), qRB[EKO_IC] = C + (+dCx - dCy);
+  EKO_FLOOR2(qRB);
+  qLB[EKO_ID] = r + (-drx - dry), qLB[EKO_IU] = u + (-dux - duy), qLB[EKO_IV] = v + (-dvx - dvy);
+  qLB[EKO_IW] = w + (-dwx - dwy), qLB[EKO_IP] = pp + (-dpx - dpy), qLB[EKO_IA] = AL + (-dALy);
+  qLB[EKO_IB] = BL + (-dBLx), qLB[EKO_IC] = C + (-dCx - dCy);
+  EKO_FLOOR2(qLB);
+  qLT[EKO_ID] = r + (-drx + dry), qLT[EKO_IU] = u + (-dux + duy), qLT[EKO_IV] = v + (-dvx + dvy);
+  qLT[EKO_IW] = w + (-dwx + dwy), qLT[EKO_IP] = pp + (-dpx + dpy), qLT[EKO_IA] = AL + (+dALy);
+  qLT[EKO_IB] = BR + (-dBRx), qLT[EKO_IC] = C + (-dCx + dCy);
+  EKO_FLOOR2(qLT);
+#undef EKO_FLOOR2
+}
+
+/* godunov_unsplit_impl v0 for MHD 2D: SolverMHDMuscl.cpp:369-420 */
+static void
+mhd2d_godunov(eko_solver * s, double * in, double * out)
+{
+  const eko_params * p = &s->p;
+  const int is = p->isize, js = p->jsize, gw = p->gw;
+  const long sy = is;
+  const long ncell = s->ncell;
+
+  make_boundaries(s, in);
+  memcpy(out, in, sizeof(double) * ncell * 8);
+  mhd2d_convert_prims(s, in);
+  s->dt = mhd2d_compute_dt_local(s);
+  if (s->t + s->dt > p->tEnd)
+    s->dt = p->tEnd - s->t;
+  const double dt = s->dt;
+  const double dtdx = dt / p->dx, dtdy = dt / p->dy;
+
+  /* ComputeTraceFunctor2D_MHD: MHDRunFunctors2D.h:782-918 */
+#pragma omp parallel for schedule(static)
+  for (int j = gw - 2; j < js - gw + 1; ++j)
+    for (int i = gw - 2; i < is - gw + 1; ++i)
+    {
+      double qNb[3][3][8], bfNb[4][4][3], qm[2][8], qp[2][8], qE[4][8];
+      for (int di = 0; di < 3; ++di)
+        for (int dj = 0; dj < 3; ++dj)
+        {
+          long c = IDX(s, i + di - 1, j + dj - 1, 0);
+          for (int v = 0; v < 8; ++v)
+            qNb[di][dj][v] = AT(s->Q, s, v, c);
+        }
+      for (int di = 0; di < 4; ++di)
+        for (int dj = 0; dj < 4; ++dj)
+        {
+          long c = IDX(s, i + di - 1, j + dj - 1, 0);
+          bfNb[di][dj][0] = AT(in, s, EKO_IA, c);
+          bfNb[di][dj][1] = AT(in, s, EKO_IB, c);
+          bfNb[di][dj][2] = AT(in, s, EKO_IC, c);
+        }
+      mhd_trace2d(qNb, bfNb, dtdx, dtdy, qm, qp, qE, p);
+      long c = IDX(s, i, j, 0);
+      for (int v = 0; v < 8; ++v)
+      {
+        AT(s->Qm[0], s, v, c) = qm[0][v];
+        AT(s->Qp[0], s, v, c) = qp[0][v];
+        AT(s->Qm[1], s, v, c) = qm[1][v];
+        AT(s->Qp[1], s, v, c) = qp[1][v];
+        for (int e = 0; e < 4; ++e)
+          AT(s->QE[e][0], s, v, c) = qE[e][v];
+      }
+    }
+
+  /* ComputeFluxesAndStoreFunctor2D_MHD (MHDRunFunctors2D.h:375-470) and
+   * ComputeEmfAndStoreFunctor2D (MHDRunFunctors2D.h:612-686) */
+#pragma omp parallel for schedule(static)
+  for (int j = gw; j < js - gw + 1; ++j)
+    for (int i = gw; i < is - gw + 1; ++i)
+    {
+      long   c = IDX(s, i, j, 0);
+      double ql[8], qr[8], flux[8], x;
+      for (int v = 0; v < 8; ++v)
+      {
+        ql[v] = AT(s->Qm[0], s, v, c - 1);
+        qr[v] = AT(s->Qp[0], s, v, c);
+      }
+      hlld(ql, qr, flux, p);
+      for (int v = 0; v < 8; ++v)
+        AT(s->Fx, s, v, c) = flux[v];
+      for (int v = 0; v < 8; ++v)
+      {
+        ql[v] = AT(s->Qm[1], s, v, c - sy);
+        qr[v] = AT(s->Qp[1], s, v, c);
+      }
+      x = ql[EKO_IU], ql[EKO_IU] = ql[EKO_IV], ql[EKO_IV] = x;
+      x = ql[EKO_IA], ql[EKO_IA] = ql[EKO_IB], ql[EKO_IB] = x;
+      x = qr[EKO_IU], qr[EKO_IU] = qr[EKO_IV], qr[EKO_IV] = x;
+      x = qr[EKO_IA], qr[EKO_IA] = qr[EKO_IB], qr[EKO_IB] = x;
+      hlld(ql, qr, flux, p);
+      for (int v = 0; v < 8; ++v)
+        AT(s->Fy, s, v, c) = flux[v];
+
+      double a[8], b[8], cc[8], d[8];
+      for (int v = 0; v < 8; ++v)
+      {
+        a[v] = AT(s->QE[0][0], s, v, c - 1 - sy);
+        b[v] = AT(s->QE[1][0], s, v, c - 1);
+        cc[v] = AT(s->QE[2][0], s, v, c - sy);
+        d[v] = AT(s->QE[3][0], s, v, c);
+      }
+      AT(s->Emf, s, 0, c) = compute_emf(a, b, cc, d, 2, p);
+    }
+
+  /* UpdateFunctor2D_MHD (MHDRunFunctors2D.h:1539-1641) then UpdateEmfFunctor2D
+   * (MHDRunFunctors2D.h:1646-1700) */
+#pragma omp parallel for schedule(static)
+  for (int j = gw; j < js - gw; ++j)
+    for (int i = gw; i < is - gw; ++i)
+    {
+      long           c = IDX(s, i, j, 0);
+      const double * Fx = s->Fx;
+      const double * Fy = s->Fy;
+      double         ud[8];
+      for (int v = 0; v < 8; ++v)
+        ud[v] = AT(out, s, v, c);
+      ud[EKO_ID] += AT(Fx, s, EKO_ID, c) * dtdx;
+      ud[EKO_IP] += AT(Fx, s, EKO_IP, c) * dtdx;
+      ud[EKO_IU] += AT(Fx, s, EKO_IU, c) * dtdx;
+      ud[EKO_IV] += AT(Fx, s, EKO_IV, c) * dtdx;
+      ud[EKO_IW] += AT(Fx, s, EKO_IW, c) * dtdx;
+      ud[EKO_IC] += AT(Fx, s, EKO_IC, c) * dtdx;
+      ud[EKO_ID] -= AT(Fx, s, EKO_ID, c + 1) * dtdx;
+      ud[EKO_IP] -= AT(Fx, s, EKO_IP, c + 1) * dtdx;
+      ud[EKO_IU] -= AT(Fx, s, EKO_IU, c + 1) * dtdx;
+      ud[EKO_IV] -= AT(Fx, s, EKO_IV, c + 1) * dtdx;
+      ud[EKO_IW] -= AT(Fx, s, EKO_IW, c + 1) * dtdx;
+      ud[EKO_IC] -= AT(Fx, s, EKO_IC, c + 1) * dtdx;
+      ud[EKO_ID] += AT(Fy, s, EKO_ID, c) * dtdy;
+      ud[EKO_IP] += AT(Fy, s, EKO_IP, c) * dtdy;
+      ud[EKO_IU] += AT(Fy, s, EKO_IV, c) * dtdy;
+      ud[EKO_IV] += AT(Fy, s, EKO_IU, c) * dtdy;
+      ud[EKO_IW] += AT(Fy, s, EKO_IW, c) * dtdy;
+      ud[EKO_IC] += AT(Fy, s, EKO_IC, c) * dtdy;
+      ud[EKO_ID] -= AT(Fy, s, EKO_ID, c + sy) * dtdy;
+      ud[EKO_IP] -= AT(Fy, s, EKO_IP, c + sy) * dtdy;
+      ud[EKO_IU] -= AT(Fy, s, EKO_IV, c + sy) * dtdy;
+      ud[EKO_IV] -= AT(Fy, s, EKO_IU, c + sy) * dtdy;
+      ud[EKO_IW] -= AT(Fy, s, EKO_IW, c + sy) * dtdy;
+      ud[EKO_IC] -= AT(Fy, s, EKO_IC, c + sy) * dtdy;
+      const double * Emf = s->Emf;
+      ud[EKO_IA] += (AT(Emf, s, 0, c + sy) - AT(Emf, s, 0, c)) * dtdy;
+      ud[EKO_IB] -= (AT(Emf, s, 0, c + 1) - AT(Emf, s, 0, c)) * dtdx;
+      for (int v = 0; v < 8; ++v)
+        AT(out, s, v, c) = ud[v];
+    }
+}
+
+/* ===================================================================== */
 /* driver                                                                 */
 /* ===================================================================== */
 
@@ -1453,8 +1785,6 @@ eko_create(const eko_params * p, const double * U0, double t0)
 {
   if (!p || !U0)
     return NULL;
-  if (p->dim == 2 && p->mhd)
-    return NULL; /* MHD 2D is not restated here */
   eko_solver * s = (eko_solver *)calloc(1, sizeof(eko_solver));
   s->p = *p;
   s->ncell = eko_ncells(p);
@@ -1498,7 +1828,12 @@ eko_create(const eko_params * p, const double * U0, double t0)
   /* constructor tail */
   make_boundaries(s, s->U);
   memcpy(s->U2, s->U, sizeof(double) * n * nb);
-  if (p->mhd)
+  if (p->mhd && p->dim == 2)
+  {
+    mhd2d_convert_prims(s, s->U);
+    s->dt = mhd2d_compute_dt_local(s);
+  }
+  else if (p->mhd)
   {
     mhd_convert_prims(s, s->U);
     s->dt = mhd_compute_dt_local(s);
@@ -1556,7 +1891,10 @@ eko_next_iteration(eko_solver * s)
   else
   {
     /* SolverMHDMuscl::next_iteration_impl (SolverMHDMuscl.h:741-780) */
-    mhd3d_godunov(s, in, out);
+    if (s->p.dim == 2)
+      mhd2d_godunov(s, in, out);
+    else
+      mhd3d_godunov(s, in, out);
   }
   s->iteration += 1;
   s->t += s->dt;

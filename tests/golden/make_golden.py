@@ -7,11 +7,13 @@ Stored per case (compressed .npz): the .ini text, the injected initial state
 U0, the final state U, the dt sequence and the final time.
 
 Run from the repository root (needs the reference sources, so only where
-they are present):  python tests/golden/make_golden.py
+they are present):  python tests/golden/make_golden.py [case ...]
+(no case names: every case)
 """
 
 import os
 import sys
+import tempfile
 
 import numpy as np
 
@@ -44,13 +46,25 @@ CASES = {
                                                       bc=(2, 2, 2, 2, 2, 2), slope_type=2.0,
                                                       nsteps=4), 4),
     "mhdblast3d_10_nan": (lambda: P.mhd_blast_3d(n=10, nsteps=3), 3),
+    "ot2d_24": (lambda: P.orszag_tang_2d(n=24, nsteps=8), 8),
+    "ot2d_noise_20x16": (lambda: P.orszag_tang_2d(n=20, ny=16, nsteps=6, vz_noise=1e-2), 6),
+    "mhd2d_random_periodic": (lambda: P.smooth_random(dim=2, mhd=True, nx=20, ny=14, seed=8,
+                                                       slope_type=2.0, nsteps=6), 6),
+    "mhd2d_random_reflect_minmod": (lambda: P.smooth_random(dim=2, mhd=True, nx=16, ny=12, seed=9,
+                                                             bc=(1, 1, 1, 1, 1, 1), slope_type=1.0,
+                                                             nsteps=6), 6),
+    "mhd2d_random_mixedbc": (lambda: P.smooth_random(dim=2, mhd=True, nx=18, ny=16, seed=10,
+                                                      bc=(2, 2, 3, 3, 1, 1), slope_type=2.0,
+                                                      nsteps=6), 6),
 }
 
 
 def main():
     out_dir = os.path.dirname(os.path.abspath(__file__))
-    work = os.path.join(ROOT, "_work", "golden_tmp")
-    for name, (build, nsteps) in CASES.items():
+    work = tempfile.mkdtemp(prefix="ek_golden_")
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        build, nsteps = CASES[name]
         ini, U0 = build()
         res = eko.run_reference(ini, U0, nsteps, os.path.join(work, name))
         np.savez_compressed(os.path.join(out_dir, name + ".npz"), ini=np.array(ini), U0=U0,

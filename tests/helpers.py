@@ -9,12 +9,15 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def golden_cases(kind=None):
-    """Names of the golden fixtures; kind: 'hydro', 'mhd' or None."""
+    """Names of the golden fixtures; kind: 'hydro', 'mhd' (3D), 'mhd2d' or None."""
     names = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    is_mhd = [n.startswith("mhd") or n.startswith("ot") for n in names]
     if kind == "hydro":
-        return [n for n in names if not n.startswith("mhd") and not n.startswith("ot")]
+        return [n for n, m in zip(names, is_mhd) if not m]
     if kind == "mhd":
-        return [n for n in names if n.startswith("mhd") or n.startswith("ot")]
+        return [n for n, m in zip(names, is_mhd) if m and "2d" not in n]
+    if kind == "mhd2d":
+        return [n for n, m in zip(names, is_mhd) if m and "2d" in n]
     return names
 
 
