@@ -213,18 +213,20 @@ def ensure_oracle():
                        stdout=subprocess.DEVNULL)
 
 
-def cpu_sample(args, seconds=15.0):
-    """Oracle on a bounded sample of the headline workload (a smaller grid of
-    the same problem), sized for roughly `seconds` of CPU work."""
+def cpu_sample(args, seconds=12.0):
+    """Oracle on a bounded sample of the headline workload: the same problem on
+    the headline grid when the host can do at least 3 steps of it in about
+    `seconds`, else on a smaller grid, with as many steps as fit."""
     from euler_kokkos_gb300 import problems as P
 
     ensure_oracle()
-    probe_n = 48
+    probe_n = 64
     ini, U0 = P.blast_3d(n=probe_n, nsteps=2)
     r, _, _ = oracle_rate(ini, U0, 2)
-    # choose a grid and a step count worth ~seconds of work at the probed rate
-    n = 128 if r * 1e6 * seconds / (128 ** 3) >= 3 else 96
-    steps = max(2, min(20, int(r * 1e6 * seconds / n ** 3)))
+    n = args.n
+    while n > 64 and r * 1e6 * seconds / n ** 3 < 3:
+        n //= 2
+    steps = max(3, min(50, int(r * 1e6 * seconds / n ** 3)))
     ini, U0 = P.blast_3d(n=n, nsteps=steps)
     rate, dt, cores = oracle_rate(ini, U0, steps)
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
@@ -267,17 +269,28 @@ def ensemble_workload(ek, P, args, sync, maxt, world):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import eko
 
+        # every instance, one after another (one problem per run, as the
+        # reference), as many steps each as fit in about 10 s
         t0 = time.perf_counter()
         done_cells = 0
-        for ini, U0 in cases[:8]:
+        nsamp = 2
+        for ini, U0 in cases:
             p = eko.params_from_ini(ini)
             o = eko.Oracle(p, U0)
-            n = len(o.run(10))
-            done_cells += p.nx * p.ny * n
+            done_cells += p.nx * p.ny * len(o.run(nsamp))
+            o.close()
+        probe = time.perf_counter() - t0
+        nsamp = max(2, min(args.ens_steps, int(2 * 10.0 / max(probe, 1e-3))))
+        t0 = time.perf_counter()
+        done_cells = 0
+        for ini, U0 in cases:
+            p = eko.params_from_ini(ini)
+            o = eko.Oracle(p, U0)
+            done_cells += p.nx * p.ny * len(o.run(nsamp))
             o.close()
         dt = time.perf_counter() - t0
         cpu = {"value": done_cells / dt / 1e6, "unit": UNIT, "cores": eko.num_threads(), "kind": "port",
-               "sample": "first 8 instances x 10 steps, one after another (%.1f s)" % dt}
+               "sample": "all %d instances x %d steps, one after another (%.1f s)" % (len(cases), nsamp, dt)}
     return {
         "value": value, "unit": UNIT, "dtype": "f32", "instances": len(cases), "interior_cells": cells,
         "steps": args.ens_steps, "ms_per_step": ms / args.ens_steps, "tiles_per_step": info["tiles"],

@@ -285,6 +285,19 @@ flips(const SrcCell & s, int v, int mhd)
   return f;
 }
 
+// x or -x; the sign of a double is flipped with an integer XOR so that no
+// FP64 instruction is issued (the result equals the FP64 negation bit for bit)
+__device__ __forceinline__ double
+neg_if(double x, bool f)
+{
+  return __longlong_as_double(__double_as_longlong(x) ^ (f ? (long long)0x8000000000000000ull : 0ll));
+}
+__device__ __forceinline__ float
+neg_if(float x, bool f)
+{
+  return f ? -x : x;
+}
+
 template <class T>
 __device__ __forceinline__ T
 ldg(const T * p)
@@ -337,6 +350,31 @@ step_scalars(const KParams & P, const DevClock * clk, int step, StepScalars<R> *
   }
   __syncthreads();
   return sh->active != 0;
+}
+
+// Visit the interior cells of a state row by row: a block takes whole rows
+// (j, k) with a grid stride and its threads take the cells of a row, so the
+// index math needs one 32-bit division per row (a per-cell 64-bit division is
+// a long software sequence).  f(i, j, k) gets ghost-inclusive indices.
+template <class F>
+__device__ __forceinline__ void
+for_interior_rows(const KParams & P, F && f)
+{
+  const int nrows = P.ny * (P.ksize > 1 ? P.nz : 1);
+  for (int row = blockIdx.x; row < nrows; row += gridDim.x)
+  {
+    const int j = row % P.ny + P.gw;
+    const int k = P.ksize > 1 ? row / P.ny + P.gw : 0;
+    for (int i = threadIdx.x + P.gw; i < P.nx + P.gw; i += blockDim.x)
+      f(i, j, k);
+  }
+}
+// blocks for a row-wise pass over the interior
+__host__ __device__ inline int
+row_blocks(const KParams & P)
+{
+  const long long nrows = (long long)P.ny * (P.ksize > 1 ? P.nz : 1);
+  return (int)(nrows < 8192 ? nrows : 8192);
 }
 
 // bookkeeping done once per step by block 0, thread 0

@@ -66,8 +66,7 @@ load_q_plane(const S * __restrict__ U, const KParams & P, const HydroConst<R> & 
 #pragma unroll
       for (int v = 0; v < NV; ++v)
       {
-        R x = (R)ldg(U + v * P.vstride + s.off);
-        u[v] = flips(s, v, 0) ? -x : x;
+        u[v] = neg_if((R)ldg(U + v * P.vstride + s.off), flips(s, v, 0));
       }
     }
     hydro_prims<R, NV>(u, q, C);
@@ -312,15 +311,12 @@ ensemble_totals_kernel(const EnsInstance * __restrict__ insts, const int * __res
   const EnsInstance & in = insts[blockIdx.y];
   const KParams &     P = in.P;
   const S *           U = (const S *)in.U[*stepc % 2];
-  const long long     n = (long long)P.nx * P.ny;
   double              m = 0.0, e = 0.0;
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-       c += (long long)gridDim.x * blockDim.x)
-  {
-    const long long off = (long long)(c / P.nx + P.gw) * P.isize + (c % P.nx + P.gw);
+  for_interior_rows(P, [&](int i, int j, int) {
+    const long long off = (long long)j * P.isize + i;
     m += (double)U[off];
     e += (double)U[P.vstride + off];
-  }
+  });
   for (int o = 16; o > 0; o >>= 1)
   {
     m += __shfl_xor_sync(0xffffffffu, m, o);
@@ -577,23 +573,15 @@ __global__ void
 hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
 {
   const HydroConst<R> C = hydro_const<R>(P);
-  const long long     n = (long long)P.nx * P.ny * (NV == 5 ? P.nz : 1);
   R                   tmax = R(-INFINITY);
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-       c += (long long)gridDim.x * blockDim.x)
-  {
-    const int       i = (int)(c % P.nx);
-    const long long r = c / P.nx;
-    const int       j = (int)(r % P.ny);
-    const int       k = (int)(r / P.ny);
-    const long long off = (long long)(k + (NV == 5 ? P.gw : 0)) * P.plane +
-                          (long long)(j + P.gw) * P.isize + (i + P.gw);
-    R u[NV];
+  for_interior_rows(P, [&](int i, int j, int k) {
+    const long long off = (long long)k * P.plane + (long long)j * P.isize + i;
+    R               u[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       u[v] = (R)ldg(U + v * P.vstride + off);
     tmax = fmax(tmax, hydro_invdt<R, NV>(u, C, P));
-  }
+  });
   block_max_commit<256>(cand_key((double)tmax), key);
 }
 

@@ -60,8 +60,7 @@ template <class S, class R>
 cudaError_t
 hydro_dt_t(int dim, const void * U, const KParams & P, unsigned long long * key, cudaStream_t st)
 {
-  const long long n = (long long)P.nx * P.ny * (dim == 3 ? P.nz : 1);
-  const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  const int blocks = row_blocks(P);
   if (dim == 2)
     hydro_dt_kernel<S, R, 4><<<blocks, 256, 0, st>>>((const S *)U, P, key);
   else
@@ -167,19 +166,12 @@ __global__ void
 totals_kernel(const S * __restrict__ U, KParams P, double * acc)
 {
   // FP64 mass and total energy over the interior; max |div B| for MHD
-  const long long n = (long long)P.nx * P.ny * (P.ksize > 1 ? P.nz : 1);
-  double          m = 0.0, e = 0.0, db = 0.0;
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-       c += (long long)gridDim.x * blockDim.x)
-  {
-    const int       i = (int)(c % P.nx) + P.gw;
-    const long long r = c / P.nx;
-    const int       j = (int)(r % P.ny) + P.gw;
-    const int       k = (int)(r / P.ny) + (P.ksize > 1 ? P.gw : 0);
+  double m = 0.0, e = 0.0, db = 0.0;
+  for_interior_rows(P, [&](int i, int j, int k) {
     const long long off = (long long)k * P.plane + (long long)j * P.isize + i;
     m += (double)U[off];
     e += (double)U[P.vstride + off];
-  }
+  });
   for (int o = 16; o > 0; o >>= 1)
   {
     m += __shfl_xor_sync(0xffffffffu, m, o);
@@ -234,8 +226,7 @@ totals(int prec, const void * U, const KParams & P, int nbvar, double * out3, cu
   cudaError_t e = cudaMemsetAsync(out3, 0, 3 * sizeof(double), st);
   if (e != cudaSuccess)
     return e;
-  const long long n = (long long)P.nx * P.ny * (P.ksize > 1 ? P.nz : 1);
-  const int       blocks = (int)((n + 255) / 256 < 2048 ? (n + 255) / 256 : 2048);
+  const int blocks = row_blocks(P);
   if (prec == 0)
     totals_kernel<double><<<blocks, 256, 0, st>>>((const double *)U, P, out3);
   else

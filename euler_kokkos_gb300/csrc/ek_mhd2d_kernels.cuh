@@ -122,13 +122,8 @@ mhd2d_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step
   }
   const MhdState<S> m = mhd_state<S>(U, P);
   const MhdConst<R> C = mhd_const<R>(P);
-  const long long   n = (long long)P.nx * P.ny;
   R                 tmax = R(-INFINITY);
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-       c += (long long)gridDim.x * blockDim.x)
-  {
-    const int     i = (int)(c % P.nx) + P.gw;
-    const int     j = (int)(c / P.nx) + P.gw;
+  for_interior_rows(P, [&](int i, int j, int) {
     const SrcCell s = src_cell(P, i, j, 0);
     R             u[5];
     double        bz;
@@ -163,7 +158,7 @@ mhd2d_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step
       cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * b * b / d));
       tmax = fmax(tmax, (cfx + fabs(q[IU])) / P.dx + (cfy + fabs(q[IV])) / P.dy);
     }
-  }
+  });
   block_max_commit<256>(cand_key((double)tmax), key ? key : &clk->key[step % 3]);
 }
 
@@ -495,9 +490,7 @@ mhd2d_step_t(int phase, const void * Uin, void * Uout, const KParams & P, DevClo
 {
   if (phase == 0)
   {
-    const long long n = (long long)P.nx * P.ny;
-    const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
-    mhd2d_dt_kernel<S, R><<<blocks, 256, 0, st>>>(Uin, P, clk, step, nullptr);
+    mhd2d_dt_kernel<S, R><<<row_blocks(P), 256, 0, st>>>(Uin, P, clk, step, nullptr);
     return cudaGetLastError();
   }
   auto        k = mhd2d_step_kernel<S, R, M2_TX, M2_TY>;
@@ -529,8 +522,7 @@ mhd2d_step(int prec, int phase, const void * Uin, void * Uout, const KParams & P
 cudaError_t
 mhd2d_dt(int prec, const void * U, const KParams & P, unsigned long long * key, cudaStream_t st)
 {
-  const long long n = (long long)P.nx * P.ny;
-  const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  const int blocks = row_blocks(P);
 #ifdef EK_EXACT_ONLY
   if (prec != 0)
     return cudaErrorNotSupported;

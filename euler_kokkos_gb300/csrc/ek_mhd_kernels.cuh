@@ -70,16 +70,14 @@ load_hydro(const MhdState<S> & m, const KParams & P, const SrcCell & s, R (&u)[5
 #pragma unroll
   for (int v = 0; v < 5; ++v)
   {
-    const R x = (R)ldg(m.h + v * P.vstride + s.off);
-    u[v] = flips(s, v, 1) ? -x : x;
+    u[v] = neg_if((R)ldg(m.h + v * P.vstride + s.off), flips(s, v, 1));
   }
 }
 template <class S>
 __device__ __forceinline__ double
 load_face(const MhdState<S> & m, const KParams & P, const SrcCell & s, int comp)
 {
-  const double x = ldg(m.b + comp * P.vstride + s.off);
-  return flips(s, IA + comp, 1) ? -x : x;
+  return neg_if(ldg(m.b + comp * P.vstride + s.off), flips(s, IA + comp, 1));
 }
 
 // primitive state of cell (gi,gj,gk): constoprim with the face fields of the
@@ -133,19 +131,12 @@ mhd_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step,
   }
   const MhdState<S> m = mhd_state<S>(U, P);
   const MhdConst<R> C = mhd_const<R>(P);
-  const long long   n = (long long)P.nx * P.ny * P.nz;
   R                 tmax = R(-INFINITY);
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-       c += (long long)gridDim.x * blockDim.x)
-  {
-    const int       i = (int)(c % P.nx) + P.gw;
-    const long long r = c / P.nx;
-    const int       j = (int)(r % P.ny) + P.gw;
-    const int       k = (int)(r / P.ny) + P.gw;
-    R               q[8];
+  for_interior_rows(P, [&](int i, int j, int k) {
+    R q[8];
     cell_prims_global<S, R>(m, P, C, i, j, k, q);
     tmax = fmax(tmax, mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz, P.idx, P.idy, P.idz));
-  }
+  });
   block_max_commit<256>(cand_key((double)tmax), key ? key : &clk->key[step % 3]);
 }
 
@@ -502,7 +493,7 @@ struct UpdTile
 };
 
 template <class S, class R, int TX, int TY, bool STAGE>
-__global__ void __launch_bounds__(TX * TY)
+__global__ void __launch_bounds__(TX * TY, sizeof(R) == 4 ? 8 : 1)
 mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
                   KParams P, DevClock * clk, int step)
 {
@@ -733,15 +724,8 @@ __global__ void
 mhd_divb_kernel(const void * __restrict__ U, KParams P, unsigned long long * key)
 {
   const MhdState<S> m = mhd_state<S>(U, P);
-  const long long   n = (long long)P.nx * P.ny * P.nz;
   unsigned long long kmax = 0ull;
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-       c += (long long)gridDim.x * blockDim.x)
-  {
-    const int       i = (int)(c % P.nx) + P.gw;
-    const long long r = c / P.nx;
-    const int       j = (int)(r % P.ny) + P.gw;
-    const int       k = P.ksize > 1 ? (int)(r / P.ny) + P.gw : 0;
+  for_interior_rows(P, [&](int i, int j, int k) {
     const SrcCell   s0 = src_cell(P, i, j, k);
     double          d = (load_face<S>(m, P, src_cell(P, i + 1, j, k), 0) - load_face<S>(m, P, s0, 0)) / P.dx +
                      (load_face<S>(m, P, src_cell(P, i, j + 1, k), 1) - load_face<S>(m, P, s0, 1)) / P.dy;
@@ -750,7 +734,7 @@ mhd_divb_kernel(const void * __restrict__ U, KParams P, unsigned long long * key
       d += (load_face<S>(m, P, src_cell(P, i, j, k + 1), 2) - load_face<S>(m, P, s0, 2)) / P.dz;
     const unsigned long long kk = cand_key(fabs(d));
     kmax = kk > kmax ? kk : kmax;
-  }
+  });
   block_max_commit<256>(kmax, key);
 }
 
@@ -779,9 +763,7 @@ mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams 
   // 1. dt of this step into clock slot step % 3
   if (phase == 0)
   {
-    const long long n = (long long)P.nx * P.ny * P.nz;
-    const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
-    mhd_dt_kernel<S, R><<<blocks, 256, 0, st>>>(Uin, P, clk, step, nullptr);
+    mhd_dt_kernel<S, R><<<row_blocks(P), 256, 0, st>>>(Uin, P, clk, step, nullptr);
     return cudaGetLastError();
   }
   // 2. trace
@@ -829,8 +811,7 @@ mhd_step(int prec, int phase, const void * Uin, void * Uout, void * work, const 
 cudaError_t
 mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key, cudaStream_t st)
 {
-  const long long n = (long long)P.nx * P.ny * P.nz;
-  const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  const int blocks = row_blocks(P);
 #ifdef EK_EXACT_ONLY
   if (prec != 0)
     return cudaErrorNotSupported;
@@ -859,8 +840,7 @@ mhd_divb_max(int prec, const void * U, const KParams & P, double * out, cudaStre
   cudaError_t          e = cudaMemsetAsync(key, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess)
     return e;
-  const long long n = (long long)P.nx * P.ny * P.nz;
-  const int       blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  const int blocks = row_blocks(P);
   if (prec == 0)
     mhd_divb_kernel<double><<<blocks, 256, 0, st>>>(U, P, key);
   else
