@@ -141,6 +141,34 @@ dkey_inv(unsigned long long k)
 namespace EK_NS
 {
 using namespace ekc;
+// Minimum resident CTAs per SM requested from the register allocator for the
+// step kernels (FP32 / FP64 instantiations); overridable at build time.
+#ifndef EK_H3_MINB_F32
+#define EK_H3_MINB_F32 4
+#endif
+#ifndef EK_H3_MINB_F64
+#define EK_H3_MINB_F64 2
+#endif
+#ifndef EK_MT_MINB_F32
+#define EK_MT_MINB_F32 0
+#endif
+#ifndef EK_MT_MINB_F64
+#define EK_MT_MINB_F64 0
+#endif
+#ifndef EK_MU_MINB_F32
+#define EK_MU_MINB_F32 8
+#endif
+#ifndef EK_MU_MINB_F64
+#define EK_MU_MINB_F64 1
+#endif
+#ifndef EK_M2_MINB_F32
+#define EK_M2_MINB_F32 0
+#endif
+#ifndef EK_M2_MINB_F64
+#define EK_M2_MINB_F64 0
+#endif
+#define EK_MINB(R, F32, F64) (sizeof(R) == 4 ? (F32) : (F64))
+
 
 // FP64 <-> FP32 conversions on the integer pipes.  The hardware conversion
 // instructions run on the FP64 unit, which issues at 1/64 of the FP32 rate on

@@ -334,7 +334,7 @@ ensemble_totals_kernel(const EnsInstance * __restrict__ insts, const int * __res
 // 3D: one CTA = a TX x TY column of interior cells marching over kchunk planes
 // ---------------------------------------------------------------------------
 template <class S, class R, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY, sizeof(R) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_H3_MINB_F32, EK_H3_MINB_F64))
 hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
 {
   constexpr int NV = 5, HX = TX + 4, HY = TY + 4, NT = TX * TY;

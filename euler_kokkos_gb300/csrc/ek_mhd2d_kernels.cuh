@@ -295,7 +295,7 @@ trace2d_compact(const R * sQ, const R * sB, int qx, int qy, int bx, int by, R dt
 }
 
 template <class S, class R, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY)
+__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_M2_MINB_F32, EK_M2_MINB_F64))
 mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KParams P, DevClock * clk,
                   int step)
 {

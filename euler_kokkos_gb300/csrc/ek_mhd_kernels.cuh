@@ -327,7 +327,7 @@ trace_cell_compact(const R * sB, int bslot[4], const R * sQ, int qslot[3], const
 }
 
 template <class S, class R, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY)
+__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_MT_MINB_F32, EK_MT_MINB_F64))
 mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P, DevClock * clk,
                  int step)
 {
@@ -493,7 +493,7 @@ struct UpdTile
 };
 
 template <class S, class R, int TX, int TY, bool STAGE>
-__global__ void __launch_bounds__(TX * TY, sizeof(R) == 4 ? 8 : 1)
+__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_MU_MINB_F32, EK_MU_MINB_F64))
 mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
                   KParams P, DevClock * clk, int step)
 {
