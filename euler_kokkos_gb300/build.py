@@ -50,22 +50,34 @@ def _units():
     ]
 
 
+def _tuned_flags():
+    from euler_kokkos_gb300 import tuning
+
+    return tuning.load_flags()
+
+
 def up_to_date() -> bool:
     if not os.path.exists(LIB):
         return False
     t = os.path.getmtime(LIB)
     srcs = _sources() + [os.path.join(os.path.dirname(HERE), "include", "ek_gb300.h"), __file__]
+    tj = os.path.join(HERE, "tuning.json")
+    if os.path.exists(tj):
+        srcs.append(tj)
     return all(os.path.getmtime(s) <= t for s in srcs)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, tuned: bool = True) -> str:
+    """Compile and link the library; tuned: add the tile shapes and register
+    budgets chosen by euler_kokkos_gb300.tuning (tuning.json), if any."""
     if not force and up_to_date():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()
     procs = []
+    extra_common = _tuned_flags() if tuned else []
     for obj, src, extra in _units():
-        cmd = [nvcc, "-c", src, "-o", os.path.join(BUILD, obj)] + ARCH + COMMON + extra
+        cmd = [nvcc, "-c", src, "-o", os.path.join(BUILD, obj)] + ARCH + COMMON + extra_common + extra
         if verbose:
             print(" ".join(cmd), flush=True)
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

@@ -28,6 +28,11 @@ fail(ek_status s, const std::string & msg)
 }
 } // namespace ek_internal
 
+// planes per CTA column of the 3D kernels when the parameters leave it at 0
+#ifndef EK_KCHUNK_DEFAULT
+#define EK_KCHUNK_DEFAULT 32
+#endif
+
 using ek_internal::fail;
 using KParams = ekc::KParams;
 using DevClock = ekc::DevClock;
@@ -205,7 +210,7 @@ make_kparams(const ek_params & p)
   k.tEnd = p.tEnd;
   k.cIso = p.cIso;
   k.riemann = p.riemann;
-  k.kchunk = p.kchunk > 0 ? p.kchunk : (k.nz <= 32 ? k.nz : 32);
+  k.kchunk = p.kchunk > 0 ? p.kchunk : (k.nz <= EK_KCHUNK_DEFAULT ? k.nz : EK_KCHUNK_DEFAULT);
   k.gamma0f = (float)p.gamma0;
   k.smallrf = (float)p.smallr;
   k.smallcf = (float)p.smallc;
@@ -933,8 +938,8 @@ ek_ensemble_create(const ek_params * params, int n, ek_ensemble ** out)
       h_insts[i].U[0] = v->U[0];
       h_insts[i].U[1] = v->U[1];
       h_insts[i].clk = v->clk;
-      // 32 x 8 tiles of the 2D step kernel, instance-major
-      const int tx = (params[i].nx + 31) / 32, ty = (params[i].ny + 7) / 8;
+      // tiles of the 2D step kernel, instance-major
+      const int tx = (params[i].nx + EK_H2_TX - 1) / EK_H2_TX, ty = (params[i].ny + EK_H2_TY - 1) / EK_H2_TY;
       for (int by = 0; by < ty; ++by)
         for (int bx = 0; bx < tx; ++bx)
           tiles.push_back({ i, bx, by });

@@ -168,6 +168,38 @@ using namespace ekc;
 #define EK_M2_MINB_F64 0
 #endif
 #define EK_MINB(R, F32, F64) (sizeof(R) == 4 ? (F32) : (F64))
+// Tile shapes (output cells per CTA in x, y) of the step kernels; the
+// defaults are the measured best, euler_kokkos_gb300/tuning.py re-tunes them.
+#ifndef EK_H2_TX
+#define EK_H2_TX 32
+#endif
+#ifndef EK_H2_TY
+#define EK_H2_TY 8
+#endif
+#ifndef EK_H3_TX
+#define EK_H3_TX 32
+#endif
+#ifndef EK_H3_TY
+#define EK_H3_TY 8
+#endif
+#ifndef EK_MT_TX
+#define EK_MT_TX 32
+#endif
+#ifndef EK_MT_TY
+#define EK_MT_TY 4
+#endif
+#ifndef EK_MU_TX
+#define EK_MU_TX 16
+#endif
+#ifndef EK_MU_TY
+#define EK_MU_TY 8
+#endif
+#ifndef EK_M2_TX
+#define EK_M2_TX 16
+#endif
+#ifndef EK_M2_TY
+#define EK_M2_TY 8
+#endif
 
 
 // FP64 <-> FP32 conversions on the integer pipes.  The hardware conversion

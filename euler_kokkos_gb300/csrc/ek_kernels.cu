@@ -11,8 +11,8 @@ namespace EK_NS
 
 namespace
 {
-constexpr int H2_TX = 32, H2_TY = 8;
-constexpr int H3_TX = 32, H3_TY = 8;
+constexpr int H2_TX = EK_H2_TX, H2_TY = EK_H2_TY;
+constexpr int H3_TX = EK_H3_TX, H3_TY = EK_H3_TY;
 
 template <class R>
 constexpr size_t

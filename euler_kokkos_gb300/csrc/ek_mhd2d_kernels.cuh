@@ -481,7 +481,7 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
     step_commit(clk, step, t, dt);
 }
 
-constexpr int M2_TX = 16, M2_TY = 8;
+constexpr int M2_TX = EK_M2_TX, M2_TY = EK_M2_TY;
 
 template <class S, class R>
 cudaError_t

@@ -752,8 +752,8 @@ mhd_update_smem(int TX, int TY, bool stage)
                       2 * (TX + 1) * (TY + 1) + 2 * (TX + 1) * TY + 2 * TX * (TY + 1));
 }
 
-constexpr int MT_TX = 32, MT_TY = 4; // trace tile
-constexpr int MU_TX = 16, MU_TY = 8; // update tile
+constexpr int MT_TX = EK_MT_TX, MT_TY = EK_MT_TY; // trace tile
+constexpr int MU_TX = EK_MU_TX, MU_TY = EK_MU_TY; // update tile
 
 template <class S, class R>
 cudaError_t
