@@ -43,6 +43,20 @@ BYTES_PER_CELL = {
     ("hydro3d", "fp64"): 2 * 5 * 8,
     ("mhd3d", "mixed"): 2 * (5 * 4 + 3 * 8),
     ("mhd3d", "fp64"): 2 * 8 * 8,
+    ("mhd2d", "mixed"): 2 * (5 * 4 + 3 * 8),
+    ("mhd2d", "fp64"): 2 * 8 * 8,
+}
+
+# DRAM bytes (read + write) per interior cell of one launch of the dominant
+# kernel, from ncu captures of `python bench.py --n 192 --steps 3 --warmup 3
+# --mhd-steps 3 --no-cpu --no-ensemble --mhd2d-n 2048` (the summaries are in
+# profiles/); the per-launch traffic of the bench workload is this figure
+# times its interior cells (the traffic of these kernels grows with the cells).
+TRAFFIC_PER_CELL = {
+    ("hydro3d", "mixed"): 37.0,   # hydro3d_step<float>: 156.0 + 106.0 MB / 7.08 M cells
+    ("hydro3d", "fp64"): 78.4,    # hydro3d_step<double>: 307.7 + 247.4 MB / 7.08 M cells
+    ("mhd3d", "mixed"): 322.2,    # mhd_update_kernel<float>: 1970.3 + 310.9 MB / 7.08 M cells
+    ("mhd2d", "mixed"): 78.7,     # mhd2d_step_kernel<float>: 186.3 + 143.7 MB / 4.19 M cells
 }
 
 
@@ -353,6 +367,8 @@ def main():
     ap.add_argument("--no-mhd", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-mhd2d", action="store_true")
+    ap.add_argument("--mhd2d-n", type=int, default=4096)
     ap.add_argument("--ens-n", type=int, default=512)
     ap.add_argument("--ens-steps", type=int, default=200)
     args = ap.parse_args()
@@ -419,7 +435,8 @@ def main():
         kms, kn = meas["kernels"][0]
         achieved = BYTES_PER_CELL[key] * meas["cells"] / (kms / 1e3) / 1e9 if kms else None
         return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm if achieved else None, "traffic": None,
+                "frac": achieved / hbm if achieved else None,
+                "traffic": TRAFFIC_PER_CELL[key] * meas["cells"] if key in TRAFFIC_PER_CELL else None,
                 "kernel_ms": kms, "peak_source": peak_kind,
                 "algorithmic_bytes_per_cell": BYTES_PER_CELL[key]}
 
@@ -447,6 +464,29 @@ def main():
             "roofline_mixed": roofline(mm, ("mhd3d", "mixed")),
             "roofline_fp64": roofline(m64, ("mhd3d", "fp64")),
             "config": "MHD_Muscl_3D Orszag-Tang %d^3, HLLD + CT, slope_type 2, CFL 0.8, periodic" % args.n,
+        }
+
+    if not args.no_mhd2d:
+        n2 = args.mhd2d_n
+        ini_2, U0_2 = P.orszag_tang_2d(n=n2, nsteps=10 ** 6)
+        m2 = measure_workload(ek, "mhd2d", ek.EK_PREC_MIXED, ini_2, U0_2, args.mhd_steps, 3, sync)
+        m264 = measure_workload(ek, "mhd2d", ek.EK_PREC_FP64, ini_2, U0_2, max(2, args.mhd_steps // 4), 3, sync)
+        a2 = m2["U"][0, 0, 3:-3, 3:-3]
+        with ek.Solver(ek.params_from_ini(ini_2, precision=ek.EK_PREC_FP64)) as s64:
+            s64.set_state(U0_2)
+            s64.run(m2["iteration"])
+            b2 = s64.get_state()[0, 0, 3:-3, 3:-3]
+        v2 = m2["cells"] * m2["steps"] / (maxt(m2["ms"]) / 1e3) / 1e6 * world
+        v264 = m264["cells"] * m264["steps"] / (maxt(m264["ms"]) / 1e3) / 1e6 * world
+        workloads["mhd2d_orszag_tang_%d" % n2] = {
+            "value_mixed": v2, "value_fp64": v264, "unit": UNIT, "mixed_over_fp64": v2 / v264,
+            "ms_per_step_mixed": m2["ms"] / m2["steps"], "ms_per_step_fp64": m264["ms"] / m264["steps"],
+            "l1_rel_err_rho_mixed_vs_fp64": float(np.abs(a2 - b2).sum() / np.abs(b2).sum()),
+            "max_divB_mixed": float(m2["totals"][2]), "max_divB_fp64": float(m264["totals"][2]),
+            "kernel_ms_mixed": {name: m2["kernels"][i][0] for i, name in ((0, "step"), (2, "cfl"))},
+            "roofline_mixed": roofline(m2, ("mhd2d", "mixed")),
+            "roofline_fp64": roofline(m264, ("mhd2d", "fp64")),
+            "config": "MHD_Muscl_2D Orszag-Tang %d^2, HLLD + CT, slope_type 2, CFL 0.8, periodic" % n2,
         }
 
     if not args.no_ensemble:
