@@ -65,7 +65,25 @@ class Params(ctypes.Structure):
         ("precision", ctypes.c_int), ("exact_fp", ctypes.c_int), ("kchunk", ctypes.c_int),
         ("mhd_stage", ctypes.c_int),
         ("solver_name_", ctypes.c_char * 32), ("problem_", ctypes.c_char * 32),
+        ("output_dir_", ctypes.c_char * 256), ("output_prefix_", ctypes.c_char * 128),
+        ("vtk_enabled", ctypes.c_int), ("vtk_ascii", ctypes.c_int),
     ]
+
+    @property
+    def output_dir(self) -> str:
+        return self.output_dir_.decode()
+
+    @output_dir.setter
+    def output_dir(self, v: str):
+        self.output_dir_ = v.encode()
+
+    @property
+    def output_prefix(self) -> str:
+        return self.output_prefix_.decode()
+
+    @output_prefix.setter
+    def output_prefix(self, v: str):
+        self.output_prefix_ = v.encode()
 
     @property
     def solver_name(self) -> str:
@@ -132,6 +150,9 @@ def load_library():
         "ek_solver_synchronize": (ctypes.c_int, [c_p]),
         "ek_solver_launch_count": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_longlong)]),
         "ek_solver_stream": (ctypes.c_int, [c_p, ctypes.POINTER(c_p)]),
+        "ek_write_vtk": (ctypes.c_int, [ctypes.POINTER(Params), c_p, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_char_p]),
+        "ek_solver_save_vtk": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.c_char_p]),
         "ek_solver_set_profiling": (ctypes.c_int, [c_p, ctypes.c_int]),
         "ek_solver_kernel_time": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                                  ctypes.POINTER(ctypes.c_longlong)]),
@@ -174,6 +195,22 @@ def params_from_ini(text: str, **overrides) -> Params:
     for k, v in overrides.items():
         setattr(p, k, v)
     return p
+
+
+def write_vtk(params: Params, U: np.ndarray, step: int = 0, debug_name: str = "",
+              layout: int = EK_LAYOUT_LEFT) -> str:
+    """Write a host state as the reference's VTK file (save_VTK_2D/3D,
+    IO_VTK.cpp:24-400) into params.output_dir; returns the file name."""
+    L = load_library()
+    Uc = np.ascontiguousarray(U, dtype=np.float64)
+    _check(L.ek_write_vtk(ctypes.byref(params), Uc.ctypes.data, layout, step, debug_name.encode()),
+           "write_vtk")
+    return vtk_filename(params, step, debug_name)
+
+
+def vtk_filename(params: Params, step: int = 0, debug_name: str = "") -> str:
+    stem = params.output_prefix + ("_" + debug_name if debug_name else "")
+    return "%s/%s_%07d.vti" % (params.output_dir or "./", stem, step)
 
 
 class Solver:
@@ -270,6 +307,12 @@ class Solver:
         out = np.empty(3, dtype=np.float64)
         _check(self._L.ek_solver_totals(self._h, out.ctypes.data), "totals")
         return out
+
+    def save_vtk(self, step: int = 0, debug_name: str = "") -> str:
+        """save_solution with VTK output: the current state in the reference's
+        file format; step is the output counter (m_times_saved)."""
+        _check(self._L.ek_solver_save_vtk(self._h, step, debug_name.encode()), "save_vtk")
+        return vtk_filename(self.params, step, debug_name)
 
     def device_state(self):
         ptr, nbytes = ctypes.c_void_p(), ctypes.c_size_t()

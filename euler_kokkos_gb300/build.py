@@ -6,6 +6,7 @@ Translation units (compiled in parallel, one -gencode):
   ek_capi.cu         -- C ABI host implementation
   ek_config.cpp      -- .ini front end
   ek_noalloc.cu      -- the MHD 3D step on a static device scratch (no allocation)
+  ek_io.cpp          -- VTK output in the reference's format
 Usage: python -m euler_kokkos_gb300.build   (or build() from Python)
 """
 
@@ -47,6 +48,7 @@ def _units():
         ("ek_capi.o", os.path.join(CSRC, "ek_capi.cu"), []),
         ("ek_config.o", os.path.join(CSRC, "ek_config.cpp"), ["-x", "cu"]),
         ("ek_noalloc.o", os.path.join(CSRC, "ek_noalloc.cu"), []),
+        ("ek_io.o", os.path.join(CSRC, "ek_io.cpp"), ["-x", "cu"]),
     ]
 
 

@@ -707,6 +707,18 @@ ek_solver_get_state(ek_solver * s, double * U, int layout)
 }
 
 extern "C" ek_status
+ek_solver_save_vtk(ek_solver * s, int step, const char * debug_name)
+{
+  if (!s || !s->has_state)
+    return fail(EK_ERR_INVALID, "ek_solver_save_vtk: no state");
+  std::vector<double> h((size_t)s->kp.vstride * s->p.nbvar);
+  ek_status           st = ek_solver_get_state(s, h.data(), EK_LAYOUT_LEFT);
+  if (st != EK_OK)
+    return st;
+  return ek_write_vtk(&s->p, h.data(), EK_LAYOUT_LEFT, step, debug_name);
+}
+
+extern "C" ek_status
 ek_solver_totals(ek_solver * s, double out[3])
 {
   if (!s || !out || !s->has_state)

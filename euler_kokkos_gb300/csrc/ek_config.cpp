@@ -129,6 +129,18 @@ get_float(const Ini & ini, const char * sec, const char * name, float def)
   return (double)(end > v ? f : def);
 }
 
+// ConfigMap::getBool: exact (case-sensitive) words, else the default
+bool
+get_bool(const Ini & ini, const char * sec, const char * name, bool def)
+{
+  const std::string s = get_string(ini, sec, name, "");
+  if (s == "1" || s == "yes" || s == "true" || s == "on")
+    return true;
+  if (s == "0" || s == "no" || s == "false" || s == "off")
+    return false;
+  return def;
+}
+
 long
 get_integer(const Ini & ini, const char * sec, const char * name, long def)
 {
@@ -207,6 +219,14 @@ ek_params_from_ini(const char * text, size_t len, ek_params * out)
   p.smallp = p.smallc * p.smallc / p.gamma0;
   p.smallpp = p.smallr * p.smallp;
   p.gamma6 = (p.gamma0 + 1.0) / (2.0 * p.gamma0);
+
+  // [output]: IO_ReadWrite.cpp:31-43 (getBool: ConfigMap.cpp:64-82), IO_VTK.cpp:62-66
+  std::string odir = get_string(ini, "output", "outputDir", "./");
+  std::string opre = get_string(ini, "output", "outputPrefix", "output");
+  std::strncpy(p.output_dir, odir.c_str(), sizeof(p.output_dir) - 1);
+  std::strncpy(p.output_prefix, opre.c_str(), sizeof(p.output_prefix) - 1);
+  p.vtk_enabled = get_bool(ini, "output", "vtk_enabled", true) ? 1 : 0;
+  p.vtk_ascii = get_bool(ini, "output", "outputVtkAscii", false) ? 1 : 0;
 
   // additions of this library, in a section the reference does not read
   std::string prec = lower(get_string(ini, "gb300", "precision", "fp64"));

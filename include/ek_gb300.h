@@ -81,6 +81,10 @@ typedef struct ek_params
   int    mhd_stage; /* MHD update kernel stages the trace planes in shared memory ([gb300] mhd_stage) */
   char   solver_name[32];
   char   problem[32];
+  char   output_dir[256];    /* [output] outputDir ("./") */
+  char   output_prefix[128]; /* [output] outputPrefix ("output") */
+  int    vtk_enabled;        /* [output] vtk_enabled (1) */
+  int    vtk_ascii;          /* [output] outputVtkAscii (0) */
 } ek_params;
 
 typedef struct ek_solver ek_solver;
@@ -151,6 +155,21 @@ ek_status ek_solver_stream(ek_solver * s, void ** stream);
  * flux/emf/update kernel (MHD), 1 the MHD trace kernel, 2 the MHD CFL kernel. */
 ek_status ek_solver_set_profiling(ek_solver * s, int enable);
 ek_status ek_solver_kernel_time(ek_solver * s, int kernel, double * total_ms, long long * launches);
+
+/* VTK output in the reference's own format: save_VTK_2D / save_VTK_3D
+ * (IO_VTK.cpp:24-400, non-MPI), reached by save_solution
+ * (SolverBase.cpp:210-219 -> IO_ReadWrite.cpp:50-130).  Writes
+ * <output_dir>/<output_prefix>_<step, 7 digits>.vti (or
+ * ..._<debug_name>_<step>.vti): ImageData cell data of the interior cells in
+ * FP64, raw appended binary or ASCII (params->vtk_ascii), variable names
+ * rho, energy, rho_vx, rho_vy, rho_vz, bx, by, bz (SolverBase.cpp:60-67).
+ * The file is byte for byte the reference's.  ek_write_vtk takes a host state
+ * in either layout (CPU only); ek_solver_save_vtk writes the solver's current
+ * state.  step is the caller's output counter (the reference's
+ * m_times_saved). */
+ek_status ek_write_vtk(const ek_params * params, const double * U, int layout, int step,
+                       const char * debug_name);
+ek_status ek_solver_save_vtk(ek_solver * s, int step, const char * debug_name);
 
 /* ---------------------------------------------------------------------------
  * Ensembles of independent Hydro_Muscl_2D runs (no counterpart in the

@@ -297,8 +297,10 @@ def read_ekst(path: str):
 
 
 def run_reference(ini_text: str, U0: np.ndarray, nsteps: int, workdir: str, fast: bool = False,
-                  threads: int | None = None):
-    """Run the reference's own solver (oracle/_ref) on an injected state."""
+                  threads: int | None = None, save: bool = False):
+    """Run the reference's own solver (oracle/_ref) on an injected state;
+    save: also write the final state through the reference's output path
+    (save_solution, as the .ini's [output] section configures it)."""
     exe = REF_RUN_FAST if fast else REF_RUN
     if not os.path.exists(exe):
         raise FileNotFoundError(exe)
@@ -314,6 +316,8 @@ def run_reference(ini_text: str, U0: np.ndarray, nsteps: int, workdir: str, fast
     env = dict(os.environ)
     if threads:
         env["OMP_NUM_THREADS"] = str(threads)
+    if save:
+        env["EK_REF_SAVE"] = "1"
     subprocess.run([exe, ini, str(nsteps), out, u0], check=True, cwd=workdir, env=env,
                    stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return read_ekst(out)

@@ -122,6 +122,11 @@ run(Solver * s, euler_kokkos::HydroParams & p, int nsteps, const char * out, con
     s->next_iteration();
     dts.push_back(s->m_dt);
   }
+  // EK_REF_SAVE set: write the final state with the reference's own output
+  // path (save_solution -> IO_ReadWrite -> save_VTK_2D/3D, as configured by
+  // the [output] section of the .ini)
+  if (std::getenv("EK_REF_SAVE"))
+    s->save_solution();
   std::vector<double> buf;
   if (s->m_iteration % 2 == 0)
     copy_out(s->U, buf, nb, is, js, ks);

@@ -59,11 +59,54 @@ CASES = {
 }
 
 
+# VTK output parity: the reference writes the final state of these cases with
+# its own writer (save_VTK_2D/3D); the fixture is the written file.
+VTK_CASES = {
+    # fixture name: (golden case, ascii)
+    "implode2d_32.vti": ("implode2d_32", False),
+    "ot3d_12.vti": ("ot3d_12", False),
+    "kh2d_16_ascii.vti": ("kh2d_16", True),
+    "mhd2d_random_periodic_ascii.vti": ("mhd2d_random_periodic", True),
+}
+
+
+def with_output(ini, out_dir, prefix, ascii):
+    """The deck with its [output] section replaced: VTK on, given dir/prefix."""
+    lines, skip = [], False
+    for line in ini.splitlines():
+        if line.strip().startswith("["):
+            skip = line.strip() == "[output]"
+            if skip:
+                lines += ["[output]", "outputDir=" + out_dir, "outputPrefix=" + prefix,
+                          "vtk_enabled=true", "hdf5_enabled=false",
+                          "outputVtkAscii=" + ("true" if ascii else "false")]
+                continue
+        if not skip:
+            lines.append(line)
+    return "\n".join(lines) + "\n"
+
+
+def make_vtk(names):
+    out_dir = os.path.dirname(os.path.abspath(__file__))
+    for fname in names:
+        case, ascii = VTK_CASES[fname]
+        build, nsteps = CASES[case]
+        ini, U0 = build()
+        work = tempfile.mkdtemp(prefix="ek_vtk_")
+        ini_o = with_output(ini, work, "ref", ascii)
+        eko.run_reference(ini_o, U0, nsteps, work, save=True)
+        src = os.path.join(work, "ref_0000000.vti")
+        with open(src, "rb") as f, open(os.path.join(out_dir, fname), "wb") as g:
+            g.write(f.read())
+        print(fname, os.path.getsize(os.path.join(out_dir, fname)), "bytes")
+
+
 def main():
     out_dir = os.path.dirname(os.path.abspath(__file__))
     work = tempfile.mkdtemp(prefix="ek_golden_")
-    names = sys.argv[1:] or list(CASES)
-    for name in names:
+    names = sys.argv[1:] or list(CASES) + list(VTK_CASES)
+    make_vtk([n for n in names if n in VTK_CASES])
+    for name in [n for n in names if n in CASES]:
         build, nsteps = CASES[name]
         ini, U0 = build()
         res = eko.run_reference(ini, U0, nsteps, os.path.join(work, name))
