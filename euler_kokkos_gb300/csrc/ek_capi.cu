@@ -163,10 +163,15 @@ validate(const ek_params & p)
   for (int f = 0; f < 2 * p.dim; ++f)
     if (p.bc[f] < 1 || p.bc[f] > 3)
       return fail(EK_ERR_INVALID, "boundary types must be 1 (reflect), 2 (outflow) or 3 (periodic)");
-  if (!p.mhd && p.riemann != 3)
-    return fail(EK_ERR_UNSUPPORTED, "hydro: only riemann=hllc is implemented");
-  if (p.mhd && p.riemann != 4)
-    return fail(EK_ERR_UNSUPPORTED, "MHD: only riemann=hlld is implemented");
+  // riemann_hydro / riemann_mhd dispatch (RiemannSolvers.h:573-640,
+  // RiemannSolvers_MHD.h:368-389): for other values the reference leaves the
+  // flux unset, so they are refused here
+  if (!p.mhd && (p.riemann < 0 || p.riemann > 3))
+    return fail(EK_ERR_UNSUPPORTED, "hydro: riemann must be approx, llf, hll or hllc");
+  if (!p.mhd && p.dim == 3 && p.riemann == 2)
+    return fail(EK_ERR_UNSUPPORTED, "Hydro_Muscl_3D: the reference's 3D solver dispatch has no hll branch");
+  if (p.mhd && p.riemann != 1 && p.riemann != 2 && p.riemann != 4)
+    return fail(EK_ERR_UNSUPPORTED, "MHD: riemann must be llf, hll or hlld");
   if (p.slope_type != 1.0 && p.slope_type != 2.0)
     return fail(EK_ERR_UNSUPPORTED, "slope_type must be 1 (minmod) or 2 (MC)");
   if (p.implementation_version != 0)
@@ -220,6 +225,10 @@ make_kparams(const ek_params & p)
   k.idy = (float)(1.0 / p.dy);
   k.idz = (float)(1.0 / (p.dim == 3 ? p.dz : 1.0));
   k.mhd_stage = p.mhd_stage;
+  k.gamma6 = p.gamma6;
+  k.smallpp = p.smallpp;
+  k.gamma6f = (float)p.gamma6;
+  k.smallppf = (float)p.smallpp;
   return k;
 }
 
@@ -880,6 +889,8 @@ ek_ensemble_create(const ek_params * params, int n, ek_ensemble ** out)
       return fail(v, "instance " + std::to_string(i) + ": " + ek_last_error());
     if (p.dim != 2 || p.mhd)
       return fail(EK_ERR_UNSUPPORTED, "ensembles hold Hydro_Muscl_2D runs");
+    if (p.riemann != 3)
+      return fail(EK_ERR_UNSUPPORTED, "ensembles use riemann=hllc");
     if (p.precision != params[0].precision || p.exact_fp != params[0].exact_fp)
       return fail(EK_ERR_INVALID, "all instances of an ensemble share precision and exact_fp");
   }

@@ -58,6 +58,8 @@ struct KParams
   float     gamma0f, smallrf, smallcf, smallpf, slopef;
   float     idx, idy, idz; // 1/dx, 1/dy, 1/dz
   int       mhd_stage;     // MHD update: stage the trace planes in shared memory
+  double    gamma6, smallpp; // riemann_approx constants (HydroParams.cpp:353-356)
+  float     gamma6f, smallppf;
 };
 
 // Per-step scalars kept on the device so that consecutive steps need no host

@@ -13,7 +13,7 @@ namespace EK_NS
 template <class R>
 struct HydroConst
 {
-  R gamma0, smallr, smallp, smallc, slope_type;
+  R gamma0, smallr, smallp, smallc, slope_type, gamma6, smallpp;
 };
 
 // slope_unsplit_hydro_3d_scalar, one direction (HydroBaseFunctor3D.h:413-462,
@@ -264,6 +264,172 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
   flux[IV] = flux[ID] * ((flux[ID] > R(0)) ? ql[IV] : qr[IV]);
   if constexpr (NV == 5)
     flux[IW] = flux[ID] * ((flux[ID] > R(0)) ? ql[IW] : qr[IW]);
+}
+
+// cmpflx (RiemannSolvers.h:20-53): flux of a Godunov state
+template <class R, int NV>
+__device__ __forceinline__ void
+cmpflx(const R (&qg)[NV], R (&flux)[NV], const HydroConst<R> & C)
+{
+  flux[ID] = qg[ID] * qg[IU];
+  flux[IU] = flux[ID] * qg[IU] + qg[IP];
+  flux[IV] = flux[ID] * qg[IV];
+  if constexpr (NV == 5)
+    flux[IW] = flux[ID] * qg[IW];
+  const R entho = R(1) / (C.gamma0 - R(1));
+  R       ekin = R(0.5) * qg[ID] * (qg[IU] * qg[IU] + qg[IV] * qg[IV]);
+  if constexpr (NV == 5)
+    ekin += R(0.5) * qg[ID] * (qg[IW] * qg[IW]);
+  const R etot = qg[IP] * entho + ekin;
+  flux[IP] = qg[IU] * (etot + qg[IP]);
+}
+
+// riemann_approx (RiemannSolvers.h:60-200): two-shock iterative solver,
+// at most 10 Newton iterations on p*
+template <class R, int NV>
+__device__ __forceinline__ void
+riemann_approx(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
+{
+  const R gamma0 = C.gamma0, gamma6 = C.gamma6, smallr = C.smallr, smallc = C.smallc, smallp = C.smallp;
+  const R rl = fmax(ql[ID], smallr), ul = ql[IU], pl = fmax(ql[IP], rl * smallp);
+  const R rr = fmax(qr[ID], smallr), ur = qr[IU], pr = fmax(qr[IP], rr * smallp);
+  const R cl = gamma0 * pl * rl;
+  const R cr = gamma0 * pr * rr;
+  R       wl = sqrt(cl);
+  R       wr = sqrt(cr);
+  R       pstar = fmax(((wr * pl + wl * pr) + wl * wr * (ul - ur)) / (wl + wr), R(0));
+  R       pold = pstar;
+  R       conv = R(1);
+  for (int iter = 0; (iter < 10) && (conv > R(1e-6)); ++iter)
+  {
+    const R wwl = sqrt(cl * (R(1) + gamma6 * (pold - pl) / pl));
+    const R wwr = sqrt(cr * (R(1) + gamma6 * (pold - pr) / pr));
+    const R qql = R(2) * wwl * wwl * wwl / (wwl * wwl + cl);
+    const R qqr = R(2) * wwr * wwr * wwr / (wwr * wwr + cr);
+    const R usl = ul - (pold - pl) / wwl;
+    const R usr = ur + (pold - pr) / wwr;
+    const R delp = fmax(qqr * qql / (qqr + qql) * (usl - usr), -pold);
+    pold = pold + delp;
+    conv = fabs(delp / (pold + C.smallpp));
+  }
+  pstar = pold;
+  wl = sqrt(cl * (R(1) + gamma6 * (pstar - pl) / pl));
+  wr = sqrt(cr * (R(1) + gamma6 * (pstar - pr) / pr));
+  const R ustar = R(0.5) * (ul + (pl - pstar) / wl + ur - (pr - pstar) / wr);
+  const R sgnm = copysign(R(1), ustar);
+  R       ro, uo, po, wo;
+  if (sgnm > R(0))
+    ro = rl, uo = ul, po = pl, wo = wl;
+  else
+    ro = rr, uo = ur, po = pr, wo = wr;
+  const R co = fmax(smallc, sqrt(fabs(gamma0 * po / ro)));
+  const R rstar = fmax(R(ro / (R(1) + ro * (po - pstar) / (wo * wo))), smallr);
+  const R cstar = fmax(smallc, sqrt(fabs(gamma0 * pstar / rstar)));
+  R       spout = co - sgnm * uo;
+  R       spin = cstar - sgnm * ustar;
+  const R ushock = wo / ro - sgnm * uo;
+  if (pstar >= po)
+  {
+    spin = ushock;
+    spout = ushock;
+  }
+  const R scr = fmax(spout - spin, smallc + fabs(spout + spin));
+  R       frac = R(0.5) * (R(1) + (spout + spin) / scr);
+  if (frac != frac)
+    frac = R(0);
+  else
+    frac = frac >= R(1) ? R(1) : frac <= R(0) ? R(0) : frac;
+  R qg[NV];
+  qg[ID] = frac * rstar + (R(1) - frac) * ro;
+  qg[IU] = frac * ustar + (R(1) - frac) * uo;
+  qg[IP] = frac * pstar + (R(1) - frac) * po;
+  if (spout < R(0))
+    qg[ID] = ro, qg[IU] = uo, qg[IP] = po;
+  if (spin > R(0))
+    qg[ID] = rstar, qg[IU] = ustar, qg[IP] = pstar;
+  qg[IV] = sgnm > R(0) ? ql[IV] : qr[IV];
+  if constexpr (NV == 5)
+    qg[IW] = sgnm > R(0) ? ql[IW] : qr[IW];
+  cmpflx<R, NV>(qg, flux, C);
+}
+
+// conservative state and flux of a primitive state, as riemann_llf and
+// riemann_hll build them (RiemannSolvers.h:262-320, 384-420)
+template <class R, int NV>
+__device__ __forceinline__ void
+hydro_uf(const R (&q)[NV], R (&u)[NV], R (&f)[NV], R entho)
+{
+  u[ID] = q[ID];
+  u[IP] = q[IP] * entho + R(0.5) * q[ID] * q[IU] * q[IU];
+  u[IP] += R(0.5) * q[ID] * q[IV] * q[IV];
+  if constexpr (NV == 5)
+    u[IP] += R(0.5) * q[ID] * q[IW] * q[IW];
+  u[IU] = q[ID] * q[IU];
+  u[IV] = q[ID] * q[IV];
+  if constexpr (NV == 5)
+    u[IW] = q[ID] * q[IW];
+  f[ID] = u[ID] * q[IU];
+  f[IP] = q[IU] * (u[IP] + q[IP]);
+  f[IU] = q[IP] + u[IU] * q[IU];
+  f[IV] = f[ID] * q[IV];
+  if constexpr (NV == 5)
+    f[IW] = f[ID] * q[IW];
+}
+
+// riemann_llf (RiemannSolvers.h:218-330)
+template <class R, int NV>
+__device__ __forceinline__ void
+riemann_llf(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
+{
+  const R entho = R(1) / (C.gamma0 - R(1));
+  const R rl = fmax(ql[ID], C.smallr), ul = ql[IU], pl = fmax(ql[IP], rl * C.smallp);
+  const R rr = fmax(qr[ID], C.smallr), ur = qr[IU], pr = fmax(qr[IP], rr * C.smallp);
+  const R cl = sqrt(C.gamma0 * pl / rl);
+  const R cr = sqrt(C.gamma0 * pr / rr);
+  const R cmax = fmax(fabs(ul) + cl, fabs(ur) + cr);
+  R       uleft[NV], uright[NV], fleft[NV], fright[NV];
+  hydro_uf<R, NV>(ql, uleft, fleft, entho);
+  hydro_uf<R, NV>(qr, uright, fright, entho);
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    flux[v] = R(0.5) * (fleft[v] + fright[v] - cmax * (uright[v] - uleft[v]));
+}
+
+// riemann_hll (RiemannSolvers.h:344-432); used for 2D only, as the
+// reference's 3D dispatch has no HLL branch
+template <class R, int NV>
+__device__ __forceinline__ void
+riemann_hll(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
+{
+  const R entho = R(1) / (C.gamma0 - R(1));
+  const R rl = fmax(ql[ID], C.smallr), ul = ql[IU], pl = fmax(ql[IP], rl * C.smallp);
+  const R rr = fmax(qr[ID], C.smallr), ur = qr[IU], pr = fmax(qr[IP], rr * C.smallp);
+  const R cl = sqrt(C.gamma0 * pl / rl);
+  const R cr = sqrt(C.gamma0 * pr / rr);
+  const R SL = fmin(fmin(ul, ur) - fmax(cl, cr), R(0));
+  const R SR = fmax(fmax(ul, ur) + fmax(cl, cr), R(0));
+  R       uleft[NV], uright[NV], fleft[NV], fright[NV];
+  hydro_uf<R, NV>(ql, uleft, fleft, entho);
+  hydro_uf<R, NV>(qr, uright, fright, entho);
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+    flux[v] = (SR * fleft[v] - SL * fright[v] + SR * SL * (uright[v] - uleft[v])) / (SR - SL);
+}
+
+// riemann_hydro (RiemannSolvers.h:573-640) with the solver fixed at compile
+// time: RS = the reference's riemannSolverType (0 approx, 1 llf, 2 hll, 3 hllc)
+template <int RS, class R, int NV>
+__device__ __forceinline__ void
+hydro_riemann(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
+{
+  if constexpr (RS == 0)
+    riemann_approx<R, NV>(ql, qr, flux, C);
+  else if constexpr (RS == 1)
+    riemann_llf<R, NV>(ql, qr, flux, C);
+  else if constexpr (RS == 2)
+    riemann_hll<R, NV>(ql, qr, flux, C);
+  else
+    hllc<R, NV>(ql, qr, flux, C);
 }
 
 // per-cell CFL candidate of ComputeDtFunctor{2D,3D}

@@ -26,6 +26,8 @@ hydro_const(const KParams & P)
     C.smallp = P.smallp;
     C.smallc = P.smallc;
     C.slope_type = P.slope_type;
+    C.gamma6 = P.gamma6;
+    C.smallpp = P.smallpp;
   }
   else
   {
@@ -34,6 +36,8 @@ hydro_const(const KParams & P)
     C.smallp = P.smallpf;
     C.smallc = P.smallcf;
     C.slope_type = P.slopef;
+    C.gamma6 = P.gamma6f;
+    C.smallpp = P.smallppf;
   }
   return C;
 }
@@ -101,7 +105,7 @@ cell_slopes(const R * q0, const R * qm, const R * qp, int hx, int hy, R st, R (&
 // 2D: one CTA = one TX x TY tile of interior cells.  hydro2d_tile is the tile
 // body shared by the single-solver kernel and the ensemble kernel.
 // ---------------------------------------------------------------------------
-template <class S, class R, int TX, int TY>
+template <class S, class R, int TX, int TY, int RS = 3>
 __device__ __forceinline__ void
 hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & P, DevClock * clk,
              int step, int bx, int by, unsigned char * smem_raw)
@@ -202,7 +206,7 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
       ql[v] = sXp[(v * TY + j) * FX + i];
       qr[v] = sXm[(v * TY + j) * FX + i + 1];
     }
-    hllc<R, NV>(ql, qr, fl, C);
+    hydro_riemann<RS, R, NV>(ql, qr, fl, C);
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       sXm[(v * TY + j) * FX + i + 1] = fl[v] * dtdx;
@@ -224,7 +228,7 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
     tmp = qr[IU];
     qr[IU] = qr[IV];
     qr[IV] = tmp;
-    hllc<R, NV>(ql, qr, fl, C);
+    hydro_riemann<RS, R, NV>(ql, qr, fl, C);
     tmp = fl[IU];
     fl[IU] = fl[IV];
     fl[IV] = tmp;
@@ -264,12 +268,12 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
     step_commit(clk, step, t, dt);
 }
 
-template <class S, class R, int TX, int TY>
+template <class S, class R, int TX, int TY, int RS>
 __global__ void __launch_bounds__(TX * TY)
 hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  hydro2d_tile<S, R, TX, TY>(Uin, Uout, P, clk, step, blockIdx.x, blockIdx.y, smem_raw);
+  hydro2d_tile<S, R, TX, TY, RS>(Uin, Uout, P, clk, step, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -333,7 +337,7 @@ ensemble_totals_kernel(const EnsInstance * __restrict__ insts, const int * __res
 // ---------------------------------------------------------------------------
 // 3D: one CTA = a TX x TY column of interior cells marching over kchunk planes
 // ---------------------------------------------------------------------------
-template <class S, class R, int TX, int TY>
+template <class S, class R, int TX, int TY, int RS>
 __global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_H3_MINB_F32, EK_H3_MINB_F64))
 hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
 {
@@ -428,7 +432,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
         tmp = qr[IU];
         qr[IU] = qr[IW];
         qr[IW] = tmp;
-        hllc<R, NV>(ql, qr, fz, C);
+        hydro_riemann<RS, R, NV>(ql, qr, fz, C);
         tmp = fz[IU];
         fz[IU] = fz[IW];
         fz[IW] = tmp;
@@ -512,7 +516,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
           qr[IU] = qr[IV];
           qr[IV] = tmp;
         }
-        hllc<R, NV>(ql, qr, fl, C);
+        hydro_riemann<RS, R, NV>(ql, qr, fl, C);
         if (ydir)
         {
           R tmp = fl[IU];

@@ -30,14 +30,14 @@ hydro3d_smem()
          (3 * NV * HY * HX + 2 * NV * H3_TY * (H3_TX + 2) + 2 * NV * (H3_TY + 2) * H3_TX);
 }
 
-template <class S, class R>
+template <class S, class R, int RS>
 cudaError_t
-hydro_step_t(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
-             cudaStream_t st)
+hydro_step_rs(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
+              cudaStream_t st)
 {
   if (dim == 2)
   {
-    auto   k = hydro2d_step<S, R, H2_TX, H2_TY>;
+    auto   k = hydro2d_step<S, R, H2_TX, H2_TY, RS>;
     size_t sm = hydro2d_smem<R>();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess)
@@ -46,14 +46,38 @@ hydro_step_t(int dim, const void * Uin, void * Uout, const KParams & P, DevClock
     k<<<grid, H2_TX * H2_TY, sm, st>>>((const S *)Uin, (S *)Uout, P, clk, step);
     return cudaGetLastError();
   }
-  auto   k = hydro3d_step<S, R, H3_TX, H3_TY>;
-  size_t sm = hydro3d_smem<R>();
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess)
-    return e;
-  dim3 grid((P.nx + H3_TX - 1) / H3_TX, (P.ny + H3_TY - 1) / H3_TY, (P.nz + P.kchunk - 1) / P.kchunk);
-  k<<<grid, H3_TX * H3_TY, sm, st>>>((const S *)Uin, (S *)Uout, P, clk, step);
-  return cudaGetLastError();
+  if constexpr (RS == 2)
+  {
+    // riemann_hydro for 3D states has no HLL branch (RiemannSolvers.h:608-640)
+    return cudaErrorNotSupported;
+  }
+  else
+  {
+    auto        k = hydro3d_step<S, R, H3_TX, H3_TY, RS>;
+    size_t      sm = hydro3d_smem<R>();
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess)
+      return e;
+    dim3 grid((P.nx + H3_TX - 1) / H3_TX, (P.ny + H3_TY - 1) / H3_TY, (P.nz + P.kchunk - 1) / P.kchunk);
+    k<<<grid, H3_TX * H3_TY, sm, st>>>((const S *)Uin, (S *)Uout, P, clk, step);
+    return cudaGetLastError();
+  }
+}
+
+// the Riemann solver is a template parameter of the step kernels
+template <class S, class R>
+cudaError_t
+hydro_step_t(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
+             cudaStream_t st)
+{
+  switch (P.riemann)
+  {
+    case 0: return hydro_step_rs<S, R, 0>(dim, Uin, Uout, P, clk, step, st);
+    case 1: return hydro_step_rs<S, R, 1>(dim, Uin, Uout, P, clk, step, st);
+    case 2: return hydro_step_rs<S, R, 2>(dim, Uin, Uout, P, clk, step, st);
+    case 3: return hydro_step_rs<S, R, 3>(dim, Uin, Uout, P, clk, step, st);
+  }
+  return cudaErrorNotSupported;
 }
 
 template <class S, class R>

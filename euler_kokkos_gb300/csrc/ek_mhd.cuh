@@ -404,6 +404,94 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   }
 }
 
+// riemann_mhd (RiemannSolvers_MHD.h:368-389) with the solver fixed at compile
+// time: RS = the reference's riemannSolverType (1 llf, 2 hll, 4 hlld)
+template <int RS, class R, int NF>
+__device__ __forceinline__ void
+mhd_riemann(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0);
+
+// find_mhd_flux (mhd_utils.h:170-231, cIso = 0): conservative state and
+// flux of a face-frame primitive state; components ID, IP, IU, IV, IW and,
+// for NF = 6, IC in slot 5
+template <class R, int NF>
+__device__ __forceinline__ void
+find_mhd_flux(const R (&q)[8], R (&cv)[NF], R (&ff)[NF], R gamma0)
+{
+  const R entho = R(1.0) / (gamma0 - R(1.0));
+  const R d = q[ID], p = q[IP], u = q[IU], v = q[IV], w = q[IW], a = q[IA], b = q[IB], c = q[IC];
+  const R ecin = R(0.5) * (u * u + v * v + w * w) * d;
+  const R emag = R(0.5) * (a * a + b * b + c * c);
+  const R etot = p * entho + ecin + emag;
+  const R ptot = p + emag;
+  cv[ID] = d, cv[IP] = etot, cv[IU] = d * u, cv[IV] = d * v, cv[IW] = d * w;
+  ff[ID] = d * u;
+  ff[IP] = (etot + ptot) * u - a * (a * u + b * v + c * w);
+  ff[IU] = d * u * u - a * a + ptot;
+  ff[IV] = d * u * v - a * b;
+  ff[IW] = d * u * w - a * c;
+  if constexpr (NF > 5)
+  {
+    cv[5] = c;
+    ff[5] = c * u - a * w;
+  }
+}
+
+// riemann_hll for MHD (RiemannSolvers_MHD.h:27-62)
+template <class R, int NF>
+__device__ __forceinline__ void
+mhd_hll(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
+{
+  const R bx_mean = R(0.5) * (ql[IA] + qr[IA]);
+  ql[IA] = bx_mean;
+  qr[IA] = bx_mean;
+  R uleft[NF], fleft[NF], uright[NF], fright[NF];
+  find_mhd_flux<R, NF>(ql, uleft, fleft, gamma0);
+  find_mhd_flux<R, NF>(qr, uright, fright, gamma0);
+  const R cfleft = mhd_speed_fast<R, 0>(ql, gamma0);
+  const R cfright = mhd_speed_fast<R, 0>(qr, gamma0);
+  const R vleft = ql[IU], vright = qr[IU];
+  const R sl = fmin(fmin(vleft, vright) - fmax(cfleft, cfright), R(0.0));
+  const R sr = fmax(fmax(vleft, vright) + fmax(cfleft, cfright), R(0.0));
+#pragma unroll
+  for (int v = 0; v < NF; ++v)
+    flux[v] = (sr * fleft[v] - sl * fright[v] + sr * sl * (uright[v] - uleft[v])) / (sr - sl);
+}
+
+// riemann_llf for MHD (RiemannSolvers_MHD.h:77-104); the information speed
+// is find_speed_info of the normal direction (mhd_utils.h:379-403)
+template <class R, int NF>
+__device__ __forceinline__ void
+mhd_llf(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
+{
+  const R bx_mean = R(0.5) * (ql[IA] + qr[IA]);
+  ql[IA] = bx_mean;
+  qr[IA] = bx_mean;
+  R uleft[NF], fleft[NF], uright[NF], fright[NF];
+  find_mhd_flux<R, NF>(ql, uleft, fleft, gamma0);
+  find_mhd_flux<R, NF>(qr, uright, fright, gamma0);
+#pragma unroll
+  for (int v = 0; v < NF; ++v)
+    flux[v] = (fleft[v] + fright[v]) / R(2);
+  const R cleft = mhd_speed_fast<R, 0>(ql, gamma0) + fabs(ql[IU]);
+  const R cright = mhd_speed_fast<R, 0>(qr, gamma0) + fabs(qr[IU]);
+  const R vel_info = fmax(cleft, cright);
+#pragma unroll
+  for (int v = 0; v < NF; ++v)
+    flux[v] -= vel_info * (uright[v] - uleft[v]) / R(2);
+}
+
+template <int RS, class R, int NF>
+__device__ __forceinline__ void
+mhd_riemann(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
+{
+  if constexpr (RS == 1)
+    mhd_llf<R, NF>(ql, qr, flux, gamma0);
+  else if constexpr (RS == 2)
+    mhd_hll<R, NF>(ql, qr, flux, gamma0);
+  else
+    mhd_hlld<R, NF>(ql, qr, flux, gamma0);
+}
+
 template <class R>
 __device__ __forceinline__ R
 fmax4(R a0, R a1, R a2, R a3)

@@ -294,7 +294,7 @@ trace2d_compact(const R * sQ, const R * sB, int qx, int qy, int bx, int by, R dt
     out[f * ost] = o[f];
 }
 
-template <class S, class R, int TX, int TY>
+template <class S, class R, int TX, int TY, int RS>
 __global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_M2_MINB_F32, EK_M2_MINB_F64))
 mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KParams P, DevClock * clk,
                   int step)
@@ -395,7 +395,7 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
       R ql[8], qr[8], fl[6];
       face2d_state<R, true>(TS(i - (d == 0), j - (d == 1)), T::PL, d, ql, sr, sp);
       face2d_state<R, false>(TS(i, j), T::PL, d, qr, sr, sp);
-      mhd_hlld<R, 6>(ql, qr, fl, C.gamma0);
+      mhd_riemann<RS, R, 6>(ql, qr, fl, C.gamma0);
       R *       dst = d == 0 ? sFx : sFy;
       const int nd = d == 0 ? T::FXS : T::FYS;
 #pragma unroll
@@ -493,7 +493,9 @@ mhd2d_step_t(int phase, const void * Uin, void * Uout, const KParams & P, DevClo
     mhd2d_dt_kernel<S, R><<<row_blocks(P), 256, 0, st>>>(Uin, P, clk, step, nullptr);
     return cudaGetLastError();
   }
-  auto        k = mhd2d_step_kernel<S, R, M2_TX, M2_TY>;
+  auto k = P.riemann == 1   ? mhd2d_step_kernel<S, R, M2_TX, M2_TY, 1>
+           : P.riemann == 2 ? mhd2d_step_kernel<S, R, M2_TX, M2_TY, 2>
+                            : mhd2d_step_kernel<S, R, M2_TX, M2_TY, 4>;
   const int   sm = (int)mhd2d_smem<R>(M2_TX, M2_TY);
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   if (e != cudaSuccess)

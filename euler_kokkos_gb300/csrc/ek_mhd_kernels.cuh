@@ -492,7 +492,7 @@ struct UpdTile
   static constexpr int EZS = (TX + 1) * (TY + 1), EYS = (TX + 1) * TY, EXS = TX * (TY + 1);
 };
 
-template <class S, class R, int TX, int TY, bool STAGE>
+template <class S, class R, int TX, int TY, bool STAGE, int RS>
 __global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_MU_MINB_F32, EK_MU_MINB_F64))
 mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
                   KParams P, DevClock * clk, int step)
@@ -600,7 +600,7 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
         R ql[8], qr[8], fl[5];
         face_state_dir<R, true>(TS(i - (d == 0), j - (d == 1), k - (d == 2)), tst, d, ql, sr, sp);
         face_state_dir<R, false>(TS(i, j, k), tst, d, qr, sr, sp);
-        mhd_hlld<R>(ql, qr, fl, C.gamma0);
+        mhd_riemann<RS, R, 5>(ql, qr, fl, C.gamma0);
         R *       dst = d == 0 ? sFx : (d == 1 ? sFy : sFz);
         const int nd = d == 0 ? T::FXS : (d == 1 ? T::FYS : T::FZS);
 #pragma unroll
@@ -779,11 +779,14 @@ mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams 
     k<<<grid, MT_TX * MT_TY, sm, st>>>(Uin, (R *)work, P, clk, step);
     return cudaGetLastError();
   }
-  // 3. fluxes, emfs, update (trace read through L1, or staged in shared memory)
+  // 3. fluxes, emfs, update (trace read through L1, or staged in shared memory
+  //    for the HLLD solver); the face Riemann solver is a template parameter
   {
-    auto       k = P.mhd_stage ? mhd_update_kernel<S, R, MU_TX, MU_TY, true>
-                               : mhd_update_kernel<S, R, MU_TX, MU_TY, false>;
-    const int  sm = (int)mhd_update_smem<R>(MU_TX, MU_TY, P.mhd_stage != 0);
+    auto k = P.riemann == 1   ? mhd_update_kernel<S, R, MU_TX, MU_TY, false, 1>
+             : P.riemann == 2 ? mhd_update_kernel<S, R, MU_TX, MU_TY, false, 2>
+             : P.mhd_stage    ? mhd_update_kernel<S, R, MU_TX, MU_TY, true, 4>
+                              : mhd_update_kernel<S, R, MU_TX, MU_TY, false, 4>;
+    const int  sm = (int)mhd_update_smem<R>(MU_TX, MU_TY, P.mhd_stage != 0 && P.riemann == 4);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e != cudaSuccess)
       return e;

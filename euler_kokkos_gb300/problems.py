@@ -288,7 +288,7 @@ def kelvin_helmholtz_2d(n=128, shear=0.5, ratio=2.0, seed=20261203, nsteps=200, 
 
 
 def smooth_random(dim=3, mhd=False, nx=16, ny=None, nz=None, seed=1, bc=None, slope_type=2.0,
-                  cfl=0.7, gamma0=None, nsteps=10, amp=0.3):
+                  cfl=0.7, gamma0=None, nsteps=10, amp=0.3, riemann=None):
     """A seeded smooth state on an arbitrary (possibly non-cubic) grid, for
     parity tests: rho ~ 1 +- amp, p ~ 1 +- amp/2, |v| ~ amp, and for MHD a
     face-centred B that is the discrete curl of a seeded smooth vector
@@ -300,7 +300,8 @@ def smooth_random(dim=3, mhd=False, nx=16, ny=None, nz=None, seed=1, bc=None, sl
         gamma0 = 5.0 / 3.0 if mhd else 1.4
     if bc is None:
         bc = (3,) * 6
-    riemann = "hlld" if mhd else "hllc"
+    if riemann is None:
+        riemann = "hlld" if mhd else "hllc"
     solver = ("MHD" if mhd else "Hydro") + "_Muscl_%dD" % dim
     ini = _deck(solver, nx, ny, nz if dim == 3 else 1, bc, gamma0, cfl, slope_type, riemann,
                 "random", nsteps)

@@ -146,6 +146,198 @@ slope1(double q, double qp, double qm, double st)
   return dsgn * fmin(dlim, fabs(dcen));
 }
 
+/* cmpflx: RiemannSolvers.h:20-53 (nt transverse velocities) */
+static void
+cmpflx(const double * qg, double * flux, int nt, const eko_params * p)
+{
+  flux[EKO_ID] = qg[EKO_ID] * qg[EKO_IU];
+  flux[EKO_IU] = flux[EKO_ID] * qg[EKO_IU] + qg[EKO_IP];
+  flux[EKO_IV] = flux[EKO_ID] * qg[EKO_IV];
+  if (nt == 2)
+    flux[EKO_IW] = flux[EKO_ID] * qg[EKO_IW];
+  double entho = ONE / (p->gamma0 - ONE);
+  double ekin = HALF * qg[EKO_ID] * (qg[EKO_IU] * qg[EKO_IU] + qg[EKO_IV] * qg[EKO_IV]);
+  if (nt == 2)
+    ekin += HALF * qg[EKO_ID] * (qg[EKO_IW] * qg[EKO_IW]);
+  double etot = qg[EKO_IP] * entho + ekin;
+  flux[EKO_IP] = qg[EKO_IU] * (etot + qg[EKO_IP]);
+}
+
+/* riemann_approx: RiemannSolvers.h:60-200 (10 Newton iterations at most) */
+static void
+riemann_approx(const double * ql, const double * qr, double * flux, int nt, const eko_params * p)
+{
+  const double gamma0 = p->gamma0, gamma6 = p->gamma6, smallr = p->smallr, smallc = p->smallc,
+               smallp = p->smallp, smallpp = p->smallpp;
+  double rl = fmax(ql[EKO_ID], smallr), ul = ql[EKO_IU], pl = fmax(ql[EKO_IP], rl * smallp);
+  double rr = fmax(qr[EKO_ID], smallr), ur = qr[EKO_IU], pr = fmax(qr[EKO_IP], rr * smallp);
+  double cl = gamma0 * pl * rl;
+  double cr = gamma0 * pr * rr;
+  double wl = sqrt(cl);
+  double wr = sqrt(cr);
+  double pstar = fmax(((wr * pl + wl * pr) + wl * wr * (ul - ur)) / (wl + wr), (double)ZERO);
+  double pold = pstar;
+  double conv = ONE;
+  for (int iter = 0; (iter < 10) && (conv > 1e-6); ++iter)
+  {
+    double wwl = sqrt(cl * (ONE + gamma6 * (pold - pl) / pl));
+    double wwr = sqrt(cr * (ONE + gamma6 * (pold - pr) / pr));
+    double qql = 2.0 * wwl * wwl * wwl / (wwl * wwl + cl);
+    double qqr = 2.0 * wwr * wwr * wwr / (wwr * wwr + cr);
+    double usl = ul - (pold - pl) / wwl;
+    double usr = ur + (pold - pr) / wwr;
+    double delp = fmax(qqr * qql / (qqr + qql) * (usl - usr), -pold);
+    pold = pold + delp;
+    conv = fabs(delp / (pold + smallpp));
+  }
+  pstar = pold;
+  wl = sqrt(cl * (ONE + gamma6 * (pstar - pl) / pl));
+  wr = sqrt(cr * (ONE + gamma6 * (pstar - pr) / pr));
+  double ustar = HALF * (ul + (pl - pstar) / wl + ur - (pr - pstar) / wr);
+  double sgnm = copysign(ONE, ustar);
+  double ro, uo, po, wo;
+  if (sgnm > ZERO)
+  {
+    ro = rl, uo = ul, po = pl, wo = wl;
+  }
+  else
+  {
+    ro = rr, uo = ur, po = pr, wo = wr;
+  }
+  double co = fmax(smallc, sqrt(fabs(gamma0 * po / ro)));
+  double rstar = fmax((double)(ro / (ONE + ro * (po - pstar) / (wo * wo))), (double)(smallr));
+  double cstar = fmax(smallc, sqrt(fabs(gamma0 * pstar / rstar)));
+  double spout = co - sgnm * uo;
+  double spin = cstar - sgnm * ustar;
+  double ushock = wo / ro - sgnm * uo;
+  if (pstar >= po)
+  {
+    spin = ushock;
+    spout = ushock;
+  }
+  double scr = fmax(spout - spin, smallc + fabs(spout + spin));
+  double frac = HALF * (ONE + (spout + spin) / scr);
+  if (frac != frac)
+    frac = 0.0;
+  else
+    frac = frac >= 1.0 ? 1.0 : frac <= 0.0 ? 0.0 : frac;
+  double qg[5];
+  qg[EKO_ID] = frac * rstar + (ONE - frac) * ro;
+  qg[EKO_IU] = frac * ustar + (ONE - frac) * uo;
+  qg[EKO_IP] = frac * pstar + (ONE - frac) * po;
+  if (spout < ZERO)
+  {
+    qg[EKO_ID] = ro, qg[EKO_IU] = uo, qg[EKO_IP] = po;
+  }
+  if (spin > ZERO)
+  {
+    qg[EKO_ID] = rstar, qg[EKO_IU] = ustar, qg[EKO_IP] = pstar;
+  }
+  if (sgnm > ZERO)
+  {
+    qg[EKO_IV] = ql[EKO_IV];
+    if (nt == 2)
+      qg[EKO_IW] = ql[EKO_IW];
+  }
+  else
+  {
+    qg[EKO_IV] = qr[EKO_IV];
+    if (nt == 2)
+      qg[EKO_IW] = qr[EKO_IW];
+  }
+  cmpflx(qg, flux, nt, p);
+}
+
+/* conservative state and flux of a primitive state, as riemann_llf and
+ * riemann_hll build them (RiemannSolvers.h:262-320, 384-420) */
+static void
+hydro_uf(const double * q, double * u, double * f, int nt, double entho)
+{
+  u[EKO_ID] = q[EKO_ID];
+  u[EKO_IP] = q[EKO_IP] * entho + HALF * q[EKO_ID] * q[EKO_IU] * q[EKO_IU];
+  u[EKO_IP] += HALF * q[EKO_ID] * q[EKO_IV] * q[EKO_IV];
+  if (nt == 2)
+    u[EKO_IP] += HALF * q[EKO_ID] * q[EKO_IW] * q[EKO_IW];
+  u[EKO_IU] = q[EKO_ID] * q[EKO_IU];
+  u[EKO_IV] = q[EKO_ID] * q[EKO_IV];
+  if (nt == 2)
+    u[EKO_IW] = q[EKO_ID] * q[EKO_IW];
+  f[EKO_ID] = u[EKO_ID] * q[EKO_IU];
+  f[EKO_IP] = q[EKO_IU] * (u[EKO_IP] + q[EKO_IP]);
+  f[EKO_IU] = q[EKO_IP] + u[EKO_IU] * q[EKO_IU];
+  f[EKO_IV] = f[EKO_ID] * q[EKO_IV];
+  if (nt == 2)
+    f[EKO_IW] = f[EKO_ID] * q[EKO_IW];
+}
+
+/* riemann_llf: RiemannSolvers.h:218-330 */
+static void
+riemann_llf(const double * ql, const double * qr, double * flux, int nt, const eko_params * p)
+{
+  const double gamma0 = p->gamma0, smallr = p->smallr, smallp = p->smallp;
+  const double entho = ONE / (gamma0 - ONE);
+  double rl = fmax(ql[EKO_ID], smallr), ul = ql[EKO_IU], pl = fmax(ql[EKO_IP], rl * smallp);
+  double rr = fmax(qr[EKO_ID], smallr), ur = qr[EKO_IU], pr = fmax(qr[EKO_IP], rr * smallp);
+  double cl = sqrt(gamma0 * pl / rl);
+  double cr = sqrt(gamma0 * pr / rr);
+  double cmax = fmax(fabs(ul) + cl, fabs(ur) + cr);
+  double uleft[5], uright[5], fleft[5], fright[5];
+  hydro_uf(ql, uleft, fleft, nt, entho);
+  hydro_uf(qr, uright, fright, nt, entho);
+  for (int v = 0; v < 4; v++)
+    flux[v] = HALF * (fleft[v] + fright[v] - cmax * (uright[v] - uleft[v]));
+  if (nt == 2)
+    flux[EKO_IW] = HALF * (fleft[EKO_IW] + fright[EKO_IW] - cmax * (uright[EKO_IW] - uleft[EKO_IW]));
+}
+
+/* riemann_hll: RiemannSolvers.h:344-432 (fleft[ID] is uleft[IU] here) */
+static void
+riemann_hll(const double * ql, const double * qr, double * flux, int nt, const eko_params * p)
+{
+  const double gamma0 = p->gamma0, smallr = p->smallr, smallp = p->smallp;
+  const double entho = ONE / (gamma0 - ONE);
+  double rl = fmax(ql[EKO_ID], smallr), ul = ql[EKO_IU], pl = fmax(ql[EKO_IP], rl * smallp);
+  double rr = fmax(qr[EKO_ID], smallr), ur = qr[EKO_IU], pr = fmax(qr[EKO_IP], rr * smallp);
+  double cl = sqrt(gamma0 * pl / rl);
+  double cr = sqrt(gamma0 * pr / rr);
+  double SL = fmin(fmin(ul, ur) - fmax(cl, cr), (double)ZERO);
+  double SR = fmax(fmax(ul, ur) + fmax(cl, cr), (double)ZERO);
+  double uleft[5], uright[5], fleft[5], fright[5];
+  hydro_uf(ql, uleft, fleft, nt, entho);
+  hydro_uf(qr, uright, fright, nt, entho);
+  fleft[EKO_ID] = uleft[EKO_IU];
+  fright[EKO_ID] = uright[EKO_IU];
+  fleft[EKO_IV] = fleft[EKO_ID] * ql[EKO_IV];
+  fright[EKO_IV] = fright[EKO_ID] * qr[EKO_IV];
+  if (nt == 2)
+  {
+    fleft[EKO_IW] = fleft[EKO_ID] * ql[EKO_IW];
+    fright[EKO_IW] = fright[EKO_ID] * qr[EKO_IW];
+  }
+  for (int v = 0; v < 4; v++)
+    flux[v] = (SR * fleft[v] - SL * fright[v] + SR * SL * (uright[v] - uleft[v])) / (SR - SL);
+  if (nt == 2)
+    flux[EKO_IW] =
+      (SR * fleft[EKO_IW] - SL * fright[EKO_IW] + SR * SL * (uright[EKO_IW] - uleft[EKO_IW])) / (SR - SL);
+}
+
+static void hllc(const double * ql, const double * qr, double * flux, int nt, const eko_params * p);
+
+/* riemann_hydro: RiemannSolvers.h:573-640 (the 3D dispatch has no HLL
+ * branch; HLL is refused for 3D by eko_create) */
+static void
+riemann_hydro(const double * ql, const double * qr, double * flux, int nt, const eko_params * p)
+{
+  if (p->riemann == EKO_RIEMANN_APPROX)
+    riemann_approx(ql, qr, flux, nt, p);
+  else if (p->riemann == EKO_RIEMANN_HLL)
+    riemann_hll(ql, qr, flux, nt, p);
+  else if (p->riemann == EKO_RIEMANN_LLF)
+    riemann_llf(ql, qr, flux, nt, p);
+  else
+    hllc(ql, qr, flux, nt, p);
+}
+
 /* riemann_hllc: RiemannSolvers.h:445-568.  nt = number of transverse
  * velocities (1 in 2D: IV; 2 in 3D: IV, IW).  q layout [ID,IP,IU,IV,(IW)] */
 static void
@@ -475,7 +667,7 @@ hydro_godunov(eko_solver * s, double * in, double * out, double dt)
             swapd(&ql[EKO_IU], &ql[it]);
             swapd(&qr[EKO_IU], &qr[it]);
           }
-          hllc(ql, qr, fl, dim == 3 ? 2 : 1, p);
+          riemann_hydro(ql, qr, fl, dim == 3 ? 2 : 1, p);
           if (d > 0)
             swapd(&fl[EKO_IU], &fl[it]);
           for (int v = 0; v < nb; ++v)
@@ -712,6 +904,83 @@ hlld(double * ql, double * qr, double * flux, const eko_params * p)
   flux[EKO_IA] = 0.0;
   flux[EKO_IB] = bo * uo - a * vo;
   flux[EKO_IC] = co * uo - a * wo;
+}
+
+/* find_mhd_flux: mhd_utils.h:170-231 (cIso = 0) */
+static void
+find_mhd_flux(const double * q, double * cv, double * ff, const eko_params * p)
+{
+  const double pp = q[EKO_IP];
+  const double entho = ONE / (p->gamma0 - ONE);
+  const double d = q[EKO_ID], u = q[EKO_IU], v = q[EKO_IV], w = q[EKO_IW], a = q[EKO_IA], b = q[EKO_IB],
+               c = q[EKO_IC];
+  const double ecin = 0.5 * (u * u + v * v + w * w) * d;
+  const double emag = 0.5 * (a * a + b * b + c * c);
+  const double etot = pp * entho + ecin + emag;
+  const double ptot = pp + emag;
+  cv[EKO_ID] = d, cv[EKO_IP] = etot, cv[EKO_IU] = d * u, cv[EKO_IV] = d * v, cv[EKO_IW] = d * w;
+  cv[EKO_IA] = a, cv[EKO_IB] = b, cv[EKO_IC] = c;
+  ff[EKO_ID] = d * u;
+  ff[EKO_IP] = (etot + ptot) * u - a * (a * u + b * v + c * w);
+  ff[EKO_IU] = d * u * u - a * a + ptot;
+  ff[EKO_IV] = d * u * v - a * b;
+  ff[EKO_IW] = d * u * w - a * c;
+  ff[EKO_IA] = 0.0;
+  ff[EKO_IB] = b * u - a * v;
+  ff[EKO_IC] = c * u - a * w;
+}
+
+/* riemann_hll (MHD): RiemannSolvers_MHD.h:27-62 (qleft/qright are modified) */
+static void
+mhd_hll(double * ql, double * qr, double * flux, const eko_params * p)
+{
+  double bx_mean = 0.5 * (ql[EKO_IA] + qr[EKO_IA]);
+  ql[EKO_IA] = bx_mean;
+  qr[EKO_IA] = bx_mean;
+  double uleft[8], fleft[8], uright[8], fright[8];
+  find_mhd_flux(ql, uleft, fleft, p);
+  find_mhd_flux(qr, uright, fright, p);
+  double cfleft = speed_fast(ql, 0, p->gamma0);
+  double cfright = speed_fast(qr, 0, p->gamma0);
+  double vleft = ql[EKO_IU], vright = qr[EKO_IU];
+  double sl = fmin(fmin(vleft, vright) - fmax(cfleft, cfright), 0.0);
+  double sr = fmax(fmax(vleft, vright) + fmax(cfleft, cfright), 0.0);
+  for (int v = 0; v < 8; ++v)
+    flux[v] = (sr * fleft[v] - sl * fright[v] + sr * sl * (uright[v] - uleft[v])) / (sr - sl);
+}
+
+/* riemann_llf (MHD): RiemannSolvers_MHD.h:77-104, find_speed_info of one
+ * direction (mhd_utils.h:379-403) */
+static void
+mhd_llf(double * ql, double * qr, double * flux, const eko_params * p)
+{
+  double bx_mean = HALF * (ql[EKO_IA] + qr[EKO_IA]);
+  ql[EKO_IA] = bx_mean;
+  qr[EKO_IA] = bx_mean;
+  double uleft[8], fleft[8], uright[8], fright[8];
+  find_mhd_flux(ql, uleft, fleft, p);
+  find_mhd_flux(qr, uright, fright, p);
+  for (int v = 0; v < 8; ++v)
+    flux[v] = (fleft[v] + fright[v]) / 2;
+  double cleft = speed_fast(ql, 0, p->gamma0) + fabs(ql[EKO_IU]);
+  double cright = speed_fast(qr, 0, p->gamma0) + fabs(qr[EKO_IU]);
+  double vel_info = fmax(cleft, cright);
+  for (int v = 0; v < 8; ++v)
+    flux[v] -= vel_info * (uright[v] - uleft[v]) / 2;
+}
+
+static void hlld(double * ql, double * qr, double * flux, const eko_params * p);
+
+/* riemann_mhd: RiemannSolvers_MHD.h:368-389 */
+static void
+riemann_mhd(double * ql, double * qr, double * flux, const eko_params * p)
+{
+  if (p->riemann == EKO_RIEMANN_HLL)
+    mhd_hll(ql, qr, flux, p);
+  else if (p->riemann == EKO_RIEMANN_LLF)
+    mhd_llf(ql, qr, flux, p);
+  else
+    hlld(ql, qr, flux, p);
 }
 
 /* FMAX4/FMIN4/FMAX5: mhd_utils.h:38-75 */
@@ -1322,7 +1591,7 @@ mhd3d_godunov(eko_solver * s, double * in, double * out)
           ql[v] = AT(s->Qm[0], s, v, c - 1);
           qr[v] = AT(s->Qp[0], s, v, c);
         }
-        hlld(ql, qr, fl, p);
+        riemann_mhd(ql, qr, fl, p);
         for (int v = 0; v < 8; ++v)
           AT(s->Fx, s, v, c) = fl[v];
         /* y: swap IU<->IV and IA<->IB */
@@ -1335,7 +1604,7 @@ mhd3d_godunov(eko_solver * s, double * in, double * out)
         swapd(&ql[EKO_IA], &ql[EKO_IB]);
         swapd(&qr[EKO_IU], &qr[EKO_IV]);
         swapd(&qr[EKO_IA], &qr[EKO_IB]);
-        hlld(ql, qr, fl, p);
+        riemann_mhd(ql, qr, fl, p);
         for (int v = 0; v < 8; ++v)
           AT(s->Fy, s, v, c) = fl[v];
         /* z: swap IU<->IW and IA<->IC */
@@ -1348,7 +1617,7 @@ mhd3d_godunov(eko_solver * s, double * in, double * out)
         swapd(&ql[EKO_IA], &ql[EKO_IC]);
         swapd(&qr[EKO_IU], &qr[EKO_IW]);
         swapd(&qr[EKO_IA], &qr[EKO_IC]);
-        hlld(ql, qr, fl, p);
+        riemann_mhd(ql, qr, fl, p);
         for (int v = 0; v < 8; ++v)
           AT(s->Fz, s, v, c) = fl[v];
 
@@ -1699,7 +1968,7 @@ mhd2d_godunov(eko_solver * s, double * in, double * out)
         ql[v] = AT(s->Qm[0], s, v, c - 1);
         qr[v] = AT(s->Qp[0], s, v, c);
       }
-      hlld(ql, qr, flux, p);
+      riemann_mhd(ql, qr, flux, p);
       for (int v = 0; v < 8; ++v)
         AT(s->Fx, s, v, c) = flux[v];
       for (int v = 0; v < 8; ++v)
@@ -1711,7 +1980,7 @@ mhd2d_godunov(eko_solver * s, double * in, double * out)
       x = ql[EKO_IA], ql[EKO_IA] = ql[EKO_IB], ql[EKO_IB] = x;
       x = qr[EKO_IU], qr[EKO_IU] = qr[EKO_IV], qr[EKO_IV] = x;
       x = qr[EKO_IA], qr[EKO_IA] = qr[EKO_IB], qr[EKO_IB] = x;
-      hlld(ql, qr, flux, p);
+      riemann_mhd(ql, qr, flux, p);
       for (int v = 0; v < 8; ++v)
         AT(s->Fy, s, v, c) = flux[v];
 
@@ -1784,6 +2053,16 @@ eko_solver *
 eko_create(const eko_params * p, const double * U0, double t0)
 {
   if (!p || !U0)
+    return NULL;
+  /* riemann_hydro (3D) has no HLL branch and riemann_mhd only HLLD/HLL/LLF:
+   * the reference leaves the flux unset there (RiemannSolvers.h:608-640,
+   * RiemannSolvers_MHD.h:368-389) */
+  if (!p->mhd && p->dim == 3 && p->riemann == EKO_RIEMANN_HLL)
+    return NULL;
+  if (p->mhd && p->riemann != EKO_RIEMANN_HLLD && p->riemann != EKO_RIEMANN_HLL &&
+      p->riemann != EKO_RIEMANN_LLF)
+    return NULL;
+  if (!p->mhd && p->riemann == EKO_RIEMANN_HLLD)
     return NULL;
   eko_solver * s = (eko_solver *)calloc(1, sizeof(eko_solver));
   s->p = *p;

@@ -45,6 +45,7 @@ typedef struct eko_params
   int    riemann;
   double tEnd;
   int    nStepmax;
+  double gamma6; /* (gamma0 + 1) / (2 gamma0), HydroParams.cpp:356 */
 } eko_params;
 
 typedef struct eko_solver eko_solver;

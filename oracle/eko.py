@@ -152,6 +152,7 @@ class eko_params(ctypes.Structure):
         ("riemann", ctypes.c_int),
         ("tEnd", ctypes.c_double),
         ("nStepmax", ctypes.c_int),
+        ("gamma6", ctypes.c_double),
     ]
 
 
@@ -212,6 +213,7 @@ class Params:
         p.cIso, p.Omega0 = 0.0, 0.0
         p.riemann = self.riemann
         p.tEnd, p.nStepmax = self.tEnd, self.nStepmax
+        p.gamma6 = self.gamma6
         return p
 
     @property

@@ -56,6 +56,18 @@ CASES = {
     "mhd2d_random_mixedbc": (lambda: P.smooth_random(dim=2, mhd=True, nx=18, ny=16, seed=10,
                                                       bc=(2, 2, 3, 3, 1, 1), slope_type=2.0,
                                                       nsteps=6), 6),
+    # the other Riemann solvers of the path (riemann = approx / llf / hll)
+    "implode2d_llf": (lambda: P.implode_2d(n=24, nsteps=10, riemann="llf"), 10),
+    "implode2d_hll": (lambda: P.implode_2d(n=24, nsteps=10, riemann="hll"), 10),
+    "implode2d_approx": (lambda: P.implode_2d(n=24, nsteps=10, riemann="approx"), 10),
+    "hydro2d_random_approx_mc": (lambda: P.smooth_random(dim=2, nx=18, ny=15, seed=12, bc=(2, 2, 3, 3, 1, 1),
+                                                          slope_type=2.0, nsteps=8, riemann="approx"), 8),
+    "blast3d_llf": (lambda: P.blast_3d(n=10, nsteps=5, riemann="llf"), 5),
+    "blast3d_approx": (lambda: P.blast_3d(n=10, nsteps=5, riemann="approx"), 5),
+    "ot3d_hll": (lambda: P.orszag_tang_3d(n=10, nsteps=4, riemann="hll"), 4),
+    "ot3d_llf": (lambda: P.orszag_tang_3d(n=10, nsteps=4, riemann="llf"), 4),
+    "ot2d_hll": (lambda: P.orszag_tang_2d(n=20, nsteps=6, riemann="hll"), 6),
+    "ot2d_llf": (lambda: P.orszag_tang_2d(n=20, nsteps=6, riemann="llf"), 6),
 }
 
 

@@ -128,7 +128,7 @@ def test_create_without_gpu_fails_cleanly():
 def test_create_rejects_unsupported_configurations():
     # validation happens before any device call
     p = ek.params_from_ini(DECK)
-    for bad in (dict(riemann=0), dict(slope_type=3.0), dict(implementation_version=1),
+    for bad in (dict(riemann=4), dict(riemann=7), dict(slope_type=3.0), dict(implementation_version=1),
                 dict(nx=1, isize=5), dict(exact_fp=1, precision=1)):
         with pytest.raises(ek.EkError) as e:
             ek.Solver(p.copy(**bad))
