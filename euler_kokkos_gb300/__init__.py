@@ -153,6 +153,9 @@ def load_library():
         "ek_write_vtk": (ctypes.c_int, [ctypes.POINTER(Params), c_p, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_char_p]),
         "ek_solver_save_vtk": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.c_char_p]),
+        "ek_solver_save_restart": (ctypes.c_int, [c_p, ctypes.c_char_p, ctypes.c_int]),
+        "ek_solver_load_restart": (ctypes.c_int, [c_p, ctypes.c_char_p, ctypes.c_int,
+                                                  ctypes.POINTER(ctypes.c_int)]),
         "ek_solver_set_profiling": (ctypes.c_int, [c_p, ctypes.c_int]),
         "ek_solver_kernel_time": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                                  ctypes.POINTER(ctypes.c_longlong)]),
@@ -307,6 +310,18 @@ class Solver:
         out = np.empty(3, dtype=np.float64)
         _check(self._L.ek_solver_totals(self._h, out.ctypes.data), "totals")
         return out
+
+    def save_restart(self, path: str, times_saved: int = 0):
+        """Write a restart file of the current state, m_t and the output counter."""
+        _check(self._L.ek_solver_save_restart(self._h, path.encode(), times_saved), "save_restart")
+
+    def load_restart(self, path: str, reset_time: bool = False) -> int:
+        """init_restart: restore the state and m_t from a restart file, start
+        at iteration 0; returns the saved output counter (m_times_saved)."""
+        n = ctypes.c_int(0)
+        _check(self._L.ek_solver_load_restart(self._h, path.encode(), int(reset_time), ctypes.byref(n)),
+               "load_restart")
+        return n.value
 
     def save_vtk(self, step: int = 0, debug_name: str = "") -> str:
         """save_solution with VTK output: the current state in the reference's

@@ -4,6 +4,7 @@
 // (SolverBase.cpp:124-195, SolverHydroMuscl.h:164-307, 635-700,
 // SolverMHDMuscl.h:384-397, 741-801) with the kernels of ek_kernels.cu.
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -483,11 +484,21 @@ clock_dt(const ek_solver * s, const DevClock & h, int step)
   return d;
 }
 
+static ek_status set_state_at(ek_solver * s, const double * U, int layout, double t0);
+
 extern "C" ek_status
 ek_solver_set_state(ek_solver * s, const double * U, int layout)
 {
   if (!s || !U || (layout != EK_LAYOUT_LEFT && layout != EK_LAYOUT_RIGHT))
     return fail(EK_ERR_INVALID, "ek_solver_set_state: bad argument");
+  return set_state_at(s, U, layout, s->p.tCurrent);
+}
+
+// the state injection of the constructor tail, starting at time t0 and
+// iteration 0 (a restarted run also starts at iteration 0, SolverHydroMuscl.h:512-580)
+static ek_status
+set_state_at(ek_solver * s, const double * U, int layout, double t0)
+{
   EK_CUDA(cudaSetDevice(s->device), "cudaSetDevice");
   to_device_layout(s, U, layout, s->hbuf);
   ek_status st = upload(s, s->hbuf, s->U[0]);
@@ -498,7 +509,7 @@ ek_solver_set_state(ek_solver * s, const double * U, int layout)
   EK_CUDA(ek_fast::fill_ghosts(s->prec, s->U[0], s->kp, s->p.mhd ? 8 : s->p.nbvar, s->stream), "ghosts");
   EK_CUDA(cudaMemcpyAsync(s->U[1], s->U[0], s->state_bytes, cudaMemcpyDeviceToDevice, s->stream), "copy");
   s->launches += 1;
-  s->t = s->p.tCurrent;
+  s->t = t0;
   s->iteration = 0;
   st2 = reset_clock(s, s->t);
   if (st2 != EK_OK)
@@ -713,6 +724,62 @@ ek_solver_get_state(ek_solver * s, double * U, int layout)
     return st;
   from_device_layout(s, s->hbuf, U, layout);
   return EK_OK;
+}
+
+// restart file: a fixed header, then the FP64 LayoutLeft state, ghosts included
+struct RestartHeader
+{
+  char    magic[8]; // "EKRSTRT1"
+  int32_t dim, mhd, nbvar, isize, jsize, ksize;
+  int32_t times_saved, iteration;
+  double  t;
+};
+
+extern "C" ek_status
+ek_solver_save_restart(ek_solver * s, const char * path, int times_saved)
+{
+  if (!s || !path || !s->has_state)
+    return fail(EK_ERR_INVALID, "ek_solver_save_restart: bad argument");
+  std::vector<double> h((size_t)s->kp.vstride * s->p.nbvar);
+  ek_status           st = ek_solver_get_state(s, h.data(), EK_LAYOUT_LEFT);
+  if (st != EK_OK)
+    return st;
+  RestartHeader hd;
+  std::memset(&hd, 0, sizeof hd);
+  std::memcpy(hd.magic, "EKRSTRT1", 8);
+  hd.dim = s->p.dim, hd.mhd = s->p.mhd, hd.nbvar = s->p.nbvar;
+  hd.isize = s->p.isize, hd.jsize = s->p.jsize, hd.ksize = s->p.dim == 3 ? s->p.ksize : 1;
+  hd.times_saved = times_saved, hd.iteration = s->iteration;
+  hd.t = s->t;
+  FILE * f = std::fopen(path, "wb");
+  if (!f)
+    return fail(EK_ERR_INVALID, std::string("ek_solver_save_restart: cannot open ") + path);
+  const bool ok = std::fwrite(&hd, sizeof hd, 1, f) == 1 && std::fwrite(h.data(), sizeof(double), h.size(), f) == h.size();
+  if (std::fclose(f) != 0 || !ok)
+    return fail(EK_ERR_INVALID, std::string("ek_solver_save_restart: write failed for ") + path);
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_load_restart(ek_solver * s, const char * path, int reset_time, int * times_saved)
+{
+  if (!s || !path)
+    return fail(EK_ERR_INVALID, "ek_solver_load_restart: bad argument");
+  FILE * f = std::fopen(path, "rb");
+  if (!f)
+    return fail(EK_ERR_INVALID, std::string("ek_solver_load_restart: cannot open ") + path);
+  RestartHeader hd;
+  std::vector<double> h((size_t)s->kp.vstride * s->p.nbvar);
+  bool ok = std::fread(&hd, sizeof hd, 1, f) == 1 && std::memcmp(hd.magic, "EKRSTRT1", 8) == 0;
+  ok = ok && hd.dim == s->p.dim && hd.mhd == s->p.mhd && hd.nbvar == s->p.nbvar && hd.isize == s->p.isize &&
+       hd.jsize == s->p.jsize && hd.ksize == (s->p.dim == 3 ? s->p.ksize : 1);
+  ok = ok && std::fread(h.data(), sizeof(double), h.size(), f) == h.size();
+  std::fclose(f);
+  if (!ok)
+    return fail(EK_ERR_INVALID, std::string("ek_solver_load_restart: not a restart file of this grid: ") + path);
+  if (times_saved)
+    *times_saved = hd.times_saved;
+  return set_state_at(s, h.data(), EK_LAYOUT_LEFT, reset_time ? 0.0 : hd.t);
 }
 
 extern "C" ek_status

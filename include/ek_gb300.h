@@ -171,6 +171,17 @@ ek_status ek_write_vtk(const ek_params * params, const double * U, int layout, i
                        const char * debug_name);
 ek_status ek_solver_save_vtk(ek_solver * s, int step, const char * debug_name);
 
+/* Restart files.  The reference restarts from its HDF5 output
+ * (init_restart: load_data -> m_times_saved, m_t; SolverHydroMuscl.h:512-580,
+ * SolverMHDMuscl.h:611-639); HDF5 is not available here, so the file is raw
+ * binary: a header (magic "EKRSTRT1", dim, mhd, nbvar, isize, jsize, ksize,
+ * times_saved, iteration, t) and the FP64 LayoutLeft state with its ghosts.
+ * Loading restores the state, m_t (0 when reset_time, the reference's
+ * restart_reset_totaltime) and the output counter, and starts at
+ * m_iteration 0 as the reference does; the grid must match. */
+ek_status ek_solver_save_restart(ek_solver * s, const char * path, int times_saved);
+ek_status ek_solver_load_restart(ek_solver * s, const char * path, int reset_time, int * times_saved);
+
 /* ---------------------------------------------------------------------------
  * Ensembles of independent Hydro_Muscl_2D runs (no counterpart in the
  * reference, which runs one problem per process): every instance has its own
