@@ -28,6 +28,7 @@ __all__ = [
     "orszag_tang_2d",
     "mhd_blast_3d",
     "kelvin_helmholtz_2d",
+    "rayleigh_taylor",
     "kh_ensemble",
     "smooth_random",
     "ini_text",
@@ -284,6 +285,65 @@ def kelvin_helmholtz_2d(n=128, shear=0.5, ratio=2.0, seed=20261203, nsteps=200, 
     U[2, 0] = dens * uu
     U[3, 0] = dens * vv
     U[1, 0] = _f(pressure) / (g - 1.0) + 0.5 * dens * (uu * uu + vv * vv)
+    return ini, U
+
+
+def rayleigh_taylor(dim=2, nx=100, ny=None, nz=None, nsteps=100, amplitude=0.01, d0=1.0, d1=2.0,
+                    g=-0.1, hancock=False, riemann="approx", slope_type=2.0, cfl=0.7, gamma0=1.4,
+                    seed=0x5A7E, noise=0.0):
+    """Rayleigh-Taylor instability under static gravity (the reference's
+    settings/test_rayleigh_taylor_{2d,3d}.ini decks, [gravity] enabled): the
+    init of HydroInitFunctors2D.h:690-772 / HydroInitFunctors3D.h:757-843 --
+    density d1 above the mid-plane of the gravity axis (y in 2D, z in 3D) and
+    d0 below, a cosine velocity perturbation along that axis, hydrostatic
+    energy (P0 + rho g.x)/(gamma0 - 1) -- on [-0.5,0.5]^(dim-1) x [-1.5,1.5],
+    periodic across and reflecting along the gravity axis.  g is the gravity
+    component along that axis; noise adds rho*(1 + noise*u) with the seeded
+    splitmix noise.  hancock turns on [gravity] hancock_predictor_enabled."""
+    if dim == 2:
+        ny = 3 * nx if ny is None else ny
+        nz = 1
+        bc = (3, 3, 1, 1, 1, 1)
+        mesh = {"xmin": -0.5, "xmax": 0.5, "ymin": -1.5, "ymax": 1.5}
+        gvec = (0.0, _f(g), 0.0)
+    else:
+        ny = nx if ny is None else ny
+        nz = 3 * nx if nz is None else nz
+        bc = (3, 3, 3, 3, 1, 1)
+        mesh = {"xmin": -0.5, "xmax": 0.5, "ymin": -0.5, "ymax": 0.5, "zmin": -1.5, "zmax": 1.5}
+        gvec = (0.0, 0.0, _f(g))
+    gw = 2
+    rt = {"amplitude": amplitude, "d0": d0, "d1": d1, "gx": 0.0, "gy": g if dim == 2 else 0.0}
+    if dim == 3:
+        rt["gz"] = g
+    grav = {"enabled": "yes", "static": "yes"}
+    if hancock:
+        grav["hancock_predictor_enabled"] = "yes"
+    ini = _deck("Hydro_Muscl_%dD" % dim, nx, ny, nz, bc, gamma0, cfl, slope_type, riemann, "rayleigh_taylor",
+                nsteps, {"mesh": mesh, "gravity": grav, "rayleigh_taylor": rt})
+    gam = _f(gamma0)
+    lo = [_f(mesh["xmin"]), _f(mesh["ymin"]), _f(mesh.get("zmin", 0.0))]
+    hi = [_f(mesh["xmax"]), _f(mesh["ymax"]), _f(mesh.get("zmax", 1.0))]
+    n = (nx, ny, nz)
+    d = [(hi[a] - lo[a]) / n[a] for a in range(3)]
+    x = _centres(nx, gw, lo[0], d[0])[None, None, :]
+    y = _centres(ny, gw, lo[1], d[1])[None, :, None]
+    z = _centres(nz, gw, lo[2], d[2])[:, None, None] if dim == 3 else np.zeros((1, 1, 1))
+    shp = (nz + 2 * gw if dim == 3 else 1, ny + 2 * gw, nx + 2 * gw)
+    axis = y if dim == 2 else z
+    mid = (lo[1] + hi[1]) / 2 if dim == 2 else (lo[2] + hi[2]) / 2
+    rho = np.broadcast_to(np.where(axis > mid, _f(d1), _f(d0)), shp).copy()
+    if noise:
+        idx = np.arange(int(np.prod(shp)), dtype=np.uint64).reshape(shp)
+        rho = rho * (1.0 + noise * splitmix_uniform(seed, idx))
+    Lx, Ly = hi[0] - lo[0], hi[1] - lo[1]
+    pert = _f(amplitude) * rho * (1 + np.cos(2 * math.pi * x / Lx)) * (1 + np.cos(2 * math.pi * y / Ly)) / 4
+    nb = 4 if dim == 2 else 5
+    U = np.zeros((nb,) + shp)
+    U[0] = rho
+    U[2 + (dim - 1)] = np.broadcast_to(pert, shp)
+    gx, gy, gz = gvec
+    U[1] = (1.0 + rho * (gx * x + gy * y + gz * z)) / (gam - 1.0)
     return ini, U
 
 

@@ -53,6 +53,7 @@ struct eko_solver
   double * Qp[3];
   double * QE[4][3]; /* edge traces [RT,RB,LT,LB][x,y,z] */
   double * Emf;    /* 3 components: I_EMFZ=0, I_EMFY=1, I_EMFX=2 (enums.h:215-220) */
+  double * G;      /* static gravity field, dim components (SolverHydroMuscl.h:86-87) */
   double   t, dt;
   int      iteration;
   long     ncell;
@@ -460,6 +461,31 @@ hydro_prims(const double * u, double * q, double * c, int dim, const eko_params 
     q[EKO_IW] = uz;
 }
 
+/* the CFL term of ComputeDtGravityFunctor2D/3D (HydroRunFunctors2D.h:158-169,
+ * HydroRunFunctors3D.h:162-183): g dt^2 / (2 dx) + u dt / dx <= cfl with
+ * u = sum(|v_i| + c), g = sum(|g_i|), dx = min(dx, dy[, dz]) */
+static inline double
+grav_invdt(const eko_solver * s, const double * q, double cs, long c)
+{
+  const eko_params * p = &s->p;
+  double dxm = fmin(p->dx, p->dy);
+  if (p->dim == 3)
+    dxm = fmin(dxm, p->dz);
+  double velocity = 0.0;
+  velocity += cs + fabs(q[EKO_IU]);
+  velocity += cs + fabs(q[EKO_IV]);
+  double kk = fabs(AT(s->G, s, 0, c)) + fabs(AT(s->G, s, 1, c));
+  if (p->dim == 3)
+  {
+    velocity += cs + fabs(q[EKO_IW]);
+    kk = kk + fabs(AT(s->G, s, 2, c));
+  }
+  kk *= p->cfl * dxm / (velocity * velocity);
+  kk = fmax(kk, 1e-4);
+  velocity *= kk / (sqrt(1.0 + 2.0 * kk) - 1.0);
+  return velocity / dxm;
+}
+
 /* ComputeDtFunctor2D/3D: HydroRunFunctors2D.h:18-88, HydroRunFunctors3D.h:16-87 */
 static double
 hydro_compute_dt_local(eko_solver * s, const double * U)
@@ -482,6 +508,11 @@ hydro_compute_dt_local(eko_solver * s, const double * U)
           for (int v = 0; v < p->nbvar; ++v)
             u[v] = AT(U, s, v, c);
           hydro_prims(u, q, &cs, dim, p);
+          if (p->grav_enabled)
+          {
+            local = fmax(local, grav_invdt(s, q, cs, c));
+            continue;
+          }
           double vx = cs + fabs(q[EKO_IU]);
           double vy = cs + fabs(q[EKO_IV]);
           if (dim == 2)
@@ -661,6 +692,15 @@ hydro_godunov(eko_solver * s, double * in, double * out, double dt)
           }
           hydro_trace(q, dqx, dqy, dqz, dtdx, dtdy, dtdz, 2 * d, qr, dim, p);
           hydro_trace(qn, dnx, dny, dnz, dtdx, dtdy, dtdz, 2 * d + 1, ql, dim, p);
+          if (p->grav_enabled && p->grav_hancock)
+          {
+            /* gravity predictor, half time step (HydroRunFunctors2D.h:656-665,
+             * HydroRunFunctors3D.h:489-500) */
+            for (int e = 0; e < dim; ++e)
+              ql[EKO_IU + e] += 0.5 * dt * AT(s->G, s, e, cn);
+            for (int e = 0; e < dim; ++e)
+              qr[EKO_IU + e] += 0.5 * dt * AT(s->G, s, e, c);
+          }
           int it = EKO_IU + d; /* normal velocity index */
           if (d > 0)
           {
@@ -698,6 +738,43 @@ hydro_godunov(eko_solver * s, double * in, double * out, double dt)
           AT(out, s, v, c) = u;
         }
       }
+
+  if (p->grav_enabled)
+  {
+    /* GravitySourceTermFunctor2D/3D (HydroRunFunctors2D.h:1555-1630,
+     * HydroRunFunctors3D.h:1903-1980); the 2D form floors the new density */
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = ku0; k < ku1; ++k)
+      for (int j = gw; j < js - gw; ++j)
+        for (int i = gw; i < is - gw; ++i)
+        {
+          long   c = IDX(s, i, j, k);
+          double rhoOld = AT(in, s, EKO_ID, c);
+          double rhoNew = dim == 2 ? fmax(p->smallr, AT(out, s, EKO_ID, c)) : AT(out, s, EKO_ID, c);
+          double rhou = AT(out, s, EKO_IU, c), rhov = AT(out, s, EKO_IV, c), rhow = 0.0;
+          double ekin_old, ekin_new;
+          if (dim == 2)
+            ekin_old = 0.5 * (rhou * rhou + rhov * rhov) / rhoNew;
+          else
+          {
+            rhow = AT(out, s, EKO_IW, c);
+            ekin_old = 0.5 * (rhou * rhou + rhov * rhov + rhow * rhow) / rhoNew;
+          }
+          rhou += 0.5 * dt * AT(s->G, s, 0, c) * (rhoOld + rhoNew);
+          rhov += 0.5 * dt * AT(s->G, s, 1, c) * (rhoOld + rhoNew);
+          AT(out, s, EKO_IU, c) = rhou;
+          AT(out, s, EKO_IV, c) = rhov;
+          if (dim == 2)
+            ekin_new = 0.5 * (rhou * rhou + rhov * rhov) / rhoNew;
+          else
+          {
+            rhow += 0.5 * dt * AT(s->G, s, 2, c) * (rhoOld + rhoNew);
+            AT(out, s, EKO_IW, c) = rhow;
+            ekin_new = 0.5 * (rhou * rhou + rhov * rhov + rhow * rhow) / rhoNew;
+          }
+          AT(out, s, EKO_IP, c) += (ekin_new - ekin_old);
+        }
+  }
 }
 
 /* ===================================================================== */
@@ -2072,6 +2149,15 @@ eko_create(const eko_params * p, const double * U0, double t0)
   s->U2 = zalloc(n * nb);
   s->Q = zalloc(n * nb);
   memcpy(s->U, U0, sizeof(double) * n * nb);
+  if (!p->mhd && p->grav_enabled)
+  {
+    /* the field the Rayleigh-Taylor init writes on every cell (ghosts
+     * included); zero for the other problems */
+    s->G = zalloc(n * p->dim);
+    for (int e = 0; e < p->dim; ++e)
+      for (long c = 0; c < n; ++c)
+        s->G[(long)e * n + c] = p->gravity[e];
+  }
   if (!p->mhd)
   {
     s->Fx = zalloc(n * nb);
@@ -2143,6 +2229,7 @@ eko_destroy(eko_solver * s)
   free(s->dB);
   free(s->dC);
   free(s->Emf);
+  free(s->G);
   for (int d = 0; d < 3; ++d)
   {
     free(s->Qm[d]);
@@ -2177,6 +2264,19 @@ eko_next_iteration(eko_solver * s)
   }
   s->iteration += 1;
   s->t += s->dt;
+  return 0;
+}
+
+int
+eko_set_gravity_field(eko_solver * s, const double * G)
+{
+  if (!s || !G || !s->G)
+    return -1;
+  memcpy(s->G, G, sizeof(double) * s->ncell * s->p.dim);
+  const double * cur = (s->iteration % 2 == 0) ? s->U : s->U2;
+  s->dt = hydro_compute_dt_local(s, cur);
+  if (s->t + s->dt > s->p.tEnd)
+    s->dt = s->p.tEnd - s->t;
   return 0;
 }
 

@@ -46,6 +46,12 @@ typedef struct eko_params
   double tEnd;
   int    nStepmax;
   double gamma6; /* (gamma0 + 1) / (2 gamma0), HydroParams.cpp:356 */
+  /* static gravity (hydro only; GravityParams.h:22-37) */
+  int    grav_enabled;  /* [gravity] enabled */
+  int    grav_hancock;  /* [gravity] hancock_predictor_enabled */
+  double gravity[3];    /* uniform field of the Rayleigh-Taylor init
+                           (HydroInitFunctors2D.h:735-771, HydroInitFunctors3D.h:806-842);
+                           0 for other problems (a zero-initialised VectorField) */
 } eko_params;
 
 typedef struct eko_solver eko_solver;
@@ -58,6 +64,10 @@ eko_solver * eko_create(const eko_params * p, const double * U0, double t0);
 void         eko_destroy(eko_solver * s);
 /* SolverBase::next_iteration (SolverBase.cpp:180-195); returns 0 on success */
 int          eko_next_iteration(eko_solver * s);
+/* Replace the gravity field (dim components over the full grid, layout
+ * G[((comp*ksize + k)*jsize + j)*isize + i]) and recompute m_dt as the
+ * constructor does; returns -1 when gravity is not enabled. */
+int          eko_set_gravity_field(eko_solver * s, const double * G);
 int          eko_finished(const eko_solver * s);
 void         eko_get_state(const eko_solver * s, double * U);
 double       eko_time(const eko_solver * s);

@@ -153,6 +153,9 @@ class eko_params(ctypes.Structure):
         ("tEnd", ctypes.c_double),
         ("nStepmax", ctypes.c_int),
         ("gamma6", ctypes.c_double),
+        ("grav_enabled", ctypes.c_int),
+        ("grav_hancock", ctypes.c_int),
+        ("gravity", ctypes.c_double * 3),
     ]
 
 
@@ -196,6 +199,9 @@ class Params:
     tEnd: float
     nStepmax: int
     problem: str
+    grav_enabled: bool = False
+    grav_hancock: bool = False
+    gravity: tuple = (0.0, 0.0, 0.0)
     extra: dict = field(default_factory=dict)
 
     def to_c(self) -> eko_params:
@@ -214,6 +220,9 @@ class Params:
         p.riemann = self.riemann
         p.tEnd, p.nStepmax = self.tEnd, self.nStepmax
         p.gamma6 = self.gamma6
+        p.grav_enabled, p.grav_hancock = int(self.grav_enabled), int(self.grav_hancock)
+        for i in range(3):
+            p.gravity[i] = self.gravity[i]
         return p
 
     @property
@@ -257,6 +266,14 @@ def params_from_ini(text: str) -> Params:
     smallp = smallc * smallc / gamma0
     smallpp = smallr * smallp
     gamma6 = (gamma0 + 1.0) / (2.0 * gamma0)
+    problem = get_string(cfg, "hydro", "problem", "unknown")
+    # GravityParams (shared/GravityParams.h:32-37); the field is the uniform
+    # one of the Rayleigh-Taylor init (RayleighTaylorInstabilityParams.h:28-34),
+    # zero for the other problems
+    gravity = (0.0, 0.0, 0.0)
+    if problem == "rayleigh_taylor":
+        gravity = (get_float(cfg, "rayleigh_taylor", "gx", 0.0), get_float(cfg, "rayleigh_taylor", "gy", -0.1),
+                   get_float(cfg, "rayleigh_taylor", "gz", 0.0) if dim == 3 else 0.0)
     return Params(
         solver_name=name, dim=dim, mhd=mhd, nx=nx, ny=ny, nz=nz, gw=gw, nbvar=nbvar,
         isize=isize, jsize=jsize, ksize=ksize, xmin=xmin, xmax=xmax, ymin=ymin, ymax=ymax,
@@ -265,7 +282,10 @@ def params_from_ini(text: str) -> Params:
         gamma6=gamma6, riemann=riemann,
         tEnd=get_float(cfg, "run", "tend", 0.0),
         nStepmax=get_integer(cfg, "run", "nstepmax", 1000),
-        problem=get_string(cfg, "hydro", "problem", "unknown"),
+        problem=problem,
+        grav_enabled=get_bool(cfg, "gravity", "enabled", False) and not mhd,
+        grav_hancock=get_bool(cfg, "gravity", "hancock_predictor_enabled", False),
+        gravity=gravity,
         extra=cfg,
     )
 
@@ -299,10 +319,12 @@ def read_ekst(path: str):
 
 
 def run_reference(ini_text: str, U0: np.ndarray, nsteps: int, workdir: str, fast: bool = False,
-                  threads: int | None = None, save: bool = False):
+                  threads: int | None = None, save: bool = False, gravity_field: np.ndarray | None = None):
     """Run the reference's own solver (oracle/_ref) on an injected state;
     save: also write the final state through the reference's output path
-    (save_solution, as the .ini's [output] section configures it)."""
+    (save_solution, as the .ini's [output] section configures it);
+    gravity_field: (dim, ksize, jsize, isize) array replacing the static
+    gravity field of a hydro run with [gravity] enabled."""
     exe = REF_RUN_FAST if fast else REF_RUN
     if not os.path.exists(exe):
         raise FileNotFoundError(exe)
@@ -320,6 +342,10 @@ def run_reference(ini_text: str, U0: np.ndarray, nsteps: int, workdir: str, fast
         env["OMP_NUM_THREADS"] = str(threads)
     if save:
         env["EK_REF_SAVE"] = "1"
+    if gravity_field is not None:
+        gpath = os.path.join(workdir, "gravity.ekst")
+        write_ekst(gpath, gravity_field, p.dim, p.gw)
+        env["EK_REF_GRAVITY"] = gpath
     subprocess.run([exe, ini, str(nsteps), out, u0], check=True, cwd=workdir, env=env,
                    stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
     return read_ekst(out)
@@ -348,6 +374,8 @@ def lib():
         L.eko_dt.argtypes = [ctypes.c_void_p]
         L.eko_dt.restype = ctypes.c_double
         L.eko_iteration.argtypes = [ctypes.c_void_p]
+        L.eko_set_gravity_field.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.eko_set_gravity_field.restype = ctypes.c_int
         L.eko_num_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -356,7 +384,7 @@ def lib():
 class Oracle:
     """One oracle run: create on an injected state, step, read back."""
 
-    def __init__(self, params: Params, U0: np.ndarray, t0: float = 0.0):
+    def __init__(self, params: Params, U0: np.ndarray, t0: float = 0.0, gravity_field: np.ndarray | None = None):
         self.params = params
         self._cp = params.to_c()
         U0 = np.ascontiguousarray(U0, dtype=np.float64)
@@ -364,6 +392,11 @@ class Oracle:
         self._h = lib().eko_create(ctypes.byref(self._cp), U0.ctypes.data, t0)
         if not self._h:
             raise ValueError("oracle does not support this configuration")
+        if gravity_field is not None:
+            G = np.ascontiguousarray(gravity_field, dtype=np.float64)
+            assert G.shape == (params.dim,) + params.shape[1:], G.shape
+            if lib().eko_set_gravity_field(self._h, G.ctypes.data) != 0:
+                raise ValueError("gravity is not enabled in these parameters")
 
     def close(self):
         if self._h:

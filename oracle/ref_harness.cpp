@@ -12,6 +12,7 @@
 //   * a dump of the final state and of the dt sequence in the EKST format.
 //
 // usage: ref_run <file.ini> <nsteps> <out.ekst> [<U0.ekst>]
+// (environment: EK_REF_SAVE, EK_REF_GRAVITY -- see run())
 //
 // EKST format (little endian): char magic[8]="EKSTATE1"; int64 dim, nbvar,
 // isize, jsize, ksize, ghost, iteration, ndt; double t; double dt[ndt];
@@ -107,6 +108,30 @@ run(Solver * s, euler_kokkos::HydroParams & p, int nsteps, const char * out, con
       return 2;
     std::fclose(f);
     copy_in(s->U, buf, dim, nb, is, js, ks);
+    // EK_REF_GRAVITY=<file.ekst> (nbvar = dim): replaces the static gravity
+    // field the constructor's init left (SolverHydroMuscl.h:86-87, 228-231)
+    if constexpr (std::is_same<Solver, muscl::SolverHydroMuscl<2>>::value ||
+                  std::is_same<Solver, muscl::SolverHydroMuscl<3>>::value)
+    {
+      const char * gpath = std::getenv("EK_REF_GRAVITY");
+      if (gpath && gpath[0])
+      {
+        FILE * g = std::fopen(gpath, "rb");
+        EkHeader gh;
+        if (!g || std::fread(&gh, sizeof gh, 1, g) != 1 || gh.nbvar != dim || gh.isize != is ||
+            gh.jsize != js || gh.ksize != ks || s->gravity_field.size() == 0)
+        {
+          std::fprintf(stderr, "bad gravity field %s\n", gpath);
+          return 2;
+        }
+        std::fseek(g, (long)(sizeof gh + sizeof(double) * gh.ndt), SEEK_SET);
+        std::vector<double> gbuf((size_t)is * js * ks * dim);
+        if (std::fread(gbuf.data(), sizeof(double), gbuf.size(), g) != gbuf.size())
+          return 2;
+        std::fclose(g);
+        copy_in(s->gravity_field, gbuf, dim, dim, is, js, ks);
+      }
+    }
     // replay the constructor tail on the injected state
     s->make_boundaries(s->U);
     Kokkos::deep_copy(s->U2, s->U);

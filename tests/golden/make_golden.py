@@ -68,7 +68,36 @@ CASES = {
     "ot3d_llf": (lambda: P.orszag_tang_3d(n=10, nsteps=4, riemann="llf"), 4),
     "ot2d_hll": (lambda: P.orszag_tang_2d(n=20, nsteps=6, riemann="hll"), 6),
     "ot2d_llf": (lambda: P.orszag_tang_2d(n=20, nsteps=6, riemann="llf"), 6),
+    # static gravity (Rayleigh-Taylor decks; the reference's init sets the
+    # uniform field): CFL with gravity, source term, Hancock predictor
+    "rt2d_approx": (lambda: P.rayleigh_taylor(dim=2, nx=16, nsteps=12, noise=0.01), 12),
+    "rt2d_hllc_hancock": (lambda: P.rayleigh_taylor(dim=2, nx=12, ny=30, nsteps=10, riemann="hllc", hancock=True,
+                                                    noise=0.02, slope_type=1.0, g=-1.0), 10),
+    "rt3d_approx": (lambda: P.rayleigh_taylor(dim=3, nx=6, nsteps=6, noise=0.01), 6),
+    "rt3d_hllc_hancock": (lambda: P.rayleigh_taylor(dim=3, nx=8, ny=6, nz=16, nsteps=5, riemann="hllc",
+                                                    hancock=True, noise=0.02, g=-1.0), 5),
+    # a non-uniform field (builder returns the field too; the harness loads
+    # it into the reference solver's gravity_field)
+    "grav2d_field_llf": (lambda: _with_field(P.rayleigh_taylor(dim=2, nx=14, ny=20, nsteps=8, riemann="llf",
+                                                               hancock=True, noise=0.02), 31), 8),
+    "grav3d_field_hllc": (lambda: _with_field(P.rayleigh_taylor(dim=3, nx=6, ny=8, nz=10, nsteps=5,
+                                                                riemann="hllc", hancock=True, noise=0.02), 32), 5),
 }
+
+
+def _with_field(case, seed):
+    """(ini, U0) -> (ini, U0, G): a seeded smooth gravity field, one
+    component per dimension, on every cell (ghosts included)."""
+    ini, U0 = case
+    dim = 3 if U0.shape[1] > 1 else 2
+    rng = np.random.default_rng(seed)
+    shp = U0.shape[1:]
+    k, j, i = np.meshgrid(*[np.arange(n, dtype=np.float64) for n in shp], indexing="ij")
+    G = np.empty((dim,) + shp)
+    for c in range(dim):
+        a = rng.uniform(0.2, 1.0, 4)
+        G[c] = a[0] * np.sin(0.4 * i + a[1]) * np.cos(0.3 * j + a[2]) * np.cos(0.5 * k + a[3]) - 0.3
+    return ini, U0, G
 
 
 # VTK output parity: the reference writes the final state of these cases with
@@ -120,11 +149,14 @@ def main():
     make_vtk([n for n in names if n in VTK_CASES])
     for name in [n for n in names if n in CASES]:
         build, nsteps = CASES[name]
-        ini, U0 = build()
-        res = eko.run_reference(ini, U0, nsteps, os.path.join(work, name))
+        case = build()
+        ini, U0 = case[:2]
+        G = case[2] if len(case) > 2 else None
+        res = eko.run_reference(ini, U0, nsteps, os.path.join(work, name), gravity_field=G)
+        extra = {} if G is None else {"G": G}
         np.savez_compressed(os.path.join(out_dir, name + ".npz"), ini=np.array(ini), U0=U0,
                             U=res["U"], dts=res["dts"], t=np.array(res["t"]),
-                            iteration=np.array(res["iteration"]))
+                            iteration=np.array(res["iteration"]), **extra)
         print(name, U0.shape, "steps", len(res["dts"]), "nan", int(np.isnan(res["U"]).sum()))
 
 

@@ -18,7 +18,7 @@ from helpers import golden_cases, interior, load_golden
 def test_oracle_matches_reference_bitwise(name):
     g = load_golden(name)
     p = eko.params_from_ini(str(g["ini"]))
-    o = eko.Oracle(p, g["U0"])
+    o = eko.Oracle(p, g["U0"], gravity_field=g.get("G"))
     dts = o.run(len(g["dts"]))
     assert np.array_equal(dts, g["dts"], equal_nan=True)
     U = o.state()
