@@ -67,6 +67,9 @@ class Params(ctypes.Structure):
         ("solver_name_", ctypes.c_char * 32), ("problem_", ctypes.c_char * 32),
         ("output_dir_", ctypes.c_char * 256), ("output_prefix_", ctypes.c_char * 128),
         ("vtk_enabled", ctypes.c_int), ("vtk_ascii", ctypes.c_int),
+        ("gravity_enabled", ctypes.c_int), ("gravity_static", ctypes.c_int),
+        ("gravity_hancock", ctypes.c_int), ("gravity_well_balanced", ctypes.c_int),
+        ("gravity", ctypes.c_double * 3),
     ]
 
     @property
@@ -138,6 +141,7 @@ def load_library():
         "ek_solver_destroy": (ctypes.c_int, [c_p]),
         "ek_solver_set_state": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
         "ek_solver_get_state": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
+        "ek_solver_set_gravity_field": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
         "ek_solver_compute_dt": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_double)]),
         "ek_solver_next_iteration": (ctypes.c_int, [c_p]),
         "ek_solver_run": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
@@ -260,6 +264,19 @@ class Solver:
         U = np.empty(shp if layout == EK_LAYOUT_LEFT else shp[::-1], dtype=np.float64)
         _check(self._L.ek_solver_get_state(self._h, U.ctypes.data, layout), "get_state")
         return U
+
+    def set_gravity_field(self, G, layout: int = EK_LAYOUT_LEFT):
+        """Static gravity field (hydro, [gravity] enabled): shape (dim, ksize,
+        jsize, isize) for LayoutLeft, (isize, jsize, ksize, dim) for
+        LayoutRight; None returns to the uniform params.gravity."""
+        if G is None:
+            _check(self._L.ek_solver_set_gravity_field(self._h, None, layout), "set_gravity_field")
+            return
+        G = np.ascontiguousarray(G, dtype=np.float64)
+        want = self.params.dim * int(np.prod(self.params.shape[1:]))
+        if G.size != want:
+            raise ValueError("gravity field has %d values, expected %d" % (G.size, want))
+        _check(self._L.ek_solver_set_gravity_field(self._h, G.ctypes.data, layout), "set_gravity_field")
 
     # -- SolverBase --------------------------------------------------------
     def compute_dt(self) -> float:

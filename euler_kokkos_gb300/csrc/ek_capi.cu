@@ -52,6 +52,7 @@ struct ek_solver
   double *      dtlog = nullptr;
   int           dtcap = 0;
   double *      scratch3 = nullptr; // device totals
+  void *        gfield = nullptr;   // static gravity field (state precision), if set
   cudaStream_t  stream = nullptr;
   int           device = 0;
   // host mirror of SolverBase state
@@ -230,6 +231,22 @@ make_kparams(const ek_params & p)
   k.smallpp = p.smallpp;
   k.gamma6f = (float)p.gamma6;
   k.smallppf = (float)p.smallpp;
+  // static gravity: hydro only (SolverMHDMuscl has no gravity terms)
+  k.grav = (!p.mhd && p.gravity_enabled) ? 1 : 0;
+  k.grav_hancock = k.grav && p.gravity_hancock ? 1 : 0;
+  for (int e = 0; e < 3; ++e)
+  {
+    k.g[e] = (e < p.dim) ? p.gravity[e] : 0.0;
+    k.gf[e] = (float)k.g[e];
+  }
+  // ComputeDtGravityFunctor: dx = fmin(dx, dy) [, fmin(dx, dz)]
+  k.dxmin = std::fmin(p.dx, p.dy);
+  if (p.dim == 3)
+    k.dxmin = std::fmin(k.dxmin, p.dz);
+  k.cfl_dxmin = p.cfl * k.dxmin;
+  k.cfl_dxminf = (float)k.cfl_dxmin;
+  k.idxminf = (float)(1.0 / k.dxmin);
+  k.gfield = nullptr;
   return k;
 }
 
@@ -320,6 +337,7 @@ ek_solver_destroy(ek_solver * s)
   cudaFree(s->clk);
   cudaFree(s->dtlog);
   cudaFree(s->scratch3);
+  cudaFree(s->gfield);
   drain_events(s);
   for (auto e : s->ev_pool)
     cudaEventDestroy(e);
@@ -518,6 +536,67 @@ set_state_at(ek_solver * s, const double * U, int layout, double t0)
   // m_dt after the constructor
   double dt = 0.0;
   return ek_solver_compute_dt(s, &dt);
+}
+
+extern "C" ek_status
+ek_solver_set_gravity_field(ek_solver * s, const double * G, int layout)
+{
+  if (!s || (layout != EK_LAYOUT_LEFT && layout != EK_LAYOUT_RIGHT))
+    return fail(EK_ERR_INVALID, "ek_solver_set_gravity_field: bad argument");
+  if (!s->kp.grav)
+    return fail(EK_ERR_INVALID, "ek_solver_set_gravity_field: gravity is not enabled (hydro solvers, "
+                                "[gravity] enabled)");
+  EK_CUDA(cudaSetDevice(s->device), "cudaSetDevice");
+  const int       dim = s->p.dim, is = s->kp.isize, js = s->kp.jsize, ks = s->kp.ksize;
+  const long long n = s->kp.vstride;
+  if (!G)
+  {
+    // back to the uniform field of the parameters
+    EK_CUDA(cudaStreamSynchronize(s->stream), "gravity field");
+    cudaFree(s->gfield);
+    s->gfield = nullptr;
+  }
+  else
+  {
+    // device copy in the state's precision, LayoutLeft, one plane per component
+    const size_t es = s->prec == EK_PREC_FP64 ? sizeof(double) : sizeof(float);
+    if (!s->gfield)
+      EK_CUDA(cudaMalloc(&s->gfield, es * (size_t)n * dim), "gravity field");
+    std::vector<double> h((size_t)n * dim);
+    if (layout == EK_LAYOUT_LEFT)
+      std::memcpy(h.data(), G, sizeof(double) * h.size());
+    else
+      for (int i = 0; i < is; ++i)
+        for (int j = 0; j < js; ++j)
+          for (int k = 0; k < ks; ++k)
+            for (int c = 0; c < dim; ++c)
+              h[(size_t)c * n + ((size_t)k * js + j) * is + i] = G[(((size_t)i * js + j) * ks + k) * dim + c];
+    if (s->prec == EK_PREC_FP64)
+      EK_CUDA(cudaMemcpyAsync(s->gfield, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s->stream),
+              "gravity field");
+    else
+    {
+      std::vector<float> f(h.size());
+      for (size_t i = 0; i < f.size(); ++i)
+        f[i] = (float)h[i];
+      EK_CUDA(cudaMemcpyAsync(s->gfield, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice, s->stream),
+              "gravity field");
+      EK_CUDA(cudaStreamSynchronize(s->stream), "gravity field");
+    }
+    EK_CUDA(cudaStreamSynchronize(s->stream), "gravity field");
+  }
+  s->kp.gfield = s->gfield;
+  if (!s->has_state)
+    return EK_OK;
+  // the CFL candidate of the current step, with the new field
+  const int          slot = s->iteration % 3;
+  unsigned long long low = EK_KEY_LOWEST;
+  EK_CUDA(cudaMemcpyAsync(&s->clk->key[slot], &low, sizeof low, cudaMemcpyHostToDevice, s->stream), "gravity dt");
+  ek_status st = launch_dt(s, s->U[s->iteration % 2], &s->clk->key[slot]);
+  if (st != EK_OK)
+    return st;
+  EK_CUDA(cudaStreamSynchronize(s->stream), "gravity dt");
+  return ek_solver_compute_dt(s, nullptr);
 }
 
 extern "C" ek_status
@@ -958,6 +1037,8 @@ ek_ensemble_create(const ek_params * params, int n, ek_ensemble ** out)
       return fail(EK_ERR_UNSUPPORTED, "ensembles hold Hydro_Muscl_2D runs");
     if (p.riemann != 3)
       return fail(EK_ERR_UNSUPPORTED, "ensembles use riemann=hllc");
+    if (p.gravity_enabled)
+      return fail(EK_ERR_UNSUPPORTED, "ensembles run without gravity");
     if (p.precision != params[0].precision || p.exact_fp != params[0].exact_fp)
       return fail(EK_ERR_INVALID, "all instances of an ensemble share precision and exact_fp");
   }

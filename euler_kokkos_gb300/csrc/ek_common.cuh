@@ -60,6 +60,16 @@ struct KParams
   int       mhd_stage;     // MHD update: stage the trace planes in shared memory
   double    gamma6, smallpp; // riemann_approx constants (HydroParams.cpp:353-356)
   float     gamma6f, smallppf;
+  // static gravity (hydro; GravityParams.h:22-37): the field is gfield
+  // (dim planes of the state's precision over the full grid) when set,
+  // else the uniform vector g
+  int          grav;         // source term + gravity CFL
+  int          grav_hancock; // Hancock predictor of the face states
+  double       g[3];
+  float        gf[3];
+  double       cfl_dxmin, dxmin; // cfl * min(dx, dy[, dz]) and min(dx, dy[, dz])
+  float        cfl_dxminf, idxminf;
+  const void * gfield;
 };
 
 // Per-step scalars kept on the device so that consecutive steps need no host

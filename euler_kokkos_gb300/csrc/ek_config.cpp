@@ -228,6 +228,20 @@ ek_params_from_ini(const char * text, size_t len, ek_params * out)
   p.vtk_enabled = get_bool(ini, "output", "vtk_enabled", true) ? 1 : 0;
   p.vtk_ascii = get_bool(ini, "output", "outputVtkAscii", false) ? 1 : 0;
 
+  // [gravity]: GravityParams (GravityParams.h:32-37), SolverBase.cpp:38; the
+  // field is the Rayleigh-Taylor init's uniform one
+  // (RayleighTaylorInstabilityParams.h:28-34), zero for the other problems
+  p.gravity_enabled = get_bool(ini, "gravity", "enabled", false) ? 1 : 0;
+  p.gravity_static = get_bool(ini, "gravity", "static", false) ? 1 : 0;
+  p.gravity_hancock = get_bool(ini, "gravity", "hancock_predictor_enabled", false) ? 1 : 0;
+  p.gravity_well_balanced = get_bool(ini, "gravity", "well_balanced_reconstruction_enabled", false) ? 1 : 0;
+  if (prob == "rayleigh_taylor")
+  {
+    p.gravity[0] = get_float(ini, "rayleigh_taylor", "gx", 0.0f);
+    p.gravity[1] = get_float(ini, "rayleigh_taylor", "gy", -0.1f);
+    p.gravity[2] = p.dim == 3 ? get_float(ini, "rayleigh_taylor", "gz", 0.0f) : 0.0;
+  }
+
   // additions of this library, in a section the reference does not read
   std::string prec = lower(get_string(ini, "gb300", "precision", "fp64"));
   p.precision = (prec == "mixed" || prec == "fp32") ? EK_PREC_MIXED : EK_PREC_FP64;

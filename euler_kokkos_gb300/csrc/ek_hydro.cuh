@@ -468,4 +468,139 @@ hydro_invdt(const R (&u)[NV], const HydroConst<R> & C, const KParams & P)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Static gravity (SolverHydroMuscl with [gravity] enabled)
+// ---------------------------------------------------------------------------
+
+// gravity vector of cell (i, j, k) in raw array indexes (ghosts included;
+// the field is read as stored, not mapped through the boundary conditions).
+// Indexes past the array (cells of partial tiles, whose results are
+// discarded) are clamped.
+template <class S, class R, int NV>
+__device__ __forceinline__ void
+grav_at(const KParams & P, int i, int j, int k, R (&g)[3])
+{
+  if (P.gfield)
+  {
+    i = min(max(i, 0), P.isize - 1);
+    j = min(max(j, 0), P.jsize - 1);
+    k = min(max(k, 0), P.ksize - 1);
+    const S *       G = (const S *)P.gfield;
+    const long long off = (long long)k * P.plane + (long long)j * P.isize + i;
+    g[0] = (R)ldg(G + off);
+    g[1] = (R)ldg(G + P.vstride + off);
+    g[2] = NV == 5 ? (R)ldg(G + 2 * P.vstride + off) : R(0);
+  }
+  else if constexpr (sizeof(R) == 8)
+  {
+    g[0] = P.g[0], g[1] = P.g[1], g[2] = P.g[2];
+  }
+  else
+  {
+    g[0] = P.gf[0], g[1] = P.gf[1], g[2] = P.gf[2];
+  }
+}
+
+// Hancock gravity predictor of one face state: q += (dt/2) g of the cell the
+// state was traced from, on the velocity components in the cell's own frame
+// (before any IU/IV/IW swap; HydroRunFunctors2D.h:656-665,
+// HydroRunFunctors3D.h:489-500).  hg = (0.5 dt) g.
+template <class R, int NV>
+__device__ __forceinline__ void
+grav_kick(R (&q)[NV], const R (&hg)[3])
+{
+  q[IU] += hg[0];
+  q[IV] += hg[1];
+  if constexpr (NV == 5)
+    q[IW] += hg[2];
+}
+
+// GravitySourceTermFunctor2D/3D (HydroRunFunctors2D.h:1555-1630,
+// HydroRunFunctors3D.h:1903-1980) on the updated state u of one cell:
+// momentum += (dt/2) g (rho_old + rho_new), energy += the kinetic energy
+// change; the 2D form floors rho_new at smallr.  FP64 keeps the reference's
+// expression (ekin_new - ekin_old); FP32 uses the equal form
+// sum du (m + du/2) / rho_new, which has no cancellation.
+template <class R, int NV>
+__device__ __forceinline__ void
+grav_source(R (&u)[NV], R rho_old, const R (&g)[3], R hdt, const HydroConst<R> & C)
+{
+  const R rn = NV == 4 ? fmax(C.smallr, u[ID]) : u[ID];
+  if constexpr (sizeof(R) == 8)
+  {
+    R ru = u[IU], rv = u[IV];
+    if constexpr (NV == 4)
+    {
+      const R ek0 = R(0.5) * (ru * ru + rv * rv) / rn;
+      ru += hdt * g[0] * (rho_old + rn);
+      rv += hdt * g[1] * (rho_old + rn);
+      u[IU] = ru;
+      u[IV] = rv;
+      const R ek1 = R(0.5) * (ru * ru + rv * rv) / rn;
+      u[IP] += (ek1 - ek0);
+    }
+    else
+    {
+      R       rw = u[IW];
+      const R ek0 = R(0.5) * (ru * ru + rv * rv + rw * rw) / rn;
+      ru += hdt * g[0] * (rho_old + rn);
+      rv += hdt * g[1] * (rho_old + rn);
+      rw += hdt * g[2] * (rho_old + rn);
+      u[IU] = ru;
+      u[IV] = rv;
+      u[IW] = rw;
+      const R ek1 = R(0.5) * (ru * ru + rv * rv + rw * rw) / rn;
+      u[IP] += (ek1 - ek0);
+    }
+  }
+  else
+  {
+    const R rs = rho_old + rn;
+    R       de = R(0);
+#pragma unroll
+    for (int e = 0; e < NV - 2; ++e)
+    {
+      const R du = hdt * g[e] * rs;
+      de += du * (u[IU + e] + R(0.5) * du);
+      u[IU + e] += du;
+    }
+    u[IP] += de * rcp_a(rn);
+  }
+}
+
+// per-cell CFL candidate of ComputeDtGravityFunctor2D/3D
+// (HydroRunFunctors2D.h:125-170, HydroRunFunctors3D.h:133-184):
+// g dt^2 / (2 dx) + u dt / dx <= cfl, u = sum(|v_i| + c), g = sum(|g_i|),
+// dx = min(dx, dy[, dz]).  FP64 keeps the reference's expression; FP32 writes
+// the correction factor kk / (sqrt(1 + 2 kk) - 1) as (sqrt(1 + 2 kk) + 1) / 2,
+// equal without the cancellation.
+template <class R, int NV>
+__device__ __forceinline__ R
+hydro_invdt_grav(const R (&u)[NV], const R (&g)[3], const HydroConst<R> & C, const KParams & P)
+{
+  R q[NV];
+  hydro_prims<R, NV>(u, q, C);
+  const R c = hydro_sound<R>(q[ID], q[IP], C);
+  R       velocity = c + fabs(q[IU]);
+  velocity += c + fabs(q[IV]);
+  R kk = fabs(g[0]) + fabs(g[1]);
+  if constexpr (NV == 5)
+  {
+    velocity += c + fabs(q[IW]);
+    kk = kk + fabs(g[2]);
+  }
+  if constexpr (sizeof(R) == 8)
+  {
+    kk *= P.cfl_dxmin / (velocity * velocity);
+    kk = fmax(kk, 1e-4);
+    velocity *= kk / (sqrt(1.0 + 2.0 * kk) - 1.0);
+    return velocity / P.dxmin;
+  }
+  else
+  {
+    kk = fmax(kk * P.cfl_dxminf * rcp_a(velocity * velocity), 1e-4f);
+    return velocity * (R(0.5) * (sqrt_a(R(1) + R(2) * kk) + R(1))) * P.idxminf;
+  }
+}
+
 } // namespace EK_NS

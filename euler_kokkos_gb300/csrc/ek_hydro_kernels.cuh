@@ -105,7 +105,7 @@ cell_slopes(const R * q0, const R * qm, const R * qp, int hx, int hy, R st, R (&
 // 2D: one CTA = one TX x TY tile of interior cells.  hydro2d_tile is the tile
 // body shared by the single-solver kernel and the ensemble kernel.
 // ---------------------------------------------------------------------------
-template <class S, class R, int TX, int TY, int RS = 3>
+template <class S, class R, int TX, int TY, int RS = 3, bool GRAV = false>
 __device__ __forceinline__ void
 hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & P, DevClock * clk,
              int step, int bx, int by, unsigned char * smem_raw)
@@ -124,6 +124,16 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
   const double        t = sc.t, dt = sc.dt;
   const R             dtdx = sc.dtdx, dtdy = sc.dtdy;
   const HydroConst<R> C = hydro_const<R>(P);
+  const R             hdt = (R)(0.5 * dt);
+  const bool          kick = GRAV && P.grav_hancock; // gravity predictor of the face states
+  // (dt/2) g of tile cell (cx, cy), for the predictor
+  auto half_g = [&](int cx, int cy, R (&hg)[3]) {
+    R g[3];
+    grav_at<S, R, NV>(P, P.gw + bx * TX + cx, P.gw + by * TY + cy, 0, g);
+#pragma unroll
+    for (int e = 0; e < 3; ++e)
+      hg[e] = hdt * g[e];
+  };
 
   const int gi0 = P.gw + bx * TX, gj0 = P.gw + by * TY;
   load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, 0, sQ);
@@ -135,19 +145,30 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
     R c[NV], dX[NV], dY[NV], dZ[NV], s[NV], f[NV];
     cell_slopes<R, NV, HX, HY>(sQ, sQ, sQ, tx + 2, ty + 2, C.slope_type, c, dX, dY, dZ, false);
     hydro_sources<R, NV>(c, dX, dY, dZ, s, C);
+    R hg[3];
+    if (kick)
+      half_g(tx, ty, hg);
     hydro_face<R, NV>(c, dX, s, dtdx, false, f, C.smallr);
+    if (kick)
+      grav_kick<R, NV>(f, hg);
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       sXm[(v * TY + ty) * FX + tx + 1] = f[v];
     hydro_face<R, NV>(c, dX, s, dtdx, true, f, C.smallr);
+    if (kick)
+      grav_kick<R, NV>(f, hg);
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       sXp[(v * TY + ty) * FX + tx + 1] = f[v];
     hydro_face<R, NV>(c, dY, s, dtdy, false, f, C.smallr);
+    if (kick)
+      grav_kick<R, NV>(f, hg);
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       sYm[(v * (TY + 2) + ty + 1) * TX + tx] = f[v];
     hydro_face<R, NV>(c, dY, s, dtdy, true, f, C.smallr);
+    if (kick)
+      grav_kick<R, NV>(f, hg);
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       sYp[(v * (TY + 2) + ty + 1) * TX + tx] = f[v];
@@ -175,9 +196,14 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
     R c[NV], dX[NV], dY[NV], dZ[NV], s[NV], f[NV];
     cell_slopes<R, NV, HX, HY>(sQ, sQ, sQ, cx + 2, cy + 2, C.slope_type, c, dX, dY, dZ, false);
     hydro_sources<R, NV>(c, dX, dY, dZ, s, C);
+    R hg[3];
+    if (kick)
+      half_g(cx, cy, hg);
     if (kind < 2)
     {
       hydro_face<R, NV>(c, dX, s, dtdx, kind == 0, f, C.smallr);
+      if (kick)
+        grav_kick<R, NV>(f, hg);
       R * dst = kind == 0 ? sXp : sXm;
 #pragma unroll
       for (int v = 0; v < NV; ++v)
@@ -186,6 +212,8 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
     else
     {
       hydro_face<R, NV>(c, dY, s, dtdy, kind == 2, f, C.smallr);
+      if (kick)
+        grav_kick<R, NV>(f, hg);
       R * dst = kind == 2 ? sYp : sYm;
 #pragma unroll
       for (int v = 0; v < NV; ++v)
@@ -244,36 +272,50 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
   if (gi < P.nx + P.gw && gj < P.ny + P.gw)
   {
     const long long off = (long long)gj * P.isize + gi;
-    R               u[NV];
+    R               u[NV], rho_old = R(0);
 #pragma unroll
     for (int v = 0; v < NV; ++v)
     {
       R x = (R)ldg(Uin + v * P.vstride + off);
+      if (v == ID)
+        rho_old = x;
       x += sXm[(v * TY + ty) * FX + tx + 1];
       x -= sXm[(v * TY + ty) * FX + tx + 2];
       x += sYm[(v * (TY + 2) + ty + 1) * TX + tx];
       x -= sYm[(v * (TY + 2) + ty + 2) * TX + tx];
       u[v] = x;
-      Uout[v * P.vstride + off] = (S)x;
+    }
+    R g[3];
+    if constexpr (GRAV)
+    {
+      // gravity source term after the flux update (SolverHydroMuscl.cpp:245-252)
+      grav_at<S, R, NV>(P, gi, gj, 0, g);
+      grav_source<R, NV>(u, rho_old, g, hdt, C);
     }
     // the next step's dt is computed on the stored (possibly rounded) state
     R us[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v)
+    {
+      Uout[v * P.vstride + off] = (S)u[v];
       us[v] = (R)(S)u[v];
-    tmax = fmax(tmax, hydro_invdt<R, NV>(us, C, P));
+    }
+    if constexpr (GRAV)
+      tmax = fmax(tmax, hydro_invdt_grav<R, NV>(us, g, C, P));
+    else
+      tmax = fmax(tmax, hydro_invdt<R, NV>(us, C, P));
   }
   block_max_commit<NT>(cand_key((double)tmax), &clk->key[(step + 1) % 3]);
   if (bx == 0 && by == 0 && threadIdx.x == 0)
     step_commit(clk, step, t, dt);
 }
 
-template <class S, class R, int TX, int TY, int RS>
+template <class S, class R, int TX, int TY, int RS, bool GRAV>
 __global__ void __launch_bounds__(TX * TY)
 hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  hydro2d_tile<S, R, TX, TY, RS>(Uin, Uout, P, clk, step, blockIdx.x, blockIdx.y, smem_raw);
+  hydro2d_tile<S, R, TX, TY, RS, GRAV>(Uin, Uout, P, clk, step, blockIdx.x, blockIdx.y, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -337,7 +379,7 @@ ensemble_totals_kernel(const EnsInstance * __restrict__ insts, const int * __res
 // ---------------------------------------------------------------------------
 // 3D: one CTA = a TX x TY column of interior cells marching over kchunk planes
 // ---------------------------------------------------------------------------
-template <class S, class R, int TX, int TY, int RS>
+template <class S, class R, int TX, int TY, int RS, bool GRAV>
 __global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_H3_MINB_F32, EK_H3_MINB_F64))
 hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
 {
@@ -357,6 +399,8 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   const double        t = sc.t, dt = sc.dt;
   const R             dtdx = sc.dtdx, dtdy = sc.dtdy, dtdz = sc.dtdz;
   const HydroConst<R> C = hydro_const<R>(P);
+  const R             hdt = (R)(0.5 * dt);
+  const bool          kick = GRAV && P.grav_hancock; // gravity predictor of the face states
 
   const int gw = P.gw;
   const int gi0 = gw + blockIdx.x * TX, gj0 = gw + blockIdx.y * TY;
@@ -379,7 +423,16 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
 
   R zmax_prev[NV];        // ZMAX face state of the cell below
   R acc[NV];              // partial update of the cell below, waiting for -Fz(k)
+  R rho_prev = R(0);      // its density before the update (gravity source term)
   R tmax = R(-INFINITY);  // CFL candidate max of the cells this thread wrote
+  // (dt/2) g of the cell at raw indexes (i, j, k), for the predictor
+  auto half_g = [&](int i, int j, int k, R (&hg)[3]) {
+    R g[3];
+    grav_at<S, R, NV>(P, i, j, k, g);
+#pragma unroll
+    for (int e = 0; e < 3; ++e)
+      hg[e] = hdt * g[e];
+  };
 
   for (int kc = k0 - 1; kc <= k1; ++kc)
   {
@@ -397,21 +450,32 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
       R c[NV], dX[NV], dY[NV], dZ[NV], s[NV], f[NV];
       cell_slopes<R, NV, HX, HY>(q0, qm, qp, tx + 2, ty + 2, C.slope_type, c, dX, dY, dZ, true);
       hydro_sources<R, NV>(c, dX, dY, dZ, s, C);
+      R hg[3];
+      if (kick)
+        half_g(gi, gj, kc + gw, hg);
       if (full)
       {
         hydro_face<R, NV>(c, dX, s, dtdx, false, f, C.smallr);
+        if (kick)
+          grav_kick<R, NV>(f, hg);
 #pragma unroll
         for (int v = 0; v < NV; ++v)
           sXm[(v * TY + ty) * FX + tx + 1] = f[v];
         hydro_face<R, NV>(c, dX, s, dtdx, true, f, C.smallr);
+        if (kick)
+          grav_kick<R, NV>(f, hg);
 #pragma unroll
         for (int v = 0; v < NV; ++v)
           sXp[(v * TY + ty) * FX + tx + 1] = f[v];
         hydro_face<R, NV>(c, dY, s, dtdy, false, f, C.smallr);
+        if (kick)
+          grav_kick<R, NV>(f, hg);
 #pragma unroll
         for (int v = 0; v < NV; ++v)
           sYm[(v * (TY + 2) + ty + 1) * TX + tx] = f[v];
         hydro_face<R, NV>(c, dY, s, dtdy, true, f, C.smallr);
+        if (kick)
+          grav_kick<R, NV>(f, hg);
 #pragma unroll
         for (int v = 0; v < NV; ++v)
           sYp[(v * (TY + 2) + ty + 1) * TX + tx] = f[v];
@@ -422,6 +486,8 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
         // (HydroRunFunctors3D.h:672-707)
         R qr[NV];
         hydro_face<R, NV>(c, dZ, s, dtdz, false, qr, C.smallr);
+        if (kick)
+          grav_kick<R, NV>(qr, hg);
         R ql[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v)
@@ -441,7 +507,11 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
           fz[v] = fz[v] * dtdz;
       }
       if (kc < k1)
+      {
         hydro_face<R, NV>(c, dZ, s, dtdz, true, zmax_prev, C.smallr);
+        if (kick)
+          grav_kick<R, NV>(zmax_prev, hg);
+      }
     }
     if (full)
     {
@@ -467,9 +537,14 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
         R c[NV], dX[NV], dY[NV], dZ[NV], s[NV], f[NV];
         cell_slopes<R, NV, HX, HY>(q0, qm, qp, cx + 2, cy + 2, C.slope_type, c, dX, dY, dZ, true);
         hydro_sources<R, NV>(c, dX, dY, dZ, s, C);
+        R hg[3];
+        if (kick)
+          half_g(gi0 + cx, gj0 + cy, kc + gw, hg);
         if (kind < 2)
         {
           hydro_face<R, NV>(c, dX, s, dtdx, kind == 0, f, C.smallr);
+          if (kick)
+            grav_kick<R, NV>(f, hg);
           R * dst = kind == 0 ? sXp : sXm;
 #pragma unroll
           for (int v = 0; v < NV; ++v)
@@ -478,6 +553,8 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
         else
         {
           hydro_face<R, NV>(c, dY, s, dtdy, kind == 2, f, C.smallr);
+          if (kick)
+            grav_kick<R, NV>(f, hg);
           R * dst = kind == 2 ? sYp : sYm;
 #pragma unroll
           for (int v = 0; v < NV; ++v)
@@ -535,16 +612,28 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
     // HydroRunFunctors3D.h:775-809), store it and take its CFL candidate
     if (kc > k0 && own)
     {
-      R us[NV];
+      R u[NV], us[NV];
       const long long off = own_off + (long long)(kc - 1 + gw) * P.plane;
 #pragma unroll
       for (int v = 0; v < NV; ++v)
+        u[v] = acc[v] - fz[v];
+      R g[3];
+      if constexpr (GRAV)
       {
-        const R x = acc[v] - fz[v];
-        Uout[v * P.vstride + off] = (S)x;
-        us[v] = (R)(S)x;
+        // gravity source term after the flux update (SolverHydroMuscl.cpp:333-338)
+        grav_at<S, R, NV>(P, gi, gj, kc - 1 + gw, g);
+        grav_source<R, NV>(u, rho_prev, g, hdt, C);
       }
-      tmax = fmax(tmax, hydro_invdt<R, NV>(us, C, P));
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+      {
+        Uout[v * P.vstride + off] = (S)u[v];
+        us[v] = (R)(S)u[v];
+      }
+      if constexpr (GRAV)
+        tmax = fmax(tmax, hydro_invdt_grav<R, NV>(us, g, C, P));
+      else
+        tmax = fmax(tmax, hydro_invdt<R, NV>(us, C, P));
     }
     if (full && own)
     {
@@ -553,6 +642,8 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
       for (int v = 0; v < NV; ++v)
       {
         R x = (R)ldg(Uin + v * P.vstride + off);
+        if (v == ID)
+          rho_prev = x;
         x += sXm[(v * TY + ty) * FX + tx + 1];
         x -= sXm[(v * TY + ty) * FX + tx + 2];
         x += sYm[(v * (TY + 2) + ty + 1) * TX + tx];
@@ -572,7 +663,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
 // CFL reduction over the interior of a state (ComputeDtFunctor{2D,3D});
 // used after the state is set (the constructor's compute_dt()).
 // ---------------------------------------------------------------------------
-template <class S, class R, int NV>
+template <class S, class R, int NV, bool GRAV>
 __global__ void
 hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
 {
@@ -584,7 +675,14 @@ hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
 #pragma unroll
     for (int v = 0; v < NV; ++v)
       u[v] = (R)ldg(U + v * P.vstride + off);
-    tmax = fmax(tmax, hydro_invdt<R, NV>(u, C, P));
+    if constexpr (GRAV)
+    {
+      R g[3];
+      grav_at<S, R, NV>(P, i, j, k, g);
+      tmax = fmax(tmax, hydro_invdt_grav<R, NV>(u, g, C, P));
+    }
+    else
+      tmax = fmax(tmax, hydro_invdt<R, NV>(u, C, P));
   });
   block_max_commit<256>(cand_key((double)tmax), key);
 }

@@ -30,14 +30,14 @@ hydro3d_smem()
          (3 * NV * HY * HX + 2 * NV * H3_TY * (H3_TX + 2) + 2 * NV * (H3_TY + 2) * H3_TX);
 }
 
-template <class S, class R, int RS>
+template <class S, class R, int RS, bool GRAV>
 cudaError_t
 hydro_step_rs(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
               cudaStream_t st)
 {
   if (dim == 2)
   {
-    auto   k = hydro2d_step<S, R, H2_TX, H2_TY, RS>;
+    auto   k = hydro2d_step<S, R, H2_TX, H2_TY, RS, GRAV>;
     size_t sm = hydro2d_smem<R>();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess)
@@ -53,7 +53,7 @@ hydro_step_rs(int dim, const void * Uin, void * Uout, const KParams & P, DevCloc
   }
   else
   {
-    auto        k = hydro3d_step<S, R, H3_TX, H3_TY, RS>;
+    auto        k = hydro3d_step<S, R, H3_TX, H3_TY, RS, GRAV>;
     size_t      sm = hydro3d_smem<R>();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess)
@@ -64,20 +64,30 @@ hydro_step_rs(int dim, const void * Uin, void * Uout, const KParams & P, DevCloc
   }
 }
 
-// the Riemann solver is a template parameter of the step kernels
+// the Riemann solver and static gravity are template parameters of the step
+// kernels
+template <class S, class R, bool GRAV>
+cudaError_t
+hydro_step_g(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
+             cudaStream_t st)
+{
+  switch (P.riemann)
+  {
+    case 0: return hydro_step_rs<S, R, 0, GRAV>(dim, Uin, Uout, P, clk, step, st);
+    case 1: return hydro_step_rs<S, R, 1, GRAV>(dim, Uin, Uout, P, clk, step, st);
+    case 2: return hydro_step_rs<S, R, 2, GRAV>(dim, Uin, Uout, P, clk, step, st);
+    case 3: return hydro_step_rs<S, R, 3, GRAV>(dim, Uin, Uout, P, clk, step, st);
+  }
+  return cudaErrorNotSupported;
+}
+
 template <class S, class R>
 cudaError_t
 hydro_step_t(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
              cudaStream_t st)
 {
-  switch (P.riemann)
-  {
-    case 0: return hydro_step_rs<S, R, 0>(dim, Uin, Uout, P, clk, step, st);
-    case 1: return hydro_step_rs<S, R, 1>(dim, Uin, Uout, P, clk, step, st);
-    case 2: return hydro_step_rs<S, R, 2>(dim, Uin, Uout, P, clk, step, st);
-    case 3: return hydro_step_rs<S, R, 3>(dim, Uin, Uout, P, clk, step, st);
-  }
-  return cudaErrorNotSupported;
+  return P.grav ? hydro_step_g<S, R, true>(dim, Uin, Uout, P, clk, step, st)
+                : hydro_step_g<S, R, false>(dim, Uin, Uout, P, clk, step, st);
 }
 
 template <class S, class R>
@@ -85,10 +95,14 @@ cudaError_t
 hydro_dt_t(int dim, const void * U, const KParams & P, unsigned long long * key, cudaStream_t st)
 {
   const int blocks = row_blocks(P);
-  if (dim == 2)
-    hydro_dt_kernel<S, R, 4><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+  if (dim == 2 && P.grav)
+    hydro_dt_kernel<S, R, 4, true><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+  else if (dim == 2)
+    hydro_dt_kernel<S, R, 4, false><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+  else if (P.grav)
+    hydro_dt_kernel<S, R, 5, true><<<blocks, 256, 0, st>>>((const S *)U, P, key);
   else
-    hydro_dt_kernel<S, R, 5><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+    hydro_dt_kernel<S, R, 5, false><<<blocks, 256, 0, st>>>((const S *)U, P, key);
   return cudaGetLastError();
 }
 } // namespace

@@ -85,6 +85,15 @@ typedef struct ek_params
   char   output_prefix[128]; /* [output] outputPrefix ("output") */
   int    vtk_enabled;        /* [output] vtk_enabled (1) */
   int    vtk_ascii;          /* [output] outputVtkAscii (0) */
+  /* static gravity, GravityParams (GravityParams.h:22-37, SolverBase.cpp:38-39);
+   * used by the hydro solvers only, as in the reference */
+  int    gravity_enabled;       /* [gravity] enabled (0) */
+  int    gravity_static;        /* [gravity] static (0): read, no effect (as in the reference) */
+  int    gravity_hancock;       /* [gravity] hancock_predictor_enabled (0) */
+  int    gravity_well_balanced; /* [gravity] well_balanced_reconstruction_enabled (0): read, no effect */
+  double gravity[3];            /* uniform field the solver starts with: [rayleigh_taylor] gx, gy, gz
+                                   (0, -0.1, 0) when problem = rayleigh_taylor, the field the
+                                   reference's init writes (HydroInitFunctors2D.h:735-771); else 0 */
 } ek_params;
 
 typedef struct ek_solver ek_solver;
@@ -117,6 +126,17 @@ ek_status ek_solver_set_state(ek_solver * s, const double * U, int layout);
  * ghost cells filled by the boundary conditions (save_solution path,
  * SolverHydroMuscl.h:749-762). */
 ek_status ek_solver_get_state(ek_solver * s, double * U, int layout);
+
+/* Static gravity field of a hydro solver with params->gravity_enabled:
+ * replaces SolverHydroMuscl::gravity_field (SolverHydroMuscl.h:86-87, a
+ * VectorField of dim components over the full grid, ghosts included, filled
+ * by the problem's init).  G holds dim components per cell in the given
+ * layout (LayoutLeft: G[((comp*ksize + k)*jsize + j)*isize + i];
+ * LayoutRight: G[((i*jsize + j)*ksize + k)*dim + comp]); NULL returns to the
+ * uniform params->gravity.  The CFL of the current state is recomputed (as the
+ * constructor's compute_dt() after init), so the next step uses the new
+ * field.  EK_ERR_INVALID when gravity is not enabled or the solver is MHD. */
+ek_status ek_solver_set_gravity_field(ek_solver * s, const double * G, int layout);
 
 /* SolverBase::compute_dt (SolverBase.cpp:124-154): dt on the current state,
  * clamped so that t + dt <= tEnd.  Writes m_dt to *dt when dt != NULL. */

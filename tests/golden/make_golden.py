@@ -72,10 +72,10 @@ CASES = {
     # uniform field): CFL with gravity, source term, Hancock predictor
     "rt2d_approx": (lambda: P.rayleigh_taylor(dim=2, nx=16, nsteps=12, noise=0.01), 12),
     "rt2d_hllc_hancock": (lambda: P.rayleigh_taylor(dim=2, nx=12, ny=30, nsteps=10, riemann="hllc", hancock=True,
-                                                    noise=0.02, slope_type=1.0, g=-1.0), 10),
+                                                    noise=0.02, slope_type=1.0, g=-0.3), 10),
     "rt3d_approx": (lambda: P.rayleigh_taylor(dim=3, nx=6, nsteps=6, noise=0.01), 6),
     "rt3d_hllc_hancock": (lambda: P.rayleigh_taylor(dim=3, nx=8, ny=6, nz=16, nsteps=5, riemann="hllc",
-                                                    hancock=True, noise=0.02, g=-1.0), 5),
+                                                    hancock=True, noise=0.02, g=-0.3), 5),
     # a non-uniform field (builder returns the field too; the harness loads
     # it into the reference solver's gravity_field)
     "grav2d_field_llf": (lambda: _with_field(P.rayleigh_taylor(dim=2, nx=14, ny=20, nsteps=8, riemann="llf",

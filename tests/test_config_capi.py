@@ -133,3 +133,24 @@ def test_create_rejects_unsupported_configurations():
         with pytest.raises(ek.EkError) as e:
             ek.Solver(p.copy(**bad))
         assert e.value.status in (1, 2), bad
+
+
+def test_gravity_sections_parse_like_reference():
+    # [gravity] (GravityParams.h:32-37) and the Rayleigh-Taylor field
+    # (RayleighTaylorInstabilityParams.h:28-34), against the oracle's front end
+    from euler_kokkos_gb300 import problems as P
+
+    for dim, hancock in ((2, False), (3, True)):
+        ini, _ = P.rayleigh_taylor(dim=dim, nx=8, nsteps=2, hancock=hancock, g=-0.3)
+        p = ek.params_from_ini(ini)
+        o = eko.params_from_ini(ini)
+        assert p.gravity_enabled == 1 and p.gravity_static == 1 and p.gravity_hancock == int(hancock)
+        assert p.gravity_well_balanced == 0
+        assert list(p.gravity) == list(o.gravity) and o.grav_enabled and o.grav_hancock == hancock
+    q = ek.params_from_ini("[run]\nsolver_name=Hydro_Muscl_2D\n[mesh]\nnx=8\nny=8\n[hydro]\nproblem=rayleigh_taylor\n"
+                          "[gravity]\nenabled=true\nwell_balanced_reconstruction_enabled=on\n")
+    assert q.gravity_enabled == 1 and q.gravity_well_balanced == 1 and list(q.gravity) == [0.0, np.float32(-0.1), 0.0]
+    r = ek.params_from_ini("[run]\nsolver_name=Hydro_Muscl_3D\n[mesh]\nnx=8\nny=8\nnz=8\n[hydro]\nproblem=implode\n"
+                          "[gravity]\nenabled=Yes\n[rayleigh_taylor]\ngz=-1\n")
+    # getBool is case-sensitive (Yes -> default false); the field is RT-only
+    assert r.gravity_enabled == 0 and list(r.gravity) == [0.0, 0.0, 0.0]

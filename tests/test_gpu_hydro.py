@@ -23,10 +23,12 @@ DT_REL_TOL = 1e-13
 MIXED_L1_TOL = 1e-5
 
 
-def run_gpu(ini, U0, nsteps, **over):
+def run_gpu(ini, U0, nsteps, G=None, **over):
     p = ek.params_from_ini(ini, **over)
     with ek.SolverFactory.create(p.solver_name, p) as s:
         s.set_state(U0)
+        if G is not None:
+            s.set_gravity_field(G)
         done = s.run(nsteps)
         assert done == nsteps
         return s.get_state(), s.dt_history(), s.m_t, s.m_iteration
@@ -43,7 +45,7 @@ def run_oracle(ini, U0, nsteps):
 def test_exact_build_matches_reference_golden_bitwise(name):
     g = load_golden(name)
     ini = str(g["ini"])
-    U, dts, t, it = run_gpu(ini, g["U0"], len(g["dts"]), exact_fp=1)
+    U, dts, t, it = run_gpu(ini, g["U0"], len(g["dts"]), G=g.get("G"), exact_fp=1)
     p = eko.params_from_ini(ini)
     assert np.array_equal(dts, g["dts"])
     assert np.array_equal(interior(U, p.gw, p.dim), interior(g["U"], p.gw, p.dim))
@@ -54,7 +56,7 @@ def test_exact_build_matches_reference_golden_bitwise(name):
 def test_fma_build_matches_reference_golden(name):
     g = load_golden(name)
     ini = str(g["ini"])
-    U, dts, t, it = run_gpu(ini, g["U0"], len(g["dts"]))
+    U, dts, t, it = run_gpu(ini, g["U0"], len(g["dts"]), G=g.get("G"))
     p = eko.params_from_ini(ini)
     err = rel_linf(interior(U, p.gw, p.dim), interior(g["U"], p.gw, p.dim))
     assert err[0] <= FP64_LINF_TOL and err[1] <= FP64_LINF_TOL, err
