@@ -257,11 +257,17 @@ class Solver:
             raise ValueError("state has %d values, expected shape %s" % (U.size, self.params.shape))
         _check(self._L.ek_solver_set_state(self._h, U.ctypes.data, layout), "set_state")
 
-    def get_state(self, layout: int = EK_LAYOUT_LEFT) -> np.ndarray:
+    def get_state(self, layout: int = EK_LAYOUT_LEFT, out: np.ndarray | None = None) -> np.ndarray:
         """Current state: shape (nbvar, ksize, jsize, isize) for LayoutLeft,
-        (isize, jsize, ksize, nbvar) for LayoutRight."""
+        (isize, jsize, ksize, nbvar) for LayoutRight; out: a C-contiguous
+        float64 array of that size to fill (e.g. in pinned host memory)."""
         shp = self.params.shape
-        U = np.empty(shp if layout == EK_LAYOUT_LEFT else shp[::-1], dtype=np.float64)
+        if out is None:
+            U = np.empty(shp if layout == EK_LAYOUT_LEFT else shp[::-1], dtype=np.float64)
+        else:
+            if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != int(np.prod(shp)):
+                raise ValueError("out must be a C-contiguous float64 array of %d values" % int(np.prod(shp)))
+            U = out
         _check(self._L.ek_solver_get_state(self._h, U.ctypes.data, layout), "get_state")
         return U
 

@@ -60,7 +60,8 @@ struct ek_solver
   int           iteration = 0;
   bool          has_state = false;
   long long     launches = 0;
-  std::vector<double> hbuf; // host staging (FP64, LayoutLeft)
+  double *      stage = nullptr; // device staging of host FP64 arrays (set/get state)
+  long long     stage_elems = 0;
   // kernel timing (ek_solver_set_profiling)
   bool                     profiling = false;
   std::vector<cudaEvent_t> ev_pool;            // recycled events
@@ -326,6 +327,7 @@ ek_solver_destroy(ek_solver * s)
   if (!s->owns)
   {
     drain_events(s);
+    cudaFree(s->stage);
     delete s;
     return EK_OK;
   }
@@ -338,6 +340,7 @@ ek_solver_destroy(ek_solver * s)
   cudaFree(s->dtlog);
   cudaFree(s->scratch3);
   cudaFree(s->gfield);
+  cudaFree(s->stage);
   drain_events(s);
   for (auto e : s->ev_pool)
     cudaEventDestroy(e);
@@ -347,93 +350,90 @@ ek_solver_destroy(ek_solver * s)
   return EK_OK;
 }
 
-// host FP64 LayoutLeft/Right <-> device storage
-static void
-to_device_layout(const ek_solver * s, const double * U, int layout, std::vector<double> & dst)
-{
-  const ek_params & p = s->p;
-  const long long   n = s->kp.vstride;
-  dst.resize((size_t)n * p.nbvar);
-  if (layout == EK_LAYOUT_LEFT)
-  {
-    std::memcpy(dst.data(), U, sizeof(double) * dst.size());
-    return;
-  }
-  // LayoutRight: ((i*jsize + j)*ksize + k)*nbvar + var
-  const int is = s->kp.isize, js = s->kp.jsize, ks = s->kp.ksize, nb = p.nbvar;
-  for (int i = 0; i < is; ++i)
-    for (int j = 0; j < js; ++j)
-      for (int k = 0; k < ks; ++k)
-        for (int v = 0; v < nb; ++v)
-          dst[(size_t)v * n + ((size_t)k * js + j) * is + i] = U[(((size_t)i * js + j) * ks + k) * nb + v];
-}
+// Host FP64 arrays (either layout) <-> device state.  The FP64 LayoutLeft
+// state is copied as is; every other combination goes through a bounded
+// device staging buffer: one cudaMemcpyAsync per chunk of the host array and
+// a kernel that converts (FP32 state) and/or transposes (LayoutRight) it on
+// the device, so the host does no per-element work.
+static const long long kStageElems = 1LL << 25; // 32 Mi doubles (256 MB)
 
-static void
-from_device_layout(const ek_solver * s, const std::vector<double> & src, double * U, int layout)
-{
-  const ek_params & p = s->p;
-  const long long   n = s->kp.vstride;
-  if (layout == EK_LAYOUT_LEFT)
-  {
-    std::memcpy(U, src.data(), sizeof(double) * src.size());
-    return;
-  }
-  const int is = s->kp.isize, js = s->kp.jsize, ks = s->kp.ksize, nb = p.nbvar;
-  for (int i = 0; i < is; ++i)
-    for (int j = 0; j < js; ++j)
-      for (int k = 0; k < ks; ++k)
-        for (int v = 0; v < nb; ++v)
-          U[(((size_t)i * js + j) * ks + k) * nb + v] = src[(size_t)v * n + ((size_t)k * js + j) * is + i];
-}
-
-// FP64 LayoutLeft host buffer <-> device state of the solver's precision
 static ek_status
-upload(ek_solver * s, const std::vector<double> & h, void * dev)
+ensure_stage(ek_solver * s, long long total)
 {
-  const long long n = s->kp.vstride;
-  if (s->prec == EK_PREC_FP64)
+  const long long want = total < kStageElems ? total : kStageElems;
+  if (s->stage_elems >= want)
+    return EK_OK;
+  cudaFree(s->stage);
+  s->stage = nullptr;
+  s->stage_elems = 0;
+  EK_CUDA(cudaMalloc((void **)&s->stage, sizeof(double) * (size_t)want), "staging buffer");
+  s->stage_elems = want;
+  return EK_OK;
+}
+
+// views into an ensemble keep no staging buffer between calls
+static void
+release_stage(ek_solver * s)
+{
+  if (s->owns)
+    return;
+  cudaFree(s->stage);
+  s->stage = nullptr;
+  s->stage_elems = 0;
+}
+
+static ek_status
+host_to_state(ek_solver * s, const double * U, int layout, void * dev)
+{
+  const long long total = s->kp.vstride * s->p.nbvar;
+  if (s->prec == EK_PREC_FP64 && layout == EK_LAYOUT_LEFT)
   {
-    EK_CUDA(cudaMemcpyAsync(dev, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s->stream),
-            "upload");
+    EK_CUDA(cudaMemcpyAsync(dev, U, sizeof(double) * (size_t)total, cudaMemcpyHostToDevice, s->stream), "upload");
+    EK_CUDA(cudaStreamSynchronize(s->stream), "upload");
     return EK_OK;
   }
-  const int nh = s->p.mhd ? 5 : s->p.nbvar;
-  std::vector<float> f((size_t)n * nh);
-  for (size_t i = 0; i < f.size(); ++i)
-    f[i] = (float)h[i];
-  EK_CUDA(cudaMemcpyAsync(dev, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice, s->stream),
-          "upload");
-  if (s->p.mhd)
-    EK_CUDA(cudaMemcpyAsync(ekc::mixed_bfield(dev, s->kp), h.data() + (size_t)5 * n,
-                            sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s->stream),
+  ek_status st = ensure_stage(s, total);
+  if (st != EK_OK)
+    return st;
+  for (long long first = 0; first < total; first += s->stage_elems)
+  {
+    const long long cnt = total - first < s->stage_elems ? total - first : s->stage_elems;
+    EK_CUDA(cudaMemcpyAsync(s->stage, U + first, sizeof(double) * (size_t)cnt, cudaMemcpyHostToDevice, s->stream),
             "upload");
+    EK_CUDA(ek_fast::convert_stage(true, s->prec, layout, s->stage, dev, s->kp, s->p.nbvar, first, cnt, s->stream),
+            "upload");
+    s->launches += 1;
+  }
   EK_CUDA(cudaStreamSynchronize(s->stream), "upload");
+  release_stage(s);
   return EK_OK;
 }
 
 static ek_status
-download(ek_solver * s, const void * dev, std::vector<double> & h)
+state_to_host(ek_solver * s, const void * dev, double * U, int layout)
 {
-  const long long n = s->kp.vstride;
-  h.resize((size_t)n * s->p.nbvar);
-  if (s->prec == EK_PREC_FP64)
+  const long long total = s->kp.vstride * s->p.nbvar;
+  if (s->prec == EK_PREC_FP64 && layout == EK_LAYOUT_LEFT)
   {
-    EK_CUDA(cudaMemcpyAsync(h.data(), dev, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s->stream),
-            "download");
+    EK_CUDA(cudaMemcpyAsync(U, dev, sizeof(double) * (size_t)total, cudaMemcpyDeviceToHost, s->stream), "download");
     EK_CUDA(cudaStreamSynchronize(s->stream), "download");
     return EK_OK;
   }
-  const int nh = s->p.mhd ? 5 : s->p.nbvar;
-  std::vector<float> f((size_t)n * nh);
-  EK_CUDA(cudaMemcpyAsync(f.data(), dev, sizeof(float) * f.size(), cudaMemcpyDeviceToHost, s->stream),
-          "download");
-  if (s->p.mhd)
-    EK_CUDA(cudaMemcpyAsync(h.data() + (size_t)5 * n, ekc::mixed_bfield(dev, s->kp),
-                            sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s->stream),
+  ek_status st = ensure_stage(s, total);
+  if (st != EK_OK)
+    return st;
+  for (long long first = 0; first < total; first += s->stage_elems)
+  {
+    const long long cnt = total - first < s->stage_elems ? total - first : s->stage_elems;
+    EK_CUDA(ek_fast::convert_stage(false, s->prec, layout, s->stage, const_cast<void *>(dev), s->kp, s->p.nbvar,
+                                   first, cnt, s->stream),
             "download");
+    s->launches += 1;
+    EK_CUDA(cudaMemcpyAsync(U + first, s->stage, sizeof(double) * (size_t)cnt, cudaMemcpyDeviceToHost, s->stream),
+            "download");
+  }
   EK_CUDA(cudaStreamSynchronize(s->stream), "download");
-  for (size_t i = 0; i < f.size(); ++i)
-    h[i] = (double)f[i];
+  release_stage(s);
   return EK_OK;
 }
 
@@ -518,8 +518,7 @@ static ek_status
 set_state_at(ek_solver * s, const double * U, int layout, double t0)
 {
   EK_CUDA(cudaSetDevice(s->device), "cudaSetDevice");
-  to_device_layout(s, U, layout, s->hbuf);
-  ek_status st = upload(s, s->hbuf, s->U[0]);
+  ek_status st = host_to_state(s, U, layout, s->U[0]);
   if (st != EK_OK)
     return st;
   // U2 = U (deep_copy), ghosts of both follow the boundary conditions
@@ -798,11 +797,7 @@ ek_solver_get_state(ek_solver * s, double * U, int layout)
   void * cur = s->U[s->iteration % 2];
   EK_CUDA(ek_fast::fill_ghosts(s->prec, cur, s->kp, s->p.mhd ? 8 : s->p.nbvar, s->stream), "ghosts");
   s->launches += 1;
-  ek_status st = download(s, cur, s->hbuf);
-  if (st != EK_OK)
-    return st;
-  from_device_layout(s, s->hbuf, U, layout);
-  return EK_OK;
+  return state_to_host(s, cur, U, layout);
 }
 
 // restart file: a fixed header, then the FP64 LayoutLeft state, ghosts included

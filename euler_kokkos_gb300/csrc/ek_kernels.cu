@@ -242,6 +242,74 @@ fill_ghosts(int prec, void * U, const KParams & P, int nbvar, cudaStream_t st)
   return cudaGetLastError();
 }
 
+namespace
+{
+// offset in the device state of element e of a host array (layout 0: LayoutLeft
+// [var][k][j][i], 1: LayoutRight [i][j][k][var]); v receives the variable
+__device__ __forceinline__ long long
+host_elem_cell(long long e, int layout, const KParams & P, int nbvar, int & v)
+{
+  if (layout == 0)
+  {
+    v = (int)(e / P.vstride);
+    return e - (long long)v * P.vstride;
+  }
+  v = (int)(e % nbvar);
+  long long c = e / nbvar;
+  const int k = (int)(c % P.ksize);
+  c /= P.ksize;
+  const int j = (int)(c % P.jsize);
+  const int i = (int)(c / P.jsize);
+  return (long long)k * P.plane + (long long)j * P.isize + i;
+}
+
+template <bool TO_STATE>
+__global__ void
+convert_stage_kernel(int prec, int layout, double * __restrict__ stage, void * __restrict__ U, KParams P, int nbvar,
+                     long long first, long long count)
+{
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
+       t += (long long)gridDim.x * blockDim.x)
+  {
+    int             v;
+    const long long cell = host_elem_cell(first + t, layout, P, nbvar, v);
+    if (prec == 0 || (P.mhd && v >= 5))
+    {
+      // FP64 state, or a face-field plane of the mixed MHD state
+      double * D = prec == 0 ? (double *)U + (long long)v * P.vstride + cell
+                             : mixed_bfield(U, P) + (long long)(v - 5) * P.vstride + cell;
+      if (TO_STATE)
+        *D = stage[t];
+      else
+        stage[t] = *D;
+    }
+    else
+    {
+      float * F = (float *)U + (long long)v * P.vstride + cell;
+      if (TO_STATE)
+        *F = __double2float_rn(stage[t]);
+      else
+        stage[t] = (double)*F;
+    }
+  }
+}
+} // namespace
+
+cudaError_t
+convert_stage(bool to_state, int prec, int layout, double * stage, void * U, const KParams & P, int nbvar,
+              long long first, long long count, cudaStream_t st)
+{
+  const long long want = (count + 255) / 256;
+  const int       blocks = (int)(want < 152 * 16 ? want : 152 * 16);
+  if (blocks <= 0)
+    return cudaSuccess;
+  if (to_state)
+    convert_stage_kernel<true><<<blocks, 256, 0, st>>>(prec, layout, stage, U, P, nbvar, first, count);
+  else
+    convert_stage_kernel<false><<<blocks, 256, 0, st>>>(prec, layout, stage, U, P, nbvar, first, count);
+  return cudaGetLastError();
+}
+
 cudaError_t
 ensemble_totals(int prec, const EnsInstance * insts, int n, const int * stepc, double * out,
                 cudaStream_t st)

@@ -47,4 +47,10 @@ cudaError_t totals(int prec, const void * U, const KParams & P, int nbvar, doubl
                    cudaStream_t st);
 cudaError_t ensemble_totals(int prec, const ekc::EnsInstance * insts, int n, const int * stepc,
                             double * out, cudaStream_t st);
+// Host FP64 arrays <-> device state.  Elements [first, first + count) of a
+// host array in the caller's layout (0 LayoutLeft, 1 LayoutRight; nbvar
+// variables) sit in the device staging buffer stage; to_state: convert them
+// into the state U (precision prec), else fill stage from U.
+cudaError_t convert_stage(bool to_state, int prec, int layout, double * stage, void * U, const KParams & P,
+                          int nbvar, long long first, long long count, cudaStream_t st);
 } // namespace ek_fast

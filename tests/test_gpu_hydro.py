@@ -166,3 +166,48 @@ def test_totals_are_fp64_and_conserved_periodic():
             s.run(20)
             m1 = s.totals()[0]
         assert abs(m1 - m0) / m0 < (1e-13 if prec == 0 else 1e-6)
+
+
+@pytest.mark.parametrize("prec", [ek.EK_PREC_FP64, ek.EK_PREC_MIXED])
+def test_state_transfer_layouts_and_precisions(prec):
+    # set_state/get_state convert and transpose on the device (staging chunks)
+    cases = [P.smooth_random(dim=3, nx=10, ny=7, nz=5, seed=32, bc=(1, 2, 3, 3, 1, 2), nsteps=1),
+             P.smooth_random(dim=3, mhd=True, nx=9, ny=6, nz=5, seed=33, bc=(3,) * 6, nsteps=1),
+             P.smooth_random(dim=2, nx=13, ny=11, seed=34, bc=(3, 3, 2, 2, 1, 1), nsteps=1)]
+    for ini, U0 in cases:
+        p = ek.params_from_ini(ini, precision=prec)
+        o = eko.Oracle(eko.params_from_ini(ini), U0)
+        want = o.state()  # ghosts filled the reference way
+        if prec == ek.EK_PREC_MIXED:
+            nh = 5 if p.mhd else p.nbvar  # FP32 hydro planes, FP64 face B
+            want = want.copy()
+            want[:nh] = want[:nh].astype(np.float32).astype(np.float64)
+        with ek.Solver(p) as s:
+            s.set_state(np.ascontiguousarray(np.transpose(U0, (3, 2, 1, 0))), layout=ek.EK_LAYOUT_RIGHT)
+            UL = s.get_state()
+            UR = s.get_state(layout=ek.EK_LAYOUT_RIGHT)
+            s.set_state(U0)
+            UL2 = s.get_state(out=np.empty_like(U0))
+        assert np.array_equal(UL, want)
+        assert np.array_equal(np.transpose(UR, (3, 2, 1, 0)), want)
+        assert np.array_equal(UL2, want)
+
+
+def test_state_transfer_in_several_chunks():
+    # 45.8 M values: more than one 32 Mi-value staging chunk
+    n = 200
+    ini, _ = P.blast_3d(n=8, nsteps=1)
+    ini = ini.replace("nx=8", "nx=%d" % (n + 8)).replace("ny=8", "ny=%d" % (n + 8)).replace("nz=8", "nz=%d" % n)
+    p = ek.params_from_ini(ini, precision=ek.EK_PREC_MIXED)
+    shp = p.shape
+    rng = np.random.default_rng(5)
+    U0 = np.empty(shp)
+    U0[0] = 1.0 + 0.1 * rng.random(shp[1:])
+    U0[1] = 2.0 + 0.1 * rng.random(shp[1:])
+    U0[2:] = 0.01 * rng.standard_normal((3,) + shp[1:])
+    with ek.Solver(p) as s:
+        s.set_state(np.ascontiguousarray(np.transpose(U0, (3, 2, 1, 0))), layout=ek.EK_LAYOUT_RIGHT)
+        got = s.get_state(layout=ek.EK_LAYOUT_RIGHT)
+    gw = p.ghost_width
+    a = np.transpose(got, (3, 2, 1, 0))[:, gw:-gw, gw:-gw, gw:-gw]
+    assert np.array_equal(a, U0[:, gw:-gw, gw:-gw, gw:-gw].astype(np.float32).astype(np.float64))
