@@ -70,6 +70,7 @@ class Params(ctypes.Structure):
         ("gravity_enabled", ctypes.c_int), ("gravity_static", ctypes.c_int),
         ("gravity_hancock", ctypes.c_int), ("gravity_well_balanced", ctypes.c_int),
         ("gravity", ctypes.c_double * 3),
+        ("no_tma", ctypes.c_int),
     ]
 
     @property

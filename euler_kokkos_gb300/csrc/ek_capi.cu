@@ -53,6 +53,9 @@ struct ek_solver
   int           dtcap = 0;
   double *      scratch3 = nullptr; // device totals
   void *        gfield = nullptr;   // static gravity field (state precision), if set
+  // tensor maps of U[0] / U[1] for the 3D hydro kernel's staged planes
+  alignas(64) CUtensorMap tmap[2];
+  bool          has_tmap = false;
   cudaStream_t  stream = nullptr;
   int           device = 0;
   // host mirror of SolverBase state
@@ -309,6 +312,9 @@ ek_solver_create(const ek_params * params, ek_solver ** out)
     e = cudaMemset(s->U[0], 0, s->state_bytes);
   if (e == cudaSuccess)
     e = cudaMemset(s->U[1], 0, s->state_bytes);
+  if (e == cudaSuccess && !p.mhd && p.dim == 3 && !p.no_tma)
+    s->has_tmap = ek_fast::hydro3d_tensor_map(s->prec, s->U[0], k, &s->tmap[0]) &&
+                  ek_fast::hydro3d_tensor_map(s->prec, s->U[1], k, &s->tmap[1]);
   if (e != cudaSuccess)
   {
     ek_status st = cuda_fail(e, "ek_solver_create");
@@ -653,8 +659,11 @@ launch_one(ek_solver * s, int kernel_id, int phase, int step)
     e = s->exact ? ek_exact::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream)
                  : ek_fast::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream);
   else
-    e = s->exact ? ek_exact::hydro_step(s->p.dim, s->prec, in, outp, s->kp, s->clk, step, s->stream)
-                 : ek_fast::hydro_step(s->p.dim, s->prec, in, outp, s->kp, s->clk, step, s->stream);
+  {
+    const CUtensorMap * tm = s->has_tmap ? &s->tmap[step % 2] : nullptr;
+    e = s->exact ? ek_exact::hydro_step(s->p.dim, s->prec, in, outp, s->kp, s->clk, step, tm, s->stream)
+                 : ek_fast::hydro_step(s->p.dim, s->prec, in, outp, s->kp, s->clk, step, tm, s->stream);
+  }
   if (s->profiling)
   {
     cudaEventRecord(e1, s->stream);
@@ -700,6 +709,8 @@ sync_from_clock(ek_solver * s)
   ek_status st = read_clock(s, &h);
   if (st != EK_OK)
     return st;
+  if (h.error & ekc::EK_DEVERR_TMA_TIMEOUT)
+    return fail(EK_ERR_CUDA, "a tensor copy of the step kernel did not complete within its 1 s wait limit");
   s->iteration = h.iteration;
   s->t = h.t[h.iteration % 3];
   if (h.iteration > 0 && h.iteration - 1 < s->dtcap)

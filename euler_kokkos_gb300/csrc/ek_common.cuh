@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h> // CUtensorMap (the type only; maps are encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 #ifndef EK_NS
@@ -89,6 +90,7 @@ struct DevClock
 enum : int
 {
   EK_DEVERR_NONFINITE_DT = 1,
+  EK_DEVERR_TMA_TIMEOUT = 2, // a tensor copy did not complete within its wait limit
 };
 
 // One instance of an ensemble of independent runs and one tile of work.
@@ -494,6 +496,76 @@ __device__ __forceinline__ unsigned long long
 cand_key(double v)
 {
   return (v != v) ? 0ull : dkey(v);
+}
+
+
+// ---------------------------------------------------------------------------
+// Tensor-memory-access (TMA) staging: one elected thread starts an
+// asynchronous tiled copy global -> shared memory that completes on an
+// mbarrier; the consumers wait on the barrier's phase.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned
+smem_addr(const void * p)
+{
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void
+mbar_init(unsigned long long * bar, unsigned count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  // make the initialised barrier visible to the tensor-copy (async) proxy
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// order this thread's earlier generic accesses of shared memory before the
+// async-proxy writes of a tensor copy issued after it
+__device__ __forceinline__ void
+fence_proxy_async_smem()
+{
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void
+mbar_expect_tx(unsigned long long * bar, unsigned bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// 4D tiled tensor copy of the box at (x, y, z, w) of *map into dst
+__device__ __forceinline__ void
+tma_load_4d(void * dst, const CUtensorMap * map, int x, int y, int z, int w, unsigned long long * bar)
+{
+  asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+               " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_addr(dst)),
+               "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ unsigned long long
+global_ns()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// wait until phase `parity` of the barrier has completed; false when that
+// has not happened within limit_ns (the caller reports the error and leaves)
+__device__ __forceinline__ bool
+mbar_wait(unsigned long long * bar, unsigned parity, unsigned long long limit_ns)
+{
+  const unsigned addr = smem_addr(bar);
+  unsigned long long t0 = 0;
+  for (int n = 0;; ++n)
+  {
+    unsigned done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done)
+                 : "r"(addr), "r"(parity)
+                 : "memory");
+    if (done)
+      return true;
+    const unsigned long long t = global_ns();
+    if (n == 0)
+      t0 = t;
+    else if (t - t0 > limit_ns)
+      return false;
+  }
 }
 
 } // namespace EK_NS

@@ -248,6 +248,7 @@ ek_params_from_ini(const char * text, size_t len, ek_params * out)
   p.exact_fp = (int)get_integer(ini, "gb300", "exact", 0);
   p.kchunk = (int)get_integer(ini, "gb300", "kchunk", 0);
   p.mhd_stage = (int)get_integer(ini, "gb300", "mhd_stage", 0);
+  p.no_tma = get_integer(ini, "gb300", "tma", 1) == 0 ? 1 : 0;
   *out = p;
   return EK_OK;
 }

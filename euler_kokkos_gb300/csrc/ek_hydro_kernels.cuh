@@ -80,6 +80,36 @@ load_q_plane(const S * __restrict__ U, const KParams & P, const HydroConst<R> & 
   }
 }
 
+// In-place conversion of a (TX+4) x (TY+4) plane of conserved variables,
+// staged in sQ[NV][HY][HX] by a tensor copy, to primitive variables.  Each
+// thread converts whole cells, so no cell is read after another thread wrote it.
+template <class R, int NV, int TX, int TY>
+__device__ __forceinline__ void
+convert_q_plane(R * sQ, const HydroConst<R> & C)
+{
+  constexpr int HX = TX + 4, HY = TY + 4, NT = TX * TY;
+  for (int c = threadIdx.x; c < HX * HY; c += NT)
+  {
+    R u[NV], q[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      u[v] = sQ[v * HY * HX + c];
+    hydro_prims<R, NV>(u, q, C);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      sQ[v * HY * HX + c] = q[v];
+  }
+}
+
+// elements between ring slots of the 3D kernel: one primitive plane rounded up
+// to a multiple of 128 bytes (the alignment of a tensor-copy destination)
+template <class R, int TX, int TY>
+__host__ __device__ constexpr int
+hydro3d_slot_elems()
+{
+  return (int)(((5 * (TX + 4) * (TY + 4) * sizeof(R) + 127) / 128 * 128) / sizeof(R));
+}
+
 // slopes of the cell at tile coordinates (hx, hy) of the planes qm/q0/qp
 template <class R, int NV, int HX, int HY>
 __device__ __forceinline__ void
@@ -379,15 +409,17 @@ ensemble_totals_kernel(const EnsInstance * __restrict__ insts, const int * __res
 // ---------------------------------------------------------------------------
 // 3D: one CTA = a TX x TY column of interior cells marching over kchunk planes
 // ---------------------------------------------------------------------------
-template <class S, class R, int TX, int TY, int RS, bool GRAV>
+template <class S, class R, int TX, int TY, int RS, bool GRAV, bool TMA>
 __global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_H3_MINB_F32, EK_H3_MINB_F64))
-hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step)
+hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevClock * clk, int step,
+             const __grid_constant__ CUtensorMap tmap)
 {
   constexpr int NV = 5, HX = TX + 4, HY = TY + 4, NT = TX * TY;
   constexpr int FX = TX + 2;
-  constexpr int QP = NV * HY * HX; // one primitive plane
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  R * sQ = reinterpret_cast<R *>(smem_raw); // [3][NV][HY][HX] ring of planes
+  constexpr int QP = hydro3d_slot_elems<R, TX, TY>(); // one primitive plane (padded)
+  // [3][NV][HY][HX] ring of planes, 128-byte aligned for the tensor copies
+  extern __shared__ __align__(128) unsigned char smem_ring[];
+  R * sQ = reinterpret_cast<R *>(smem_ring);
   R * sXm = sQ + 3 * QP;
   R * sXp = sXm + NV * TY * FX;
   R * sYm = sXp + NV * TY * FX;
@@ -415,11 +447,41 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   const bool xy_in = gi0 - 2 >= gw && gi0 + TX + 1 < P.nx + gw && gj0 - 2 >= gw && gj0 + TY + 1 < P.ny + gw;
   auto       plane_in = [&](int gk) { return xy_in && gk >= gw && gk < P.nz + gw; };
 
-  // prologue: planes k0-2, k0-1
+  // Planes whose whole tile halo lies in the interior are staged by a tensor
+  // copy of the (HX, HY, 1, NV) box of U, started one plane ahead (while the
+  // previous plane's fluxes and update run) and converted in place; the other
+  // planes are loaded through the boundary mapping.  One copy is in flight at
+  // a time, on one mbarrier.
+  __shared__ unsigned long long tma_bar;
+  __shared__ int                tma_bad;
+  const bool                    tma = TMA && xy_in && (smem_addr(sQ) & 127u) == 0;
+  if constexpr (TMA)
+  {
+    if (threadIdx.x == 0)
+    {
+      tma_bad = 0;
+      if (tma)
+        mbar_init(&tma_bar, 1);
+    }
+    __syncthreads();
+  }
+  constexpr unsigned TMA_BYTES = NV * HX * HY * sizeof(S);
+  auto tma_issue = [&](int p) { // one thread: interior plane p into its ring slot
+    mbar_expect_tx(&tma_bar, TMA_BYTES);
+    tma_load_4d(sQ + ((p + 3) % 3) * QP, &tmap, gi0 - 2, gj0 - 2, p + gw, 0, &tma_bar);
+  };
+  // The copied planes are the interior ones (0 <= p < nz) from k0 on, one per
+  // iteration: plane kc+1 is in flight at the top of iteration kc when it is
+  // interior, and it is copy number kc+1-k0 on the barrier (phase parity).
+  auto pending = [&](int kc) { return tma && kc + 1 < P.nz; };
+
+  // prologue: planes k0-2, k0-1, and the copy of k0
   load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 2 + gw, sQ + ((k0 + 1) % 3) * QP,
                                  plane_in(k0 - 2 + gw));
   load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, k0 - 1 + gw, sQ + ((k0 + 2) % 3) * QP,
                                  plane_in(k0 - 1 + gw));
+  if (pending(k0 - 1) && threadIdx.x == 0)
+    tma_issue(k0);
 
   R zmax_prev[NV];        // ZMAX face state of the cell below
   R acc[NV];              // partial update of the cell below, waiting for -Fz(k)
@@ -437,9 +499,27 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   for (int kc = k0 - 1; kc <= k1; ++kc)
   {
     // plane kc+1 into ring slot (kc+1)%3  [(kc+1+3)%3 to stay non-negative]
-    load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, kc + 1 + gw, sQ + ((kc + 4) % 3) * QP,
-                                   plane_in(kc + 1 + gw));
+    if (pending(kc))
+    {
+      if (!mbar_wait(&tma_bar, (unsigned)(kc + 1 - k0) & 1u, 1000000000ull))
+        tma_bad = 1;
+      convert_q_plane<R, NV, TX, TY>(sQ + ((kc + 4) % 3) * QP, C);
+    }
+    else
+      load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, kc + 1 + gw, sQ + ((kc + 4) % 3) * QP,
+                                     plane_in(kc + 1 + gw));
     __syncthreads();
+    if (TMA && tma_bad)
+    {
+      // the copy did not complete within 1 s: report it, give the copy one
+      // more bounded wait so it does not land after the block has left
+      if (threadIdx.x == 0)
+      {
+        atomicOr(&clk->error, EK_DEVERR_TMA_TIMEOUT);
+        mbar_wait(&tma_bar, (unsigned)(kc + 1 - k0) & 1u, 1000000000ull);
+      }
+      return;
+    }
     const R * q0 = sQ + ((kc + 3) % 3) * QP;
     const R * qm = sQ + ((kc + 2) % 3) * QP;
     const R * qp = sQ + ((kc + 4) % 3) * QP;
@@ -562,7 +642,14 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
         }
       }
     }
+    // every thread orders its generic accesses of the ring before the tensor
+    // copy that will overwrite plane kc-1's slot
+    if (tma)
+      fence_proxy_async_smem();
     __syncthreads();
+    // plane kc-1 is no longer read: start the copy of plane kc+2 into its slot
+    if (kc + 1 <= k1 && pending(kc + 1) && threadIdx.x == 0)
+      tma_issue(kc + 2);
 
     if (full)
     {

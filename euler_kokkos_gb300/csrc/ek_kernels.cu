@@ -1,6 +1,8 @@
 // Kernel instantiations and launchers.  Compiled twice (see ek_launch.h):
 //   -DEK_NS=ek_exact --fmad=false   FP64 only, bitwise parity build
 //   -DEK_NS=ek_fast  --fmad=true    FP64 + mixed FP32
+#include <cstring>
+
 #include "ek_launch.h"
 #include "ek_hydro_kernels.cuh"
 #include "ek_mhd_kernels.cuh"
@@ -25,15 +27,16 @@ template <class R>
 constexpr size_t
 hydro3d_smem()
 {
-  constexpr int NV = 5, HX = H3_TX + 4, HY = H3_TY + 4;
-  return sizeof(R) *
-         (3 * NV * HY * HX + 2 * NV * H3_TY * (H3_TX + 2) + 2 * NV * (H3_TY + 2) * H3_TX);
+  // three padded ring slots and the face buffers
+  constexpr int NV = 5;
+  return sizeof(R) * (3 * hydro3d_slot_elems<R, H3_TX, H3_TY>() + 2 * NV * H3_TY * (H3_TX + 2) +
+                      2 * NV * (H3_TY + 2) * H3_TX);
 }
 
 template <class S, class R, int RS, bool GRAV>
 cudaError_t
 hydro_step_rs(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
-              cudaStream_t st)
+              const CUtensorMap * tmap, cudaStream_t st)
 {
   if (dim == 2)
   {
@@ -53,13 +56,19 @@ hydro_step_rs(int dim, const void * Uin, void * Uout, const KParams & P, DevCloc
   }
   else
   {
-    auto        k = hydro3d_step<S, R, H3_TX, H3_TY, RS, GRAV>;
+    // interior planes staged by tensor copies when Uin has a tensor map
+    auto        k = tmap ? hydro3d_step<S, R, H3_TX, H3_TY, RS, GRAV, true>
+                         : hydro3d_step<S, R, H3_TX, H3_TY, RS, GRAV, false>;
     size_t      sm = hydro3d_smem<R>();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess)
       return e;
     dim3 grid((P.nx + H3_TX - 1) / H3_TX, (P.ny + H3_TY - 1) / H3_TY, (P.nz + P.kchunk - 1) / P.kchunk);
-    k<<<grid, H3_TX * H3_TY, sm, st>>>((const S *)Uin, (S *)Uout, P, clk, step);
+    CUtensorMap m;
+    std::memset(&m, 0, sizeof m);
+    if (tmap)
+      m = *tmap;
+    k<<<grid, H3_TX * H3_TY, sm, st>>>((const S *)Uin, (S *)Uout, P, clk, step, m);
     return cudaGetLastError();
   }
 }
@@ -69,14 +78,14 @@ hydro_step_rs(int dim, const void * Uin, void * Uout, const KParams & P, DevCloc
 template <class S, class R, bool GRAV>
 cudaError_t
 hydro_step_g(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
-             cudaStream_t st)
+             const CUtensorMap * tmap, cudaStream_t st)
 {
   switch (P.riemann)
   {
-    case 0: return hydro_step_rs<S, R, 0, GRAV>(dim, Uin, Uout, P, clk, step, st);
-    case 1: return hydro_step_rs<S, R, 1, GRAV>(dim, Uin, Uout, P, clk, step, st);
-    case 2: return hydro_step_rs<S, R, 2, GRAV>(dim, Uin, Uout, P, clk, step, st);
-    case 3: return hydro_step_rs<S, R, 3, GRAV>(dim, Uin, Uout, P, clk, step, st);
+    case 0: return hydro_step_rs<S, R, 0, GRAV>(dim, Uin, Uout, P, clk, step, tmap, st);
+    case 1: return hydro_step_rs<S, R, 1, GRAV>(dim, Uin, Uout, P, clk, step, tmap, st);
+    case 2: return hydro_step_rs<S, R, 2, GRAV>(dim, Uin, Uout, P, clk, step, tmap, st);
+    case 3: return hydro_step_rs<S, R, 3, GRAV>(dim, Uin, Uout, P, clk, step, tmap, st);
   }
   return cudaErrorNotSupported;
 }
@@ -84,10 +93,10 @@ hydro_step_g(int dim, const void * Uin, void * Uout, const KParams & P, DevClock
 template <class S, class R>
 cudaError_t
 hydro_step_t(int dim, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
-             cudaStream_t st)
+             const CUtensorMap * tmap, cudaStream_t st)
 {
-  return P.grav ? hydro_step_g<S, R, true>(dim, Uin, Uout, P, clk, step, st)
-                : hydro_step_g<S, R, false>(dim, Uin, Uout, P, clk, step, st);
+  return P.grav ? hydro_step_g<S, R, true>(dim, Uin, Uout, P, clk, step, tmap, st)
+                : hydro_step_g<S, R, false>(dim, Uin, Uout, P, clk, step, tmap, st);
 }
 
 template <class S, class R>
@@ -109,16 +118,16 @@ hydro_dt_t(int dim, const void * U, const KParams & P, unsigned long long * key,
 
 cudaError_t
 hydro_step(int dim, int prec, const void * Uin, void * Uout, const KParams & P, DevClock * clk,
-           int step, cudaStream_t st)
+           int step, const CUtensorMap * tmap, cudaStream_t st)
 {
 #ifdef EK_EXACT_ONLY
   if (prec != 0)
     return cudaErrorNotSupported;
-  return hydro_step_t<double, double>(dim, Uin, Uout, P, clk, step, st);
+  return hydro_step_t<double, double>(dim, Uin, Uout, P, clk, step, tmap, st);
 #else
   if (prec == 0)
-    return hydro_step_t<double, double>(dim, Uin, Uout, P, clk, step, st);
-  return hydro_step_t<float, float>(dim, Uin, Uout, P, clk, step, st);
+    return hydro_step_t<double, double>(dim, Uin, Uout, P, clk, step, tmap, st);
+  return hydro_step_t<float, float>(dim, Uin, Uout, P, clk, step, tmap, st);
 #endif
 }
 
@@ -197,6 +206,39 @@ ensemble2d_grid(int prec)
 }
 
 #ifndef EK_EXACT_ONLY
+bool
+hydro3d_tensor_map(int prec, const void * U, const KParams & P, CUtensorMap * out)
+{
+  // cuTensorMapEncodeTiled through the runtime's driver entry point (no
+  // link-time dependency on the driver library)
+  using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static Encode encode = [] {
+    void *                          fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+          cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return (Encode)fn;
+  }();
+  const size_t es = prec == 0 ? sizeof(double) : sizeof(float);
+  // global strides must be multiples of 16 bytes; the box's x origin
+  // (gi0 - 2 = blockIdx.x * TX) is then 16-byte aligned since TX % 4 == 0
+  if (!encode || P.ksize < 2 || ((size_t)P.isize * es) % 16 != 0 || (H3_TX % 4) != 0 ||
+      (reinterpret_cast<uintptr_t>(U) % 16) != 0)
+    return false;
+  const cuuint64_t dims[4] = { (cuuint64_t)P.isize, (cuuint64_t)P.jsize, (cuuint64_t)P.ksize, 5 };
+  const cuuint64_t strides[3] = { (cuuint64_t)P.isize * es, (cuuint64_t)P.plane * es, (cuuint64_t)P.vstride * es };
+  const cuuint32_t box[4] = { H3_TX + 4, H3_TY + 4, 1, 5 };
+  const cuuint32_t estr[4] = { 1, 1, 1, 1 };
+  return encode(out, prec == 0 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                const_cast<void *>(U), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 namespace
 {
 template <class S>

@@ -14,8 +14,9 @@
   using ekc::KParams;                                                                               \
   using ekc::DevClock;                                                                              \
   /* prec: 0 FP64, 1 mixed.  Uin/Uout device state arrays. */                                      \
+  /* tmap: tensor map of Uin for the 3D kernel's staged planes, or null */                        \
   cudaError_t hydro_step(int dim, int prec, const void * Uin, void * Uout, const KParams & P,        \
-                         DevClock * clk, int step, cudaStream_t st);                                \
+                         DevClock * clk, int step, const CUtensorMap * tmap, cudaStream_t st);      \
   cudaError_t hydro_dt(int dim, int prec, const void * U, const KParams & P,                       \
                        unsigned long long * key, cudaStream_t st);                                  \
   cudaError_t mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key,         \
@@ -53,4 +54,7 @@ cudaError_t ensemble_totals(int prec, const ekc::EnsInstance * insts, int n, con
 // into the state U (precision prec), else fill stage from U.
 cudaError_t convert_stage(bool to_state, int prec, int layout, double * stage, void * U, const KParams & P,
                           int nbvar, long long first, long long count, cudaStream_t st);
+// Tensor map of a 3D hydro state U (box = the 3D kernel's tile plus halo, all
+// five variables); false when the layout does not allow tensor copies.
+bool hydro3d_tensor_map(int prec, const void * U, const KParams & P, CUtensorMap * out);
 } // namespace ek_fast

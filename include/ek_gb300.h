@@ -94,6 +94,8 @@ typedef struct ek_params
   double gravity[3];            /* uniform field the solver starts with: [rayleigh_taylor] gx, gy, gz
                                    (0, -0.1, 0) when problem = rayleigh_taylor, the field the
                                    reference's init writes (HydroInitFunctors2D.h:735-771); else 0 */
+  int    no_tma;                /* 1: the 3D hydro kernel loads every plane with plain loads instead of
+                                   staging interior planes by tensor copies ([gb300] tma = 0) */
 } ek_params;
 
 typedef struct ek_solver ek_solver;

@@ -153,3 +153,14 @@ def test_mhd_ignores_gravity_and_refusals():
     ini3, _ = P.rayleigh_taylor(dim=2, nx=16, nsteps=2, riemann="hllc")
     with pytest.raises(ek.EkError):
         ek.Ensemble([ek.params_from_ini(ini3)])
+
+
+def test_gravity_with_tensor_copy_staging_matches_oracle():
+    # a grid with tiles whose halo is interior (tensor-copy staged planes)
+    ini, U0 = P.rayleigh_taylor(dim=3, nx=40, ny=40, nz=48, nsteps=4, riemann="hllc", hancock=True, noise=0.02)
+    p = eko.params_from_ini(ini)
+    G = _field(U0.shape[1:], 3, 13)
+    Ug, dg, tg = run_gpu(ini, U0, 4, G=G, exact_fp=1, kchunk=12)
+    Uo, do, to, p = run_oracle(ini, U0, 4, G=G)
+    assert np.array_equal(dg, do)
+    assert np.array_equal(interior(Ug, p.gw, p.dim), interior(Uo, p.gw, p.dim))

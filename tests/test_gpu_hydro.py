@@ -211,3 +211,25 @@ def test_state_transfer_in_several_chunks():
     gw = p.ghost_width
     a = np.transpose(got, (3, 2, 1, 0))[:, gw:-gw, gw:-gw, gw:-gw]
     assert np.array_equal(a, U0[:, gw:-gw, gw:-gw, gw:-gw].astype(np.float32).astype(np.float64))
+
+
+@pytest.mark.parametrize("prec", [ek.EK_PREC_FP64, ek.EK_PREC_MIXED])
+def test_tensor_copy_staging_matches_plain_loads(prec):
+    # interior planes staged by tensor copies (isize % 4 == 0, tiles whose halo
+    # is interior) give the same bits as the plain boundary-mapped loads
+    ini, U0 = P.smooth_random(dim=3, nx=68, ny=52, nz=21, seed=51, bc=(1, 2, 3, 3, 2, 1), slope_type=2.0,
+                              nsteps=6)
+    out = []
+    for no_tma in (0, 1):
+        U, d, _, _ = run_gpu(ini, U0, 6, precision=prec, no_tma=no_tma, kchunk=8)
+        out.append((U, d))
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][0], out[1][0])
+
+
+def test_tensor_copy_staging_exact_matches_oracle():
+    ini, U0 = P.blast_3d(n=64, nsteps=5)
+    Ug, dg, tg, _ = run_gpu(ini, U0, 5, exact_fp=1, kchunk=16)
+    Uo, do, to, p = run_oracle(ini, U0, 5)
+    assert np.array_equal(dg, do)
+    assert np.array_equal(interior(Ug, p.gw, p.dim), interior(Uo, p.gw, p.dim))
