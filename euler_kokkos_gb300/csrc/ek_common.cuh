@@ -568,4 +568,29 @@ mbar_wait(unsigned long long * bar, unsigned parity, unsigned long long limit_ns
   }
 }
 
+
+// Per-thread asynchronous copies global -> shared memory (element gathers
+// whose source addresses follow the boundary mapping); completion is waited
+// for by the issuing thread (cp.async.wait_all) before a block barrier.
+template <int BYTES>
+__device__ __forceinline__ void
+cp_async(void * dst, const void * src)
+{
+  static_assert(BYTES == 4 || BYTES == 8, "cp.async element size");
+  if constexpr (BYTES == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void
+cp_async_commit()
+{
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void
+cp_async_wait_all()
+{
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 } // namespace EK_NS

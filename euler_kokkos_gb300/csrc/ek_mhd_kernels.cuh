@@ -334,7 +334,11 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
   using T = TraceTile<TX, TY>;
   constexpr int NT = TX * TY;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R * sB = reinterpret_cast<R *>(smem_raw); // [4][3][BY][BX] face fields (storage precision R)
+  // raw copies of the next face-field plane (FP64) and hydro plane (storage
+  // type S), landed by asynchronous copies one plane ahead
+  double * rawB = reinterpret_cast<double *>(smem_raw); // [3][BY][BX]
+  S *      rawU = reinterpret_cast<S *>(rawB + T::BP);  // [5][QY][QX]
+  R * sB = reinterpret_cast<R *>(rawU + 5 * T::QX * T::QY); // [4][3][BY][BX] face fields (storage precision R)
   R * sQ = sB + 4 * T::BP;                  // [3][8][QY][QX]
   R *      sE = sQ + 3 * T::QP;                                // [2][3][EY][EX]
 
@@ -362,9 +366,45 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
         dst[(comp * T::BY + y) * T::BX + x] = to_r<R>(load_face<S>(m, P, s, comp));
     }
   };
-  // primitives of plane gk from the hydro variables and the face planes
-  // bslot (gk) and bslot1 (gk+1)
-  auto load_Q = [&](int gk, int slot, int bs0, int bs1) {
+  // the same plane through rawB: issue the copies, then (after this thread's
+  // cp.async.wait_all) convert the cells this thread copied
+  auto issue_B = [&](int gk) {
+    for (int c = threadIdx.x; c < T::BX * T::BY; c += NT)
+    {
+      const int     x = c % T::BX, y = c / T::BX;
+      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+#pragma unroll
+      for (int comp = 0; comp < 3; ++comp)
+        cp_async<8>(rawB + (comp * T::BY + y) * T::BX + x, m.b + comp * P.vstride + s.off);
+    }
+  };
+  auto convert_B = [&](int gk, int slot) {
+    R * dst = sB + slot * T::BP;
+    for (int c = threadIdx.x; c < T::BX * T::BY; c += NT)
+    {
+      const int     x = c % T::BX, y = c / T::BX;
+      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+#pragma unroll
+      for (int comp = 0; comp < 3; ++comp)
+      {
+        const int i = (comp * T::BY + y) * T::BX + x;
+        dst[i] = to_r<R>(neg_if(rawB[i], flips(s, IA + comp, 1)));
+      }
+    }
+  };
+  auto issue_U = [&](int gk) {
+    for (int c = threadIdx.x; c < T::QX * T::QY; c += NT)
+    {
+      const int     x = c % T::QX, y = c / T::QX;
+      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        cp_async<sizeof(S)>(rawU + (v * T::QY + y) * T::QX + x, m.h + v * P.vstride + s.off);
+    }
+  };
+  // primitives of plane gk from the hydro variables (global memory, or rawU
+  // when from_raw) and the face planes bslot (gk) and bslot1 (gk+1)
+  auto load_Q = [&](int gk, int slot, int bs0, int bs1, bool from_raw) {
     R *       dst = sQ + slot * T::QP;
     const R * B0 = sB + bs0 * T::BP;
     const R * B1 = sB + bs1 * T::BP;
@@ -373,7 +413,14 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
       const int     x = c % T::QX, y = c / T::QX;
       const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
       R             u[5], q[8];
-      load_hydro<S, R>(m, P, s, u);
+      if (from_raw)
+      {
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          u[v] = neg_if((R)rawU[(v * T::QY + y) * T::QX + x], flips(s, v, 1));
+      }
+      else
+        load_hydro<S, R>(m, P, s, u);
       R bl[3], br[3];
       // sB x index = global - (c0-1): the Q cell at x has B index x
       bl[0] = B0[(0 * T::BY + y) * T::BX + x];
@@ -439,13 +486,17 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
   auto qsl = [](int k) { return (k + 6) % 3; };
   auto esl = [](int k) { return (k + 4) % 2; };
 
-  // prologue: face planes k0-1..k0+1, Q(k0-1), Q(k0), E(k0)
+  // prologue: face planes k0-1..k0+1, Q(k0-1), Q(k0), E(k0); the copies of
+  // face plane k0+2 and hydro plane k0+1 start here
   load_B(k0 - 1, bsl(k0 - 1));
   load_B(k0, bsl(k0));
   load_B(k0 + 1, bsl(k0 + 1));
+  issue_B(k0 + 2);
+  issue_U(k0 + 1);
+  cp_async_commit();
   __syncthreads();
-  load_Q(k0 - 1, qsl(k0 - 1), bsl(k0 - 1), bsl(k0));
-  load_Q(k0, qsl(k0), bsl(k0), bsl(k0 + 1));
+  load_Q(k0 - 1, qsl(k0 - 1), bsl(k0 - 1), bsl(k0), false);
+  load_Q(k0, qsl(k0), bsl(k0), bsl(k0 + 1), false);
   __syncthreads();
   compute_E(esl(k0), qsl(k0 - 1), qsl(k0), bsl(k0 - 1), bsl(k0));
 
@@ -455,10 +506,19 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
   const long long ost = P.vstride;
   for (int k = k0; k < k1; ++k)
   {
-    load_B(k + 2, bsl(k + 2));
+    // face plane k+2 and hydro plane k+1 were copied during the previous
+    // plane's work: convert them, then start the next plane's copies
+    cp_async_wait_all();
+    convert_B(k + 2, bsl(k + 2));
     __syncthreads();
-    load_Q(k + 1, qsl(k + 1), bsl(k + 1), bsl(k + 2));
+    load_Q(k + 1, qsl(k + 1), bsl(k + 1), bsl(k + 2), true);
     __syncthreads();
+    if (k + 1 < k1)
+    {
+      issue_B(k + 3);
+      issue_U(k + 2);
+      cp_async_commit();
+    }
     compute_E(esl(k + 1), qsl(k), qsl(k + 1), bsl(k), bsl(k + 1));
     __syncthreads();
     if (own)
@@ -472,6 +532,7 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
     }
     __syncthreads();
   }
+  cp_async_wait_all(); // no copy may land after the block has left
 }
 
 // ---------------------------------------------------------------------------
@@ -738,11 +799,12 @@ mhd_divb_kernel(const void * __restrict__ U, KParams P, unsigned long long * key
   block_max_commit<256>(kmax, key);
 }
 
-template <class R>
+template <class S, class R>
 constexpr size_t
 mhd_trace_smem(int TX, int TY)
 {
-  return sizeof(R) * (4 * 3 * (TX + 3) * (TY + 3) + 3 * 8 * (TX + 2) * (TY + 2) + 2 * 3 * (TX + 1) * (TY + 1));
+  return sizeof(double) * 3 * (TX + 3) * (TY + 3) + sizeof(S) * 5 * (TX + 2) * (TY + 2) +
+         sizeof(R) * (4 * 3 * (TX + 3) * (TY + 3) + 3 * 8 * (TX + 2) * (TY + 2) + 2 * 3 * (TX + 1) * (TY + 1));
 }
 template <class R>
 constexpr size_t
@@ -770,7 +832,7 @@ mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams 
   if (phase == 1)
   {
     auto       k = mhd_trace_kernel<S, R, MT_TX, MT_TY>;
-    const int  sm = (int)mhd_trace_smem<R>(MT_TX, MT_TY);
+    const int  sm = (int)mhd_trace_smem<S, R>(MT_TX, MT_TY);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e != cudaSuccess)
       return e;
