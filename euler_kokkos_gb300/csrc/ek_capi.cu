@@ -180,8 +180,15 @@ validate(const ek_params & p)
     return fail(EK_ERR_UNSUPPORTED, "MHD: riemann must be llf, hll or hlld");
   if (p.slope_type != 1.0 && p.slope_type != 2.0)
     return fail(EK_ERR_UNSUPPORTED, "slope_type must be 1 (minmod) or 2 (MC)");
-  if (p.implementation_version != 0)
-    return fail(EK_ERR_UNSUPPORTED, "only implementationVersion=0 is implemented");
+  // implementationVersion (SolverHydroMuscl.cpp:234-293, SolverMHDMuscl.cpp:397-445,
+  // 490-560): hydro 1 is version 0's arithmetic split into more kernels (the
+  // same bits); hydro 2 adds the face fluxes to the cells with atomics
+  // (version 0's results up to the summation order).  Both run the fused
+  // version-0 step.  The MHD versions 1 and 2 compute other numbers.
+  if (p.implementation_version < 0 || p.implementation_version > 2)
+    return fail(EK_ERR_INVALID, "implementationVersion must be 0, 1 or 2");
+  if (p.mhd && p.implementation_version != 0)
+    return fail(EK_ERR_UNSUPPORTED, "MHD: implementationVersion 1 and 2 compute another scheme; use 0");
   if (p.cIso > 0 || p.Omega0 > 0)
     return fail(EK_ERR_UNSUPPORTED, "isothermal and shearing-box terms are not implemented");
   if (p.exact_fp && p.precision != EK_PREC_FP64)

@@ -351,6 +351,26 @@ def run_reference(ini_text: str, U0: np.ndarray, nsteps: int, workdir: str, fast
     return read_ekst(out)
 
 
+def run_reference_deck(ini_text: str, nsteps: int, workdir: str):
+    """Run the reference's own solver (oracle/_ref) from its own init (no
+    injected state); returns the initial state too (EK_REF_DUMP0)."""
+    if not os.path.exists(REF_RUN):
+        raise FileNotFoundError(REF_RUN)
+    workdir = os.path.abspath(workdir)
+    os.makedirs(workdir, exist_ok=True)
+    ini = os.path.join(workdir, "deck.ini")
+    out = os.path.join(workdir, "out.ekst")
+    u0 = os.path.join(workdir, "u0.ekst")
+    with open(ini, "w") as f:
+        f.write(ini_text)
+    env = dict(os.environ, EK_REF_DUMP0=u0)
+    subprocess.run([REF_RUN, ini, str(nsteps), out], check=True, cwd=workdir, env=env,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    res = read_ekst(out)
+    res["U0"] = read_ekst(u0)["U"]
+    return res
+
+
 # --------------------------------------------------------------------------
 # C restatement
 # --------------------------------------------------------------------------

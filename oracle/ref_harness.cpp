@@ -12,7 +12,7 @@
 //   * a dump of the final state and of the dt sequence in the EKST format.
 //
 // usage: ref_run <file.ini> <nsteps> <out.ekst> [<U0.ekst>]
-// (environment: EK_REF_SAVE, EK_REF_GRAVITY -- see run())
+// (environment: EK_REF_SAVE, EK_REF_GRAVITY, EK_REF_DUMP0 -- see run())
 //
 // EKST format (little endian): char magic[8]="EKSTATE1"; int64 dim, nbvar,
 // isize, jsize, ksize, ghost, iteration, ndt; double t; double dt[ndt];
@@ -79,6 +79,33 @@ copy_out(const View & v, std::vector<double> & buf, int nb, int is, int js, int 
         }
 }
 
+// one EKST file: header, dt sequence, state (copy_out layout)
+static int
+write_ekst(const char * path, int dim, int nb, int is, int js, int ks, int ghost, int iteration, double t,
+           const std::vector<double> & dts, const std::vector<double> & buf)
+{
+  FILE * f = std::fopen(path, "wb");
+  if (!f)
+    return 3;
+  EkHeader h{};
+  std::memcpy(h.magic, "EKSTATE1", 8);
+  h.dim = dim;
+  h.nbvar = nb;
+  h.isize = is;
+  h.jsize = js;
+  h.ksize = ks;
+  h.ghost = ghost;
+  h.iteration = iteration;
+  h.ndt = (int64_t)dts.size();
+  h.t = t;
+  std::fwrite(&h, sizeof h, 1, f);
+  if (!dts.empty())
+    std::fwrite(dts.data(), sizeof(double), dts.size(), f);
+  std::fwrite(buf.data(), sizeof(double), buf.size(), f);
+  std::fclose(f);
+  return 0;
+}
+
 template <class Solver>
 static int
 run(Solver * s, euler_kokkos::HydroParams & p, int nsteps, const char * out, const char * in, bool mhd)
@@ -141,6 +168,16 @@ run(Solver * s, euler_kokkos::HydroParams & p, int nsteps, const char * out, con
     s->compute_dt();
   }
   (void)mhd;
+  // EK_REF_DUMP0=<file>: the state the run starts from (the reference's own
+  // init when no state is injected)
+  const char * dump0 = std::getenv("EK_REF_DUMP0");
+  if (dump0 && dump0[0])
+  {
+    std::vector<double> b0;
+    copy_out(s->U, b0, nb, is, js, ks);
+    if (write_ekst(dump0, dim, nb, is, js, ks, p.ghostWidth, s->m_iteration, s->m_t, {}, b0) != 0)
+      return 3;
+  }
   std::vector<double> dts;
   for (int n = 0; n < nsteps && !s->finished(); ++n)
   {
@@ -157,26 +194,7 @@ run(Solver * s, euler_kokkos::HydroParams & p, int nsteps, const char * out, con
     copy_out(s->U, buf, nb, is, js, ks);
   else
     copy_out(s->U2, buf, nb, is, js, ks);
-  FILE * f = std::fopen(out, "wb");
-  if (!f)
-    return 3;
-  EkHeader h{};
-  std::memcpy(h.magic, "EKSTATE1", 8);
-  h.dim = dim;
-  h.nbvar = nb;
-  h.isize = is;
-  h.jsize = js;
-  h.ksize = ks;
-  h.ghost = p.ghostWidth;
-  h.iteration = s->m_iteration;
-  h.ndt = (int64_t)dts.size();
-  h.t = s->m_t;
-  std::fwrite(&h, sizeof h, 1, f);
-  if (!dts.empty())
-    std::fwrite(dts.data(), sizeof(double), dts.size(), f);
-  std::fwrite(buf.data(), sizeof(double), buf.size(), f);
-  std::fclose(f);
-  return 0;
+  return write_ekst(out, dim, nb, is, js, ks, p.ghostWidth, s->m_iteration, s->m_t, dts, buf);
 }
 
 int

@@ -85,6 +85,83 @@ CASES = {
 }
 
 
+# The reference's own input decks (settings/*.ini; the MPI decks excepted),
+# at reduced grid sizes, run from the reference's OWN init for a few steps:
+# fixture name: (deck file, mesh overrides, steps, implementationVersion
+# override or None).  Hydro version 2 only changes the summation order of the
+# update (atomics); the MHD versions 1 and 2 compute other numbers.  Those
+# decks run at version 0 here; the round-off equivalence of hydro version 2
+# is pinned by the *_v2 fixtures.
+DECKS = {
+    "deck_blast_2D": ("test_blast_2D.ini", {"nx": 32, "ny": 48}, 10, None),
+    "deck_blast_3D": ("test_blast_3D.ini", {"nx": 16, "ny": 12, "nz": 8}, 6, None),
+    "deck_four_quadrant_2D": ("test_four_quadrant_2D.ini", {"nx": 32, "ny": 32}, 10, None),
+    "deck_four_quadrant_3D": ("test_four_quadrant_3D.ini", {"nx": 12, "ny": 12, "nz": 12}, 5, None),
+    "deck_implode_2D": ("test_implode_2D.ini", {"nx": 32, "ny": 16}, 10, None),
+    "deck_implode_3D": ("test_implode_3D.ini", {"nx": 16, "ny": 12, "nz": 8}, 6, None),
+    "deck_mhd_blast_2D": ("test_mhd_blast_2D.ini", {"nx": 32, "ny": 48}, 6, None),
+    "deck_mhd_blast_3D": ("test_mhd_blast_3D.ini", {"nx": 12, "ny": 12, "nz": 12}, 4, 0),
+    "deck_mhd_brio_wu_2d_x": ("test_mhd_brio_wu_2d_x.ini", {"nx": 64, "ny": 8}, 10, 0),
+    "deck_mhd_brio_wu_2d_y": ("test_mhd_brio_wu_2d_y.ini", {"nx": 8, "ny": 64}, 10, 0),
+    "deck_mhd_brio_wu_3d_x": ("test_mhd_brio_wu_3d_x.ini", {"nx": 48, "ny": 6, "nz": 6}, 6, 0),
+    "deck_mhd_brio_wu_3d_y": ("test_mhd_brio_wu_3d_y.ini", {"nx": 6, "ny": 48, "nz": 6}, 6, 0),
+    "deck_mhd_brio_wu_3d_z": ("test_mhd_brio_wu_3d_z.ini", {"nx": 6, "ny": 6, "nz": 48}, 6, 0),
+    "deck_mhd_orszag_tang_2D": ("test_mhd_orszag_tang_2D.ini", {"nx": 32, "ny": 32}, 8, None),
+    "deck_mhd_orszag_tang_3D": ("test_mhd_orszag_tang_3D.ini", {"nx": 16, "ny": 16, "nz": 8}, 5, None),
+    "deck_mhd_rotor": ("test_mhd_rotor.ini", {"nx": 32, "ny": 32}, 8, None),
+    "deck_gresho_vortex_2D": ("test_muscl_gresho_vortex_2D.ini", {"nx": 32, "ny": 32}, 8, None),
+    "deck_isentropic_vortex_2d": ("test_muscl_isentropic_vortex_2d.ini", {"nx": 32, "ny": 32}, 8, None),
+    "deck_kelvin_helmholtz_2D": ("test_muscl_kelvin_helmholtz_2D.ini", {"nx": 32, "ny": 32}, 8, None),
+    "deck_kelvin_helmholtz_2D_mhd": ("test_muscl_kelvin_helmholtz_2D_mhd.ini", {"nx": 32, "ny": 32}, 6, None),
+    "deck_kelvin_helmholtz_3D": ("test_muscl_kelvin_helmholtz_3D.ini", {"nx": 16, "ny": 16, "nz": 16}, 5, None),
+    "deck_rayleigh_taylor_2d": ("test_rayleigh_taylor_2d.ini", {"nx": 20, "ny": 60}, 10, None),
+    "deck_rayleigh_taylor_3d": ("test_rayleigh_taylor_3d.ini", {"nx": 10, "ny": 10, "nz": 30}, 5, None),
+    "deck_mhd_fieldloop2d": ("mhd_fieldloop2d.ini", {"nx": 32, "ny": 20}, 8, None),
+    "deck_mhd_fieldloop3d": ("mhd_fieldloop3d.ini", {"nx": 16, "ny": 8, "nz": 8}, 5, None),
+    # the reference's atomic-update versions, as the decks ask for them
+    "deck_implode_2D_v2": ("test_implode_2D.ini", {"nx": 32, "ny": 16}, 10, 2),
+    "deck_kelvin_helmholtz_3D_v2": ("test_muscl_kelvin_helmholtz_3D.ini", {"nx": 16, "ny": 16, "nz": 16}, 5, 2),
+}
+SETTINGS = os.path.join(os.environ.get("EK_REFERENCE", "/root/reference"), "settings")
+
+
+def deck_text(fname, mesh, nsteps, version):
+    """The deck with its mesh resized, nStepmax = nsteps, output off and
+    (optionally) implementationVersion replaced."""
+    out, sec = [], ""
+    with open(os.path.join(SETTINGS, fname)) as f:
+        lines = f.read().splitlines()
+    for line in lines:
+        t = line.strip()
+        if t.startswith("["):
+            sec = t[1:t.index("]")].lower() if "]" in t else ""
+            out.append(line)
+            continue
+        key = t.split("=", 1)[0].strip() if "=" in t and not t.startswith(("#", ";")) else None
+        if sec == "mesh" and key in mesh:
+            line = "%s=%d" % (key, mesh[key])
+        elif sec == "run" and key and key.lower() == "nstepmax":
+            line = "nStepmax=%d" % nsteps
+        elif sec == "output" and key and key.lower() in ("vtk_enabled", "hdf5_enabled", "pnetcdf_enabled"):
+            line = "%s=false" % key
+        elif sec == "other" and key == "implementationVersion" and version is not None:
+            line = "implementationVersion=%d" % version
+        out.append(line)
+    return "\n".join(out) + "\n"
+
+
+def make_decks(names, out_dir):
+    work = tempfile.mkdtemp(prefix="ek_deck_")
+    for name in names:
+        fname, mesh, nsteps, version = DECKS[name]
+        ini = deck_text(fname, mesh, nsteps, version)
+        res = eko.run_reference_deck(ini, nsteps, os.path.join(work, name))
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), ini=np.array(ini), U0=res["U0"],
+                            U=res["U"], dts=res["dts"], t=np.array(res["t"]),
+                            iteration=np.array(res["iteration"]))
+        print(name, res["U0"].shape, "steps", len(res["dts"]), "nan", int(np.isnan(res["U"]).sum()))
+
+
 def _with_field(case, seed):
     """(ini, U0) -> (ini, U0, G): a seeded smooth gravity field, one
     component per dimension, on every cell (ghosts included)."""
@@ -145,8 +222,9 @@ def make_vtk(names):
 def main():
     out_dir = os.path.dirname(os.path.abspath(__file__))
     work = tempfile.mkdtemp(prefix="ek_golden_")
-    names = sys.argv[1:] or list(CASES) + list(VTK_CASES)
+    names = sys.argv[1:] or list(CASES) + list(VTK_CASES) + list(DECKS)
     make_vtk([n for n in names if n in VTK_CASES])
+    make_decks([n for n in names if n in DECKS], out_dir)
     for name in [n for n in names if n in CASES]:
         build, nsteps = CASES[name]
         case = build()

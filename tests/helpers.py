@@ -8,17 +8,36 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def golden_cases(kind=None):
-    """Names of the golden fixtures; kind: 'hydro', 'mhd' (3D), 'mhd2d' or None."""
+def _solver_of(name):
+    with np.load(os.path.join(GOLDEN, name + ".npz")) as z:
+        ini = str(z["ini"])
+    solver = version = None
+    for line in ini.splitlines():
+        t = line.strip()
+        if t.startswith("solver_name="):
+            solver = t.split("=", 1)[1].strip()
+        elif t.startswith("implementationVersion="):
+            version = int(t.split("=", 1)[1].split()[0])
+    return solver, version or 0
+
+
+def golden_cases(kind=None, bitwise=True):
+    """Names of the golden fixtures; kind: 'hydro', 'mhd' (3D), 'mhd2d' or None.
+    bitwise: the fixtures the version-0 arithmetic reproduces bit for bit
+    (False: the ones written by the reference's atomic-update hydro version 2,
+    equal up to the summation order)."""
     names = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz")))
-    is_mhd = [n.startswith("mhd") or n.startswith("ot") for n in names]
-    if kind == "hydro":
-        return [n for n, m in zip(names, is_mhd) if not m]
-    if kind == "mhd":
-        return [n for n, m in zip(names, is_mhd) if m and "2d" not in n]
-    if kind == "mhd2d":
-        return [n for n, m in zip(names, is_mhd) if m and "2d" in n]
-    return names
+    out = []
+    for n in names:
+        solver, version = _solver_of(n)
+        mhd = solver.startswith("MHD")
+        atomic = not mhd and version == 2
+        if atomic == bitwise:
+            continue
+        if kind is None or (kind == "hydro" and not mhd) or (kind == "mhd" and solver == "MHD_Muscl_3D") or \
+                (kind == "mhd2d" and solver == "MHD_Muscl_2D"):
+            out.append(n)
+    return out
 
 
 def load_golden(name):

@@ -128,11 +128,21 @@ def test_create_without_gpu_fails_cleanly():
 def test_create_rejects_unsupported_configurations():
     # validation happens before any device call
     p = ek.params_from_ini(DECK)
-    for bad in (dict(riemann=4), dict(riemann=7), dict(slope_type=3.0), dict(implementation_version=1),
+    for bad in (dict(riemann=4), dict(riemann=7), dict(slope_type=3.0), dict(implementation_version=3),
                 dict(nx=1, isize=5), dict(exact_fp=1, precision=1)):
         with pytest.raises(ek.EkError) as e:
             ek.Solver(p.copy(**bad))
         assert e.value.status in (1, 2), bad
+    # the MHD implementationVersions 1 and 2 compute another scheme in the reference
+    from euler_kokkos_gb300 import problems as P
+
+    for dim, v in ((3, 2), (3, 1), (2, 2), (2, 1)):
+        ini = (P.orszag_tang_3d(n=8, nsteps=1) if dim == 3 else P.orszag_tang_2d(n=8, nsteps=1))[0]
+        q = ek.params_from_ini(ini.replace("implementationVersion=0", "implementationVersion=%d" % v))
+        assert q.implementation_version == v
+        with pytest.raises(ek.EkError) as e:
+            ek.Solver(q)
+        assert e.value.status == 2, (dim, v)
 
 
 def test_gravity_sections_parse_like_reference():

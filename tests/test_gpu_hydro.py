@@ -233,3 +233,17 @@ def test_tensor_copy_staging_exact_matches_oracle():
     Uo, do, to, p = run_oracle(ini, U0, 5)
     assert np.array_equal(dg, do)
     assert np.array_equal(interior(Ug, p.gw, p.dim), interior(Uo, p.gw, p.dim))
+
+
+@pytest.mark.parametrize("name", golden_cases("hydro", bitwise=False))
+def test_atomic_update_version_fixtures_to_roundoff(name):
+    # decks run by the reference at implementationVersion 2 (face fluxes added
+    # with atomics): the fused version-0 step equals them up to the summation order
+    g = load_golden(name)
+    ini = str(g["ini"])
+    p = eko.params_from_ini(ini)
+    assert ek.params_from_ini(ini).implementation_version == 2
+    U, dts, t, it = run_gpu(ini, g["U0"], len(g["dts"]), exact_fp=1)
+    assert np.max(np.abs(dts - g["dts"]) / g["dts"]) <= 1e-13
+    err = rel_linf(interior(U, p.gw, p.dim), interior(g["U"], p.gw, p.dim))
+    assert np.all(err <= 1e-13), err

@@ -51,3 +51,19 @@ def test_oracle_implode_symmetry():
     o.run(10)
     rho = interior(o.state(), p.gw, p.dim)[0, 0]
     assert np.allclose(rho, rho.T, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("name", golden_cases(bitwise=False))
+def test_oracle_matches_atomic_update_versions_to_roundoff(name):
+    # fixtures written by the reference's hydro implementationVersion 2, which
+    # adds the face fluxes with atomics: version 0's arithmetic (the oracle)
+    # equals them up to the summation order
+    g = load_golden(name)
+    p = eko.params_from_ini(str(g["ini"]))
+    o = eko.Oracle(p, g["U0"])
+    dts = o.run(len(g["dts"]))
+    assert np.max(np.abs(dts - g["dts"]) / g["dts"]) <= 1e-13
+    a, b = interior(o.state(), p.gw, p.dim), interior(g["U"], p.gw, p.dim)
+    scale = np.abs(b).reshape(b.shape[0], -1).max(axis=1)
+    err = np.abs(a - b).reshape(b.shape[0], -1).max(axis=1) / np.where(scale > 0, scale, 1)
+    assert np.all(err <= 1e-13), err
