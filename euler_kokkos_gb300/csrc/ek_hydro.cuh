@@ -22,6 +22,16 @@ template <class R>
 __device__ __forceinline__ R
 slope1(R q, R qp, R qm, R st)
 {
+  if constexpr (sizeof(R) == 4)
+  {
+    // the same limiter with the sign taken by copysign and the zero case by
+    // one select (FP32 form; signed zeros may differ)
+    const float dlft = st * (q - qm);
+    const float drgt = st * (qp - q);
+    const float dcen = 0.5f * (qp - qm);
+    const float m = fminf(fminf(fabsf(dlft), fabsf(drgt)), fabsf(dcen));
+    return (dlft * drgt > 0.f) ? copysignf(m, dcen) : 0.f;
+  }
   const R dlft = st * (q - qm);
   const R drgt = st * (qp - q);
   const R dcen = R(0.5) * (qp - qm);
@@ -212,7 +222,24 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
   }
 
   R ro, uo, ptoto, etoto;
-  if (SL > R(0))
+  if constexpr (sizeof(R) == 4)
+  {
+    // FP32: the reference's four-way choice without branches -- the star
+    // state is formed once, on the side of the contact (left when ustar > 0)
+    const bool  left = ustar > 0.f;
+    const float Sk = left ? SL : SR, rk = left ? rl : rr, uk = left ? ul : ur;
+    const float ek = left ? etotl : etotr, pk = left ? ptotl : ptotr;
+    const float is = rcp_a(Sk - ustar);
+    const float rs = rk * (Sk - uk) * is;
+    const float es = ((Sk - uk) * ek - pk * uk + ptotstar * ustar) * is;
+    const bool  cL = SL > 0.f;                       // left state
+    const bool  cR = !cL && !left && !(SR > 0.f);    // right state
+    ro = cL ? rl : (cR ? rr : rs);
+    uo = cL ? ul : (cR ? ur : ustar);
+    ptoto = cL ? ptotl : (cR ? ptotr : ptotstar);
+    etoto = cL ? etotl : (cR ? etotr : es);
+  }
+  else if (SL > R(0))
   {
     ro = rl;
     uo = ul;
@@ -223,33 +250,15 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
   {
     uo = ustar;
     ptoto = ptotstar;
-    if constexpr (sizeof(R) == 4)
-    {
-      const float is = rcp_a(SL - ustar);
-      ro = rl * (SL - ul) * is;
-      etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) * is;
-    }
-    else
-    {
-      ro = rl * (SL - ul) / (SL - ustar);
-      etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) / (SL - ustar);
-    }
+    ro = rl * (SL - ul) / (SL - ustar);
+    etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) / (SL - ustar);
   }
   else if (SR > R(0))
   {
     uo = ustar;
     ptoto = ptotstar;
-    if constexpr (sizeof(R) == 4)
-    {
-      const float is = rcp_a(SR - ustar);
-      ro = rr * (SR - ur) * is;
-      etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) * is;
-    }
-    else
-    {
-      ro = rr * (SR - ur) / (SR - ustar);
-      etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) / (SR - ustar);
-    }
+    ro = rr * (SR - ur) / (SR - ustar);
+    etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) / (SR - ustar);
   }
   else
   {
