@@ -624,29 +624,28 @@ mag_riemann2d_hlld_f32(const EdgeQ<float> & LL, const EdgeQ<float> & RL, const E
   const float BstarR = (SAT * BstarRR - SAB * BstarRL) * iAy;
   const float BstarL = (SAT * BstarLR - SAB * BstarLL) * iAy;
 
-  float     E = 0.f, tmpE;
-  const int SB_pos = (int)(1 + copysignf(1.f, SB)) / 2, SB_neg = 1 - SB_pos;
-  const int ST_pos = (int)(1 + copysignf(1.f, ST)) / 2, ST_neg = 1 - ST_pos;
-  const int SL_pos = (int)(1 + copysignf(1.f, SL)) / 2, SL_neg = 1 - SL_pos;
-  const int SR_pos = (int)(1 + copysignf(1.f, SR)) / 2, SR_neg = 1 - SR_pos;
+  // the reference's sign masks (1 + copysign(1, S)) / 2 as sign-bit tests and
+  // its mask-weighted sums as selects: exactly one term of each sum is live
+  const bool SBp = !signbit(SB), STp = !signbit(ST), SLp = !signbit(SL), SRp = !signbit(SR);
+  float      E = 0.f, tmpE;
 
   tmpE = (SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL) * iAx * iAy -
          SAT * SAB * iAy * (AstarT - AstarB) + SAR * SAL * iAx * (BstarR - BstarL);
-  E += (float)(SB_neg * ST_pos * SL_neg * SR_pos) * tmpE;
+  E += (!SBp && STp && !SLp && SRp) ? tmpE : 0.f;
 
   tmpE = (SAR * EstarLLx - SAL * EstarRLx + SAR * SAL * (bRL - bLL)) * iAx;
-  tmpE = (float)SL_pos * ELL + (float)(SL_neg * SR_neg) * ERL + (float)(SL_neg * SR_pos) * tmpE;
-  E += (float)SB_pos * tmpE;
+  tmpE = SLp ? ELL : (!SRp ? ERL : tmpE);
+  E += SBp ? tmpE : 0.f;
 
   tmpE = (SAR * EstarLRx - SAL * EstarRRx + SAR * SAL * (bRR - bLR)) * iAx;
-  tmpE = (float)SL_pos * ELR + (float)(SL_neg * SR_neg) * ERR + (float)(SL_neg * SR_pos) * tmpE;
-  E += (float)(SB_neg * ST_neg) * tmpE;
+  tmpE = SLp ? ELR : (!SRp ? ERR : tmpE);
+  E += (!SBp && !STp) ? tmpE : 0.f;
 
   tmpE = (SAT * EstarLLy - SAB * EstarLRy - SAT * SAB * (aLR - aLL)) * iAy;
-  E += (float)(SB_neg * ST_pos * SL_pos) * tmpE;
+  E += (!SBp && STp && SLp) ? tmpE : 0.f;
 
   tmpE = (SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL)) * iAy;
-  E += (float)(SB_neg * ST_pos * SL_neg * SR_neg) * tmpE;
+  E += (!SBp && STp && !SLp && !SRp) ? tmpE : 0.f;
   return E;
 }
 
