@@ -381,7 +381,6 @@ def main():
     args.warmup = max(args.warmup, 3)
 
     rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
 
     if args.impl == "reference":
@@ -391,16 +390,12 @@ def main():
 
     import torch
 
+    from euler_kokkos_gb300.replicas import Replicas
+
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("gloo")
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
+    rep = Replicas()
+    world = rep.world
+    barrier = rep.barrier
 
     def sync():
         torch.cuda.synchronize()
@@ -418,12 +413,7 @@ def main():
     clocks = clk.summary()
     fp64 = measure_workload(ek, "hydro3d", ek.EK_PREC_FP64, ini, U0, args.steps, args.warmup, sync)
 
-    def maxt(ms):
-        if dist is None:
-            return ms
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    maxt = rep.max
 
     ms_mixed, ms_fp64 = maxt(mixed["ms"]), maxt(fp64["ms"])
     cells = mixed["cells"]
@@ -544,8 +534,7 @@ def main():
     barrier()
     if line is not None:
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    rep.close()
 
 
 if __name__ == "__main__":
