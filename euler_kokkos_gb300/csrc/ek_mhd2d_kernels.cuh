@@ -465,13 +465,18 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
     }
     else
     {
-      // FP64 island: the face fields (CT) and Bz accumulate in FP64
-      bz += f2d(sFx[5 * T::FXS + fx0] * dtdx);
-      bz -= f2d(sFx[5 * T::FXS + fx0 + 1] * dtdx);
-      bz += f2d(sFy[5 * T::FYS + fy0] * dtdy);
-      bz -= f2d(sFy[5 * T::FYS + fy0 + TX] * dtdy);
-      bx += (f2d(e01) - f2d(e00)) * ddtdy;
-      by -= (f2d(e10) - f2d(e00)) * ddtdx;
+      // FP64 island: the face fields (CT) accumulate in FP64 so div B stays at
+      // FP64 round-off (one subtraction and one fused multiply-add each).  Bz
+      // (cell-centred in 2D, outside div B) is advanced in FP32 like the
+      // hydro variables; its storage stays FP64.
+      float bzf = to_r<float>(bz);
+      bzf += sFx[5 * T::FXS + fx0] * dtdx;
+      bzf -= sFx[5 * T::FXS + fx0 + 1] * dtdx;
+      bzf += sFy[5 * T::FYS + fy0] * dtdy;
+      bzf -= sFy[5 * T::FYS + fy0 + TX] * dtdy;
+      bz = f2d(bzf);
+      bx = fma(f2d(e01) - f2d(e00), ddtdy, bx);
+      by = fma(f2d(e00) - f2d(e10), ddtdx, by);
     }
     bout[0 * st + off] = bx;
     bout[1 * st + off] = by;

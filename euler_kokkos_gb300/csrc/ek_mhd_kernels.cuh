@@ -727,13 +727,14 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       }
       else
       {
-        // FP64 island: the CT update keeps div B at FP64 round-off
-        bx += (f2d(Ezp[ezi + (TX + 1)]) - f2d(Ezp[ezi])) * ddtdy;
-        by -= (f2d(Ezp[ezi + 1]) - f2d(Ezp[ezi])) * ddtdx;
-        bx -= (f2d(Ey[eyi]) - f2d(Eyp[eyi])) * ddtdz;
-        by += (f2d(Ex[exi]) - f2d(Exp[exi])) * ddtdz;
-        bz += (f2d(Eyp[eyi + 1]) - f2d(Eyp[eyi])) * ddtdx;
-        bz -= (f2d(Exp[exi + TX]) - f2d(Exp[exi])) * ddtdy;
+        // FP64 island: the CT update keeps div B at FP64 round-off (one
+        // subtraction and one fused multiply-add per term)
+        bx = fma(f2d(Ezp[ezi + (TX + 1)]) - f2d(Ezp[ezi]), ddtdy, bx);
+        by = fma(f2d(Ezp[ezi]) - f2d(Ezp[ezi + 1]), ddtdx, by);
+        bx = fma(f2d(Eyp[eyi]) - f2d(Ey[eyi]), ddtdz, bx);
+        by = fma(f2d(Ex[exi]) - f2d(Exp[exi]), ddtdz, by);
+        bz = fma(f2d(Eyp[eyi + 1]) - f2d(Eyp[eyi]), ddtdx, bz);
+        bz = fma(f2d(Exp[exi]) - f2d(Exp[exi + TX]), ddtdy, bz);
       }
       bout[0 * st + off] = bx;
       bout[1 * st + off] = by;
