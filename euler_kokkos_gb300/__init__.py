@@ -143,6 +143,8 @@ def load_library():
         "ek_solver_set_state": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
         "ek_solver_get_state": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
         "ek_solver_set_gravity_field": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
+        "ek_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                                    ctypes.POINTER(ctypes.c_double)]),
         "ek_solver_compute_dt": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_double)]),
         "ek_solver_next_iteration": (ctypes.c_int, [c_p]),
         "ek_solver_run": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
@@ -184,6 +186,17 @@ def load_library():
         f.argtypes = args
     _lib = L
     return L
+
+
+def selftest_bounded_wait(limit_us: int = 2000):
+    """Run the step kernels' bounded mbarrier wait on a barrier that never
+    completes; returns (expired, elapsed_us): every wait must give up after
+    about limit_us and the kernel must return (no hang)."""
+    L = load_library()
+    expired, elapsed = ctypes.c_int(), ctypes.c_double()
+    _check(L.ek_selftest_bounded_wait(int(limit_us), ctypes.byref(expired), ctypes.byref(elapsed)),
+           "selftest_bounded_wait")
+    return bool(expired.value), elapsed.value
 
 
 def _check(status: int, what: str, allow=()):

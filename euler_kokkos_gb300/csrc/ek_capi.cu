@@ -551,6 +551,27 @@ set_state_at(ek_solver * s, const double * U, int layout, double t0)
 }
 
 extern "C" ek_status
+ek_selftest_bounded_wait(int limit_us, int * expired, double * elapsed_us)
+{
+  if (limit_us < 1 || limit_us > 1000000 || !expired || !elapsed_us)
+    return fail(EK_ERR_INVALID, "ek_selftest_bounded_wait: bad argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(EK_ERR_NO_DEVICE, "no CUDA device available");
+  unsigned long long * d = nullptr;
+  unsigned long long   h[2] = { 0, 0 };
+  EK_CUDA(cudaMalloc((void **)&d, sizeof h), "selftest");
+  cudaError_t e = ek_fast::selftest_bounded_wait((unsigned long long)limit_us * 1000ull, d, 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  EK_CUDA(e, "selftest");
+  *expired = h[0] == 128 ? 1 : 0;
+  *elapsed_us = (double)h[1] / 1000.0;
+  return EK_OK;
+}
+
+extern "C" ek_status
 ek_solver_set_gravity_field(ek_solver * s, const double * G, int layout)
 {
   if (!s || (layout != EK_LAYOUT_LEFT && layout != EK_LAYOUT_RIGHT))

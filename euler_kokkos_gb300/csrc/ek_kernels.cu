@@ -206,6 +206,34 @@ ensemble2d_grid(int prec)
 }
 
 #ifndef EK_EXACT_ONLY
+namespace
+{
+__global__ void
+bounded_wait_kernel(unsigned long long limit_ns, unsigned long long * out)
+{
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0)
+    mbar_init(&bar, 1); // one arrival expected; none comes
+  __syncthreads();
+  const unsigned long long t0 = global_ns();
+  const bool               ok = mbar_wait(&bar, 0u, limit_ns);
+  const unsigned long long dt = global_ns() - t0;
+  if (!ok)
+    atomicAdd(out, 1ull);
+  atomicMax(out + 1, dt);
+}
+} // namespace
+
+cudaError_t
+selftest_bounded_wait(unsigned long long limit_ns, unsigned long long * out, cudaStream_t st)
+{
+  cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess)
+    return e;
+  bounded_wait_kernel<<<1, 128, 0, st>>>(limit_ns, out);
+  return cudaGetLastError();
+}
+
 bool
 hydro3d_tensor_map(int prec, const void * U, const KParams & P, CUtensorMap * out)
 {

@@ -54,6 +54,9 @@ cudaError_t ensemble_totals(int prec, const ekc::EnsInstance * insts, int n, con
 // into the state U (precision prec), else fill stage from U.
 cudaError_t convert_stage(bool to_state, int prec, int layout, double * stage, void * U, const KParams & P,
                           int nbvar, long long first, long long count, cudaStream_t st);
+// The bounded mbarrier wait on a barrier nothing completes (one block):
+// out[0] = number of threads whose wait expired, out[1] = longest wait in ns.
+cudaError_t selftest_bounded_wait(unsigned long long limit_ns, unsigned long long * out, cudaStream_t st);
 // Tensor map of a 3D hydro state U (box = the 3D kernel's tile plus halo, all
 // five variables); false when the layout does not allow tensor copies.
 bool hydro3d_tensor_map(int prec, const void * U, const KParams & P, CUtensorMap * out);

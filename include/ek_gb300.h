@@ -167,6 +167,13 @@ ek_status ek_solver_synchronize(ek_solver * s);
 /* Number of kernel launches issued by this solver so far. */
 ek_status ek_solver_launch_count(ek_solver * s, long long * n);
 
+/* Diagnostic: run the bounded mbarrier wait that guards the step kernels'
+ * tensor copies on a barrier nothing completes, with a limit of limit_us
+ * microseconds, on the current device.  *expired = 1 when every thread's wait
+ * gave up (the kernel then left normally), *elapsed_us = the longest wait.
+ * Shows that a copy that never lands ends in an error status, not a hang. */
+ek_status ek_selftest_bounded_wait(int limit_us, int * expired, double * elapsed_us);
+
 /* The CUDA stream (cudaStream_t) all work of the solver is issued on. */
 ek_status ek_solver_stream(ek_solver * s, void ** stream);
 
