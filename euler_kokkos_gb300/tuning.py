@@ -9,7 +9,9 @@ euler_kokkos_gb300.tuning`` builds the library once per candidate set into
 ABI (CUDA events around each launch: ek_solver_set_profiling /
 ek_solver_kernel_time), keeps the fastest candidate of each family and writes
 the choice to ``tuning.json`` beside this file, which build() turns into -D
-flags.  The objective is the mixed-precision (FP32) kernel time, the
+flags.  The workloads are the benchmark's sizes (3D blast and Orszag-Tang
+256^3, 2D Orszag-Tang 4096^2, 2D implode 2048^2): the best tile depends on
+the grid.  The objective is the mixed-precision (FP32) kernel time, the
 performance form; the FP64 build uses the same shapes.  Run it on the GPU it
 tunes for; it needs nvcc and a few minutes.
 """
@@ -28,21 +30,29 @@ TUNING_FILE = os.path.join(HERE, "tuning.json")
 # Candidate sets per kernel family; candidate 0 is the built-in default.
 CANDIDATES = {
     "hydro2d": [{"EK_H2_TX": "32", "EK_H2_TY": "8"}, {"EK_H2_TX": "32", "EK_H2_TY": "4"}, {"EK_H2_TX": "64", "EK_H2_TY": "4"},
-                {"EK_H2_TX": "16", "EK_H2_TY": "16"}, {"EK_H2_TX": "64", "EK_H2_TY": "8"}],
+                {"EK_H2_TX": "16", "EK_H2_TY": "16"}, {"EK_H2_TX": "64", "EK_H2_TY": "8"},
+                {"EK_H2_TX": "16", "EK_H2_TY": "8"}, {"EK_H2_TX": "32", "EK_H2_TY": "16"}],
     "hydro3d": [{"EK_H3_TX": "32", "EK_H3_TY": "8", "EK_H3_MINB_F32": "4", "EK_H3_MINB_F64": "2"},
                 {"EK_H3_TX": "32", "EK_H3_TY": "4", "EK_H3_MINB_F32": "8", "EK_H3_MINB_F64": "4"},
                 {"EK_H3_TX": "64", "EK_H3_TY": "4", "EK_H3_MINB_F32": "4", "EK_H3_MINB_F64": "2"},
                 {"EK_H3_TX": "16", "EK_H3_TY": "16", "EK_H3_MINB_F32": "4", "EK_H3_MINB_F64": "2"},
-                {"EK_H3_TX": "32", "EK_H3_TY": "16", "EK_H3_MINB_F32": "2", "EK_H3_MINB_F64": "1"}],
+                {"EK_H3_TX": "32", "EK_H3_TY": "16", "EK_H3_MINB_F32": "2", "EK_H3_MINB_F64": "1"},
+                {"EK_H3_TX": "16", "EK_H3_TY": "16", "EK_H3_MINB_F32": "3", "EK_H3_MINB_F64": "2"},
+                {"EK_H3_TX": "16", "EK_H3_TY": "8", "EK_H3_MINB_F32": "8", "EK_H3_MINB_F64": "4"}],
     "mhd_trace": [{"EK_MT_TX": "32", "EK_MT_TY": "4"}, {"EK_MT_TX": "16", "EK_MT_TY": "8"}, {"EK_MT_TX": "32", "EK_MT_TY": "8"},
-                  {"EK_MT_TX": "64", "EK_MT_TY": "2"}, {"EK_MT_TX": "16", "EK_MT_TY": "4"}],
+                  {"EK_MT_TX": "64", "EK_MT_TY": "2"}, {"EK_MT_TX": "16", "EK_MT_TY": "4"},
+                  {"EK_MT_TX": "32", "EK_MT_TY": "4", "EK_MT_MINB_F32": "6"}, {"EK_MT_TX": "64", "EK_MT_TY": "4"}],
     "mhd_update": [{"EK_MU_TX": "16", "EK_MU_TY": "8", "EK_MU_MINB_F32": "8"},
                    {"EK_MU_TX": "32", "EK_MU_TY": "4", "EK_MU_MINB_F32": "8"},
                    {"EK_MU_TX": "8", "EK_MU_TY": "16", "EK_MU_MINB_F32": "8"},
                    {"EK_MU_TX": "16", "EK_MU_TY": "16", "EK_MU_MINB_F32": "4"},
-                   {"EK_MU_TX": "32", "EK_MU_TY": "8", "EK_MU_MINB_F32": "4"}],
+                   {"EK_MU_TX": "32", "EK_MU_TY": "8", "EK_MU_MINB_F32": "4"},
+                   {"EK_MU_TX": "32", "EK_MU_TY": "8", "EK_MU_MINB_F32": "3"},
+                   {"EK_MU_TX": "32", "EK_MU_TY": "8", "EK_MU_MINB_F32": "2"}],
     "mhd2d": [{"EK_M2_TX": "16", "EK_M2_TY": "8"}, {"EK_M2_TX": "32", "EK_M2_TY": "8"}, {"EK_M2_TX": "16", "EK_M2_TY": "16"},
-              {"EK_M2_TX": "32", "EK_M2_TY": "4"}, {"EK_M2_TX": "8", "EK_M2_TY": "8"}],
+              {"EK_M2_TX": "32", "EK_M2_TY": "4"}, {"EK_M2_TX": "8", "EK_M2_TY": "8"},
+              {"EK_M2_TX": "16", "EK_M2_TY": "16", "EK_M2_MINB_F32": "3"},
+              {"EK_M2_TX": "16", "EK_M2_TY": "16", "EK_M2_MINB_F32": "4"}],
 }
 KCHUNKS = (16, 32, 64)
 
@@ -90,12 +100,12 @@ def measure(families):
         ini, U0 = P.blast_3d(n=256, nsteps=10 ** 6)
         res["hydro3d"] = {str(k): _kernel_ms(ek, ini, U0, [("step", 0)], 8, kchunk=k)["step"] for k in KCHUNKS}
     if "mhd_trace" in families or "mhd_update" in families:
-        ini, U0 = P.orszag_tang_3d(n=192, nsteps=10 ** 6)
+        ini, U0 = P.orszag_tang_3d(n=256, nsteps=10 ** 6)
         r = {str(k): _kernel_ms(ek, ini, U0, [("update", 0), ("trace", 1)], 4, kchunk=k) for k in KCHUNKS}
         res["mhd_trace"] = {k: v["trace"] for k, v in r.items()}
         res["mhd_update"] = {k: v["update"] for k, v in r.items()}
     if "mhd2d" in families:
-        ini, U0 = P.orszag_tang_2d(n=2048, nsteps=10 ** 6)
+        ini, U0 = P.orszag_tang_2d(n=4096, nsteps=10 ** 6)
         res["mhd2d"] = _kernel_ms(ek, ini, U0, [("step", 0)], 6)["step"]
     return res
 
