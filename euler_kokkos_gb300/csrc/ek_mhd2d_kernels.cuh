@@ -110,7 +110,7 @@ load_mhd2d_cell(const MhdState<S> & m, const KParams & P, const SrcCell & s, R (
 // 1. CFL reduction of the step
 // ---------------------------------------------------------------------------
 template <class S, class R>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, EK_MINB(R, 5, 2))
 mhd2d_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step,
                 unsigned long long * key)
 {

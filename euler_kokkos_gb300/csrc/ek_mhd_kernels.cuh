@@ -118,7 +118,7 @@ cell_prims_global(const MhdState<S> & m, const KParams & P, const MhdConst<R> & 
 // 1. CFL reduction of the step (on the primitive variables of the input)
 // ---------------------------------------------------------------------------
 template <class S, class R>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, EK_MINB(R, 5, 2))
 mhd_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step,
               unsigned long long * key)
 {
