@@ -7,6 +7,8 @@ Translation units (compiled in parallel, one -gencode):
   ek_config.cpp      -- .ini front end
   ek_noalloc.cu      -- the MHD 3D step on a static device scratch (no allocation)
   ek_io.cpp          -- VTK output in the reference's format
+and the driver executable _build/ek_main (ek_main.cpp: the reference's main
+loop over the C ABI).
 Usage: python -m euler_kokkos_gb300.build   (or build() from Python)
 """
 
@@ -22,6 +24,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libek_gb300.so")
 
+
+def main_path() -> str:
+    """The driver executable, beside the library."""
+    return os.path.join(os.path.dirname(LIB), "ek_main")
+
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "-I" + CSRC, "-I" + os.path.join(os.path.dirname(HERE), "include")]
@@ -36,7 +43,7 @@ def _nvcc() -> str:
 
 def _sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))
-            if f.endswith((".cu", ".cuh", ".h", ".cpp"))]
+            if f.endswith((".cu", ".cuh", ".h", ".cpp")) and f != "ek_main.cpp"]
 
 
 def _units():
@@ -59,7 +66,9 @@ def _tuned_flags():
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(main_path()):
+        return False
+    if os.path.getmtime(os.path.join(CSRC, "ek_main.cpp")) > os.path.getmtime(main_path()):
         return False
     t = os.path.getmtime(LIB)
     srcs = _sources() + [os.path.join(os.path.dirname(HERE), "include", "ek_gb300.h"), __file__]
@@ -99,6 +108,14 @@ def build(force: bool = False, verbose: bool = False, tuned: bool = True) -> str
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
     os.replace(tmp, LIB)
+    # the driver executable, linked against the library beside it
+    cxx = shutil.which("g++") or shutil.which("c++")
+    cmd = [cxx, "-O2", "-std=c++17", os.path.join(CSRC, "ek_main.cpp"),
+           "-I" + os.path.join(os.path.dirname(HERE), "include"), "-L" + os.path.dirname(LIB), "-lek_gb300",
+           "-Wl,-rpath,$ORIGIN", "-o", main_path()]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("ek_main link failed:\n" + r.stdout.decode(errors="replace"))
     return LIB
 
 
