@@ -135,7 +135,9 @@ cell_slopes(const R * q0, const R * qm, const R * qp, int hx, int hy, R st, R (&
 // 2D: one CTA = one TX x TY tile of interior cells.  hydro2d_tile is the tile
 // body shared by the single-solver kernel and the ensemble kernel.
 // ---------------------------------------------------------------------------
-template <class S, class R, int TX, int TY, int RS = 3, bool GRAV = false>
+// LOADED: the caller already stored the tile's primitive plane in sQ (the
+// ensemble's prefetch); otherwise it is loaded here.
+template <class S, class R, int TX, int TY, int RS = 3, bool GRAV = false, bool LOADED = false>
 __device__ __forceinline__ void
 hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & P, DevClock * clk,
              int step, int bx, int by, unsigned char * smem_raw)
@@ -166,8 +168,11 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
   };
 
   const int gi0 = P.gw + bx * TX, gj0 = P.gw + by * TY;
-  load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, 0, sQ);
-  __syncthreads();
+  if constexpr (!LOADED)
+  {
+    load_q_plane<S, R, NV, TX, TY>(Uin, P, C, gi0, gj0, 0, sQ);
+    __syncthreads();
+  }
 
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   // traces of the interior cell
@@ -353,23 +358,84 @@ hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
 // kernel walks the flat (instance, tile) work list; one launch = one step of
 // every instance.  No inter-block waits.
 // ---------------------------------------------------------------------------
+// raw conserved variables of a tile's (TX+4) x (TY+4) halo plane, gathered
+// from the boundary-mapped cells by per-thread asynchronous copies
+template <class S, int NV, int TX, int TY>
+__device__ __forceinline__ void
+issue_raw_plane(const S * __restrict__ U, const KParams & P, int gi0, int gj0, S * raw)
+{
+  constexpr int HX = TX + 4, HY = TY + 4, NT = TX * TY;
+  for (int c = threadIdx.x; c < HX * HY; c += NT)
+  {
+    const SrcCell s = src_cell(P, gi0 - 2 + c % HX, gj0 - 2 + c / HX, 0);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      cp_async<sizeof(S)>(raw + v * HY * HX + c, U + v * P.vstride + s.off);
+  }
+}
+// ... and, once this thread's copies landed, the primitives of the cells it
+// copied (reflecting walls flip the normal velocity, as load_q_plane does)
+template <class S, class R, int NV, int TX, int TY>
+__device__ __forceinline__ void
+convert_raw_plane(const S * raw, const KParams & P, const HydroConst<R> & C, int gi0, int gj0, R * sQ)
+{
+  constexpr int HX = TX + 4, HY = TY + 4, NT = TX * TY;
+  for (int c = threadIdx.x; c < HX * HY; c += NT)
+  {
+    const SrcCell s = src_cell(P, gi0 - 2 + c % HX, gj0 - 2 + c / HX, 0);
+    R             u[NV], q[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      u[v] = neg_if((R)raw[v * HY * HX + c], flips(s, v, 0));
+    hydro_prims<R, NV>(u, q, C);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      sQ[v * HY * HX + c] = q[v];
+  }
+}
+
+template <class S, class R, int TX, int TY>
+__host__ __device__ constexpr size_t
+ensemble_raw_bytes()
+{
+  return sizeof(S) * 4 * (TX + 4) * (TY + 4);
+}
+
 template <class S, class R, int TX, int TY>
 __global__ void __launch_bounds__(TX * TY)
 ensemble2d_step(const EnsInstance * __restrict__ insts, const EnsTile * __restrict__ tiles, int ntiles,
-                const int * __restrict__ stepc)
+                const int * __restrict__ stepc, size_t tile_smem)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // raw staging of the next work item's plane, after the tile's own buffers
+  S * raw = reinterpret_cast<S *>(smem_raw + tile_smem);
   // the step number lives in device memory (advanced by ensemble_advance after
   // every step), so a captured sequence of steps can be replayed as is
   const int step = *stepc;
+  // the plane of work item t is gathered while item t - gridDim.x computes
+  auto issue = [&](int t) {
+    const EnsTile       w = tiles[t];
+    const EnsInstance & in = insts[w.inst];
+    issue_raw_plane<S, 4, TX, TY>((const S *)in.U[step % 2], in.P, in.P.gw + w.bx * TX, in.P.gw + w.by * TY, raw);
+    cp_async_commit();
+  };
+  if (blockIdx.x < ntiles)
+    issue(blockIdx.x);
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x)
   {
-    const EnsTile      w = tiles[t];
+    const EnsTile       w = tiles[t];
     const EnsInstance & in = insts[w.inst];
-    hydro2d_tile<S, R, TX, TY>((const S *)in.U[step % 2], (S *)in.U[(step + 1) % 2], in.P, in.clk, step,
-                               w.bx, w.by, smem_raw);
+    const int           gi0 = in.P.gw + w.bx * TX, gj0 = in.P.gw + w.by * TY;
+    cp_async_wait_all();
+    convert_raw_plane<S, R, 4, TX, TY>(raw, in.P, hydro_const<R>(in.P), gi0, gj0, reinterpret_cast<R *>(smem_raw));
+    // every thread converted the cells it copied: the staging is free again
+    if (t + gridDim.x < ntiles)
+      issue(t + gridDim.x);
+    hydro2d_tile<S, R, TX, TY, 3, false, true>((const S *)in.U[step % 2], (S *)in.U[(step + 1) % 2], in.P,
+                                                in.clk, step, w.bx, w.by, smem_raw);
     __syncthreads(); // shared tiles are reused by the next work item
   }
+  cp_async_wait_all(); // no copy may land after the block has left
 }
 
 __global__ void

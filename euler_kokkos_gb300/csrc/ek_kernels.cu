@@ -154,11 +154,11 @@ ensemble2d_t(const EnsInstance * insts, const EnsTile * tiles, int ntiles, int *
              cudaStream_t st)
 {
   auto        k = ensemble2d_step<S, R, H2_TX, H2_TY>;
-  size_t      sm = hydro2d_smem<R>();
+  size_t      sm = hydro2d_smem<R>() + ensemble_raw_bytes<S, R, H2_TX, H2_TY>();
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess)
     return e;
-  k<<<grid, H2_TX * H2_TY, sm, st>>>(insts, tiles, ntiles, stepc);
+  k<<<grid, H2_TX * H2_TY, sm, st>>>(insts, tiles, ntiles, stepc, hydro2d_smem<R>());
   e = cudaGetLastError();
   if (e != cudaSuccess)
     return e;
@@ -170,7 +170,7 @@ int
 ensemble2d_grid_t()
 {
   auto   k = ensemble2d_step<S, R, H2_TX, H2_TY>;
-  size_t sm = hydro2d_smem<R>();
+  size_t sm = hydro2d_smem<R>() + ensemble_raw_bytes<S, R, H2_TX, H2_TY>();
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   int per_sm = 0, dev = 0, nsm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, H2_TX * H2_TY, sm);
