@@ -1017,6 +1017,7 @@ struct ek_ensemble
   ekc::EnsTile *           d_tiles = nullptr;
   int *                    d_step = nullptr;
   double *                 d_totals = nullptr;
+  void *                   d_scalars = nullptr; // per-instance step scalars (64 B each)
   int                      ntiles = 0;
   int                      grid = 0;
   int                      step = 0; // host copy of the device step counter
@@ -1049,6 +1050,7 @@ ek_ensemble_destroy(ek_ensemble * e)
   cudaFree(e->d_tiles);
   cudaFree(e->d_step);
   cudaFree(e->d_totals);
+  cudaFree(e->d_scalars);
   if (e->stream)
     cudaStreamDestroy(e->stream);
   delete e;
@@ -1151,6 +1153,8 @@ ek_ensemble_create(const ek_params * params, int n, ek_ensemble ** out)
     }
     e->ntiles = (int)tiles.size();
     err = cudaMalloc((void **)&e->d_tiles, sizeof(ekc::EnsTile) * tiles.size());
+    if (err == cudaSuccess)
+      err = cudaMalloc(&e->d_scalars, 64 * (size_t)n);
   }
   if (err == cudaSuccess)
     err = cudaMemcpyAsync(e->d_insts, h_insts.data(), sizeof(ekc::EnsInstance) * n, cudaMemcpyHostToDevice,
@@ -1199,10 +1203,10 @@ ensemble_launch_steps(ek_ensemble * e, int nsteps)
 {
   for (int k = 0; k < nsteps; ++k)
   {
-    cudaError_t err = e->exact ? ek_exact::ensemble2d_step(e->prec, e->d_insts, e->d_tiles, e->ntiles,
-                                                           e->d_step, e->grid, e->stream)
-                               : ek_fast::ensemble2d_step(e->prec, e->d_insts, e->d_tiles, e->ntiles,
-                                                          e->d_step, e->grid, e->stream);
+    cudaError_t err = e->exact ? ek_exact::ensemble2d_step(e->prec, e->d_insts, e->n, e->d_tiles, e->ntiles,
+                                                           e->d_step, e->d_scalars, e->grid, e->stream)
+                               : ek_fast::ensemble2d_step(e->prec, e->d_insts, e->n, e->d_tiles, e->ntiles,
+                                                          e->d_step, e->d_scalars, e->grid, e->stream);
     if (err != cudaSuccess)
       return cuda_fail(err, "ensemble step");
   }
@@ -1248,7 +1252,7 @@ ek_ensemble_run(ek_ensemble * e, int nsteps, int use_graph)
     }
     EK_CUDA(cudaGraphLaunch(e->graph_exec, e->stream), "graph launch");
   }
-  e->launches += 2LL * nsteps;
+  e->launches += 3LL * nsteps;
   e->step += nsteps;
   return EK_OK;
 }

@@ -137,10 +137,12 @@ cell_slopes(const R * q0, const R * qm, const R * qp, int hx, int hy, R st, R (&
 // ---------------------------------------------------------------------------
 // LOADED: the caller already stored the tile's primitive plane in sQ (the
 // ensemble's prefetch); otherwise it is loaded here.
+// pre: the step scalars computed for the whole instance (the ensemble), else
+// thread 0 computes them for this CTA.
 template <class S, class R, int TX, int TY, int RS = 3, bool GRAV = false, bool LOADED = false>
 __device__ __forceinline__ void
 hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & P, DevClock * clk,
-             int step, int bx, int by, unsigned char * smem_raw)
+             int step, int bx, int by, unsigned char * smem_raw, const StepScalars<R> * pre = nullptr)
 {
   constexpr int NV = 4, HX = TX + 4, HY = TY + 4, NT = TX * TY;
   constexpr int FX = TX + 2; // face-state rows in x: cells -1..TX
@@ -151,10 +153,21 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
   R * sYp = sYm + NV * (TY + 2) * TX;        // YMAX state
 
   __shared__ StepScalars<R> sc;
-  if (!step_scalars<R>(P, clk, step, &sc))
-    return;
-  const double        t = sc.t, dt = sc.dt;
-  const R             dtdx = sc.dtdx, dtdy = sc.dtdy;
+  StepScalars<R>            ss;
+  if (pre)
+  {
+    ss = *pre;
+    if (!ss.active)
+      return;
+  }
+  else
+  {
+    if (!step_scalars<R>(P, clk, step, &sc))
+      return;
+    ss = sc;
+  }
+  const double        t = ss.t, dt = ss.dt;
+  const R             dtdx = ss.dtdx, dtdy = ss.dtdy;
   const HydroConst<R> C = hydro_const<R>(P);
   const R             hdt = (R)(0.5 * dt);
   const bool          kick = GRAV && P.grav_hancock; // gravity predictor of the face states
@@ -401,10 +414,32 @@ ensemble_raw_bytes()
   return sizeof(S) * 4 * (TX + 4) * (TY + 4);
 }
 
+// The step scalars (active, t, dt, dt/dx, dt/dy) of every instance, once per
+// step: the FP64 divisions run in one thread per instance, not per tile.
+template <class R>
+__global__ void
+ensemble_scalars_kernel(const EnsInstance * __restrict__ insts, int n, const int * __restrict__ stepc,
+                        StepScalars<R> * __restrict__ out)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const KParams & P = insts[i].P;
+  double          t = 0.0, dt = 0.0;
+  StepScalars<R>  s;
+  s.active = step_dt(P, insts[i].clk, *stepc, &t, &dt) ? 1 : 0;
+  s.t = t;
+  s.dt = dt;
+  s.dtdx = (R)(dt / P.dx);
+  s.dtdy = (R)(dt / P.dy);
+  s.dtdz = (R)(dt / P.dz);
+  out[i] = s;
+}
+
 template <class S, class R, int TX, int TY>
 __global__ void __launch_bounds__(TX * TY)
 ensemble2d_step(const EnsInstance * __restrict__ insts, const EnsTile * __restrict__ tiles, int ntiles,
-                const int * __restrict__ stepc, size_t tile_smem)
+                const int * __restrict__ stepc, size_t tile_smem, const StepScalars<R> * __restrict__ scal)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // raw staging of the next work item's plane, after the tile's own buffers
@@ -431,8 +466,9 @@ ensemble2d_step(const EnsInstance * __restrict__ insts, const EnsTile * __restri
     // every thread converted the cells it copied: the staging is free again
     if (t + gridDim.x < ntiles)
       issue(t + gridDim.x);
+    __syncthreads(); // the primitive plane is complete
     hydro2d_tile<S, R, TX, TY, 3, false, true>((const S *)in.U[step % 2], (S *)in.U[(step + 1) % 2], in.P,
-                                                in.clk, step, w.bx, w.by, smem_raw);
+                                                in.clk, step, w.bx, w.by, smem_raw, scal + w.inst);
     __syncthreads(); // shared tiles are reused by the next work item
   }
   cp_async_wait_all(); // no copy may land after the block has left

@@ -150,15 +150,21 @@ namespace
 {
 template <class S, class R>
 cudaError_t
-ensemble2d_t(const EnsInstance * insts, const EnsTile * tiles, int ntiles, int * stepc, int grid,
-             cudaStream_t st)
+ensemble2d_t(const EnsInstance * insts, int n, const EnsTile * tiles, int ntiles, int * stepc, void * scal,
+             int grid, cudaStream_t st)
 {
-  auto        k = ensemble2d_step<S, R, H2_TX, H2_TY>;
-  size_t      sm = hydro2d_smem<R>() + ensemble_raw_bytes<S, R, H2_TX, H2_TY>();
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  static_assert(sizeof(StepScalars<R>) <= 64, "per-instance step scalars are allocated 64 bytes each");
+  StepScalars<R> * sc = static_cast<StepScalars<R> *>(scal);
+  ensemble_scalars_kernel<R><<<(n + 127) / 128, 128, 0, st>>>(insts, n, stepc, sc);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess)
     return e;
-  k<<<grid, H2_TX * H2_TY, sm, st>>>(insts, tiles, ntiles, stepc, hydro2d_smem<R>());
+  auto   k = ensemble2d_step<S, R, H2_TX, H2_TY>;
+  size_t sm = hydro2d_smem<R>() + ensemble_raw_bytes<S, R, H2_TX, H2_TY>();
+  e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess)
+    return e;
+  k<<<grid, H2_TX * H2_TY, sm, st>>>(insts, tiles, ntiles, stepc, hydro2d_smem<R>(), sc);
   e = cudaGetLastError();
   if (e != cudaSuccess)
     return e;
@@ -181,17 +187,17 @@ ensemble2d_grid_t()
 } // namespace
 
 cudaError_t
-ensemble2d_step(int prec, const EnsInstance * insts, const EnsTile * tiles, int ntiles, int * stepc,
-                int grid, cudaStream_t st)
+ensemble2d_step(int prec, const EnsInstance * insts, int n, const EnsTile * tiles, int ntiles, int * stepc,
+                void * scal, int grid, cudaStream_t st)
 {
 #ifdef EK_EXACT_ONLY
   if (prec != 0)
     return cudaErrorNotSupported;
-  return ensemble2d_t<double, double>(insts, tiles, ntiles, stepc, grid, st);
+  return ensemble2d_t<double, double>(insts, n, tiles, ntiles, stepc, scal, grid, st);
 #else
   if (prec == 0)
-    return ensemble2d_t<double, double>(insts, tiles, ntiles, stepc, grid, st);
-  return ensemble2d_t<float, float>(insts, tiles, ntiles, stepc, grid, st);
+    return ensemble2d_t<double, double>(insts, n, tiles, ntiles, stepc, scal, grid, st);
+  return ensemble2d_t<float, float>(insts, n, tiles, ntiles, stepc, scal, grid, st);
 #endif
 }
 

@@ -31,8 +31,9 @@
   cudaError_t mhd2d_dt(int prec, const void * U, const KParams & P, unsigned long long * key,       \
                        cudaStream_t st);                                                            \
   /* one step of every instance of a 2D hydro ensemble (persistent kernel) */                       \
-  cudaError_t ensemble2d_step(int prec, const ekc::EnsInstance * insts, const ekc::EnsTile * tiles,  \
-                              int ntiles, int * stepc, int grid, cudaStream_t st);                  \
+  /* scal: per-instance step scalars (n entries of 64 bytes), written by the step */                \
+  cudaError_t ensemble2d_step(int prec, const ekc::EnsInstance * insts, int n, const ekc::EnsTile * tiles, \
+                              int ntiles, int * stepc, void * scal, int grid, cudaStream_t st);     \
   int         ensemble2d_grid(int prec);                                                            \
   }
 
