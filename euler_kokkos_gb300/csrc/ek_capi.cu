@@ -481,6 +481,8 @@ reset_clock(ek_solver * s, double t0)
     h.key[i] = EK_KEY_LOWEST;
     h.t[i] = 0.0;
     h.sid[i] = -1;
+    h.sc[i].step = -1;
+    h.fin[i] = 0;
   }
   h.sid[0] = 0;
   h.t[0] = t0;

@@ -76,6 +76,12 @@ struct KParams
 // Per-step scalars kept on the device so that consecutive steps need no host
 // round trip.  Slot s = step % 3 holds the max-reduced inverse time step
 // (as an order-preserving integer key) and the time at the start of step.
+// dt of a step and its FP64 ratios, computed once per step (step = -1: none)
+struct StepConsts
+{
+  double t, dt, dtdx, dtdy, dtdz;
+  int    step, active;
+};
 struct DevClock
 {
   unsigned long long key[3];
@@ -85,6 +91,8 @@ struct DevClock
   int                error;     // sticky device error flags
   double *           dtlog;     // dt of each step (capacity dtcap)
   int                dtcap;
+  StepConsts         sc[3];     // per slot, by the last block of the CFL kernel
+  unsigned int       fin[3];    // blocks of that kernel done (reset by the last)
 };
 
 enum : int
@@ -424,6 +432,59 @@ step_scalars(const KParams & P, const DevClock * clk, int step, StepScalars<R> *
   }
   __syncthreads();
   return sh->active != 0;
+}
+
+// Called by every block of the kernel that completes the CFL key of `step`
+// (after its atomicMax): the last block to finish computes the step's dt and
+// dt/dx ratios in FP64 once, for the step's kernels to read (step_consts), so
+// that no block of those kernels runs the divisions behind a barrier.  The
+// clock fields written by other blocks are read through volatile loads.
+__device__ __forceinline__ void
+finalize_step(DevClock * clk, const KParams & P, int step)
+{
+  __shared__ int last;
+  __syncthreads();
+  const int s = step % 3;
+  if (threadIdx.x == 0)
+  {
+    __threadfence();
+    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+    last = atomicAdd(&clk->fin[s], 1u) == nb - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0)
+  {
+    __threadfence();
+    volatile DevClock * v = clk;
+    StepConsts          c;
+    c.step = step;
+    c.active = 0;
+    c.t = c.dt = c.dtdx = c.dtdy = c.dtdz = 0.0;
+    if (v->sid[s] == step) // step_dt's arithmetic
+    {
+      const double invDt = dkey_inv(v->key[s]);
+      double       d = P.cfl / invDt;
+      const double tt = v->t[s];
+      if (tt + d > P.tEnd)
+        d = P.tEnd - tt;
+      c.t = tt;
+      c.dt = d;
+      c.active = !(tt >= P.tEnd - 1e-14);
+      c.dtdx = d / P.dx;
+      c.dtdy = d / P.dy;
+      c.dtdz = d / P.dz;
+    }
+    clk->sc[s] = c;
+    clk->fin[s] = 0;
+  }
+}
+// the constants of `step`; false when the step must not run (or they were
+// not computed for it)
+__device__ __forceinline__ bool
+step_consts(const DevClock * clk, int step, StepConsts & c)
+{
+  c = clk->sc[step % 3];
+  return c.step == step && c.active;
 }
 
 // Visit the interior cells of a state row by row: a block takes whole rows

@@ -160,6 +160,8 @@ mhd2d_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step
     }
   });
   block_max_commit<256>(cand_key((double)tmax), key ? key : &clk->key[step % 3]);
+  if (!key)
+    finalize_step(clk, P, step); // dt and its ratios for the step kernel
 }
 
 // ---------------------------------------------------------------------------
@@ -309,22 +311,12 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
   R * sFy = sFx + 6 * T::FXS;               // [6][TY+1][TX]  y fluxes
   R * sE = sFy + 6 * T::FYS;                // [TY+1][TX+1]   z-edge emf
 
-  __shared__ StepScalars<R> sc;
-  __shared__ double         sdd[2]; // FP64 dt/dx, dt/dy of the face-field update
-  if (threadIdx.x == 0)
-  {
-    double t0, dt0;
-    if (step_dt(P, clk, step, &t0, &dt0))
-    {
-      sdd[0] = dt0 / P.dx;
-      sdd[1] = dt0 / P.dy;
-    }
-  }
-  if (!step_scalars<R>(P, clk, step, &sc))
+  StepConsts sc;
+  if (!step_consts(clk, step, sc))
     return;
   const double      t = sc.t, dt = sc.dt;
-  const R           dtdx = sc.dtdx, dtdy = sc.dtdy;
-  const double      ddtdx = sdd[0], ddtdy = sdd[1];
+  const R           dtdx = to_r<R>(sc.dtdx), dtdy = to_r<R>(sc.dtdy);
+  const double      ddtdx = sc.dtdx, ddtdy = sc.dtdy; // FP64 ratios of the face-field update
   const MhdConst<R> C = mhd_const<R>(P);
   const MhdState<S> m = mhd_state<S>(Uin, P);
   const int         gw = P.gw;

@@ -138,6 +138,8 @@ mhd_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step,
     tmax = fmax(tmax, mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz, P.idx, P.idy, P.idz));
   });
   block_max_commit<256>(cand_key((double)tmax), key ? key : &clk->key[step % 3]);
+  if (!key)
+    finalize_step(clk, P, step); // dt and its ratios for the trace and update kernels
 }
 
 // ---------------------------------------------------------------------------
@@ -342,10 +344,10 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
   R * sQ = sB + 4 * T::BP;                  // [3][8][QY][QX]
   R *      sE = sQ + 3 * T::QP;                                // [2][3][EY][EX]
 
-  __shared__ StepScalars<R> sc;
-  if (!step_scalars<R>(P, clk, step, &sc))
+  StepConsts sc;
+  if (!step_consts(clk, step, sc))
     return;
-  const R           dtdx = sc.dtdx, dtdy = sc.dtdy, dtdz = sc.dtdz;
+  const R           dtdx = to_r<R>(sc.dtdx), dtdy = to_r<R>(sc.dtdy), dtdz = to_r<R>(sc.dtdz);
   const MhdConst<R> C = mhd_const<R>(P);
   const MhdState<S> m = mhd_state<S>(U, P);
   const int gw = P.gw;
@@ -569,23 +571,12 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
   R * sEy = sEz + 2 * T::EZS;               // [2][TY][TX+1]
   R * sEx = sEy + 2 * T::EYS;               // [2][TY+1][TX]
 
-  __shared__ StepScalars<R> sc;
-  __shared__ double         sdd[3]; // FP64 dt/dx, dt/dy, dt/dz of the CT update
-  if (threadIdx.x == 0)
-  {
-    double t0, dt0;
-    if (step_dt(P, clk, step, &t0, &dt0))
-    {
-      sdd[0] = dt0 / P.dx;
-      sdd[1] = dt0 / P.dy;
-      sdd[2] = dt0 / P.dz;
-    }
-  }
-  if (!step_scalars<R>(P, clk, step, &sc))
+  StepConsts sc;
+  if (!step_consts(clk, step, sc))
     return;
   const double      t = sc.t, dt = sc.dt;
-  const R           dtdx = sc.dtdx, dtdy = sc.dtdy, dtdz = sc.dtdz;
-  const double      ddtdx = sdd[0], ddtdy = sdd[1], ddtdz = sdd[2];
+  const R           dtdx = to_r<R>(sc.dtdx), dtdy = to_r<R>(sc.dtdy), dtdz = to_r<R>(sc.dtdz);
+  const double      ddtdx = sc.dtdx, ddtdy = sc.dtdy, ddtdz = sc.dtdz; // FP64 ratios of the CT update
   const MhdConst<R> C = mhd_const<R>(P);
   const int         gw = P.gw;
   const int         i0 = gw + blockIdx.x * TX, j0 = gw + blockIdx.y * TY;

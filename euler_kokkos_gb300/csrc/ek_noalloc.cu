@@ -87,6 +87,9 @@ noalloc_clock_init(ekc::DevClock * clk, double t0, double * dt_slot)
     clk->key[s] = EK_KEY_LOWEST;
     clk->t[s] = 0.0;
     clk->sid[s] = -1;
+    clk->sc[s].step = -1;
+    clk->sc[s].active = 0;
+    clk->fin[s] = 0;
   }
   clk->sid[0] = 0;
   clk->t[0] = t0;
