@@ -315,10 +315,12 @@ ek_solver_create(const ek_params * params, ek_solver ** out)
     if (s->work_bytes)
       e = cudaMalloc(&s->work, s->work_bytes);
   }
+  // on the solver's stream: a legacy-stream memset is not ordered before the
+  // uploads of the (non-blocking) solver stream
   if (e == cudaSuccess)
-    e = cudaMemset(s->U[0], 0, s->state_bytes);
+    e = cudaMemsetAsync(s->U[0], 0, s->state_bytes, s->stream);
   if (e == cudaSuccess)
-    e = cudaMemset(s->U[1], 0, s->state_bytes);
+    e = cudaMemsetAsync(s->U[1], 0, s->state_bytes, s->stream);
   if (e == cudaSuccess && !p.mhd && p.dim == 3 && !p.no_tma)
     s->has_tmap = ek_fast::hydro3d_tensor_map(s->prec, s->U[0], k, &s->tmap[0]) &&
                   ek_fast::hydro3d_tensor_map(s->prec, s->U[1], k, &s->tmap[1]);
@@ -450,8 +452,10 @@ state_to_host(ek_solver * s, const void * dev, double * U, int layout)
   return EK_OK;
 }
 
+// fin_step >= 0 (hydro): key is the clock's slot of that step; its step
+// constants are computed too
 static ek_status
-launch_dt(ek_solver * s, const void * U, unsigned long long * key)
+launch_dt(ek_solver * s, const void * U, unsigned long long * key, int fin_step = -1)
 {
   cudaError_t e;
   if (s->p.mhd && s->p.dim == 2)
@@ -461,8 +465,11 @@ launch_dt(ek_solver * s, const void * U, unsigned long long * key)
     e = s->exact ? ek_exact::mhd_dt(s->prec, U, s->kp, key, s->stream)
                  : ek_fast::mhd_dt(s->prec, U, s->kp, key, s->stream);
   else
-    e = s->exact ? ek_exact::hydro_dt(s->p.dim, s->prec, U, s->kp, key, s->stream)
-                 : ek_fast::hydro_dt(s->p.dim, s->prec, U, s->kp, key, s->stream);
+  {
+    DevClock * fin = fin_step >= 0 ? s->clk : nullptr;
+    e = s->exact ? ek_exact::hydro_dt(s->p.dim, s->prec, U, s->kp, key, fin, fin_step, s->stream)
+                 : ek_fast::hydro_dt(s->p.dim, s->prec, U, s->kp, key, fin, fin_step, s->stream);
+  }
   if (e == cudaErrorNotSupported)
     return fail(EK_ERR_UNSUPPORTED, "kernel not available for this configuration");
   EK_CUDA(e, "dt kernel");
@@ -494,7 +501,7 @@ reset_clock(ek_solver * s, double t0)
   // hydro: slot 0 holds the CFL of the initial state (the constructor's
   // compute_dt()); MHD recomputes dt inside every step
   if (!s->p.mhd)
-    return launch_dt(s, s->U[0], &s->clk->key[0]);
+    return launch_dt(s, s->U[0], &s->clk->key[0], 0);
   return EK_OK;
 }
 
@@ -627,7 +634,7 @@ ek_solver_set_gravity_field(ek_solver * s, const double * G, int layout)
   const int          slot = s->iteration % 3;
   unsigned long long low = EK_KEY_LOWEST;
   EK_CUDA(cudaMemcpyAsync(&s->clk->key[slot], &low, sizeof low, cudaMemcpyHostToDevice, s->stream), "gravity dt");
-  ek_status st = launch_dt(s, s->U[s->iteration % 2], &s->clk->key[slot]);
+  ek_status st = launch_dt(s, s->U[s->iteration % 2], &s->clk->key[slot], s->iteration);
   if (st != EK_OK)
     return st;
   EK_CUDA(cudaStreamSynchronize(s->stream), "gravity dt");
@@ -745,8 +752,10 @@ sync_from_clock(ek_solver * s)
   s->t = h.t[h.iteration % 3];
   if (h.iteration > 0 && h.iteration - 1 < s->dtcap)
   {
-    EK_CUDA(cudaMemcpy(&s->dt, s->dtlog + (h.iteration - 1), sizeof(double), cudaMemcpyDeviceToHost),
+    EK_CUDA(cudaMemcpyAsync(&s->dt, s->dtlog + (h.iteration - 1), sizeof(double), cudaMemcpyDeviceToHost,
+                            s->stream),
             "dt read");
+    EK_CUDA(cudaStreamSynchronize(s->stream), "dt read");
   }
   if (!(s->dt > 0.0) || !std::isfinite(s->dt))
     return fail(EK_ERR_NONFINITE, "time step is not finite and positive (dt = " + std::to_string(s->dt) + ")");
@@ -826,7 +835,8 @@ ek_solver_dt_history(ek_solver * s, double * dts, int n)
   if (!s || (!dts && n > 0) || n < 0 || n > s->iteration || n > s->dtcap)
     return fail(EK_ERR_INVALID, "ek_solver_dt_history: bad argument");
   if (n)
-    EK_CUDA(cudaMemcpy(dts, s->dtlog, sizeof(double) * n, cudaMemcpyDeviceToHost), "dt history");
+    EK_CUDA(cudaMemcpyAsync(dts, s->dtlog, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream), "dt history");
+    EK_CUDA(cudaStreamSynchronize(s->stream), "dt history");
   return EK_OK;
 }
 
@@ -1281,7 +1291,11 @@ ek_ensemble_time(ek_ensemble * e, int i, double * t, double * dt, int * iteratio
   v->iteration = h.iteration;
   v->t = h.t[h.iteration % 3];
   if (h.iteration > 0 && h.iteration - 1 < v->dtcap)
-    EK_CUDA(cudaMemcpy(&v->dt, v->dtlog + (h.iteration - 1), sizeof(double), cudaMemcpyDeviceToHost), "dt");
+  {
+    EK_CUDA(cudaMemcpyAsync(&v->dt, v->dtlog + (h.iteration - 1), sizeof(double), cudaMemcpyDeviceToHost, v->stream),
+            "dt");
+    EK_CUDA(cudaStreamSynchronize(v->stream), "dt");
+  }
   return ek_solver_time(v, t, dt, iteration);
 }
 

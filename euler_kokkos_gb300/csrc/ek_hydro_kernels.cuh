@@ -152,8 +152,7 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
   R * sYm = sXp + NV * TY * FX;              // YMIN state of cells -1..TY, then y-flux
   R * sYp = sYm + NV * (TY + 2) * TX;        // YMAX state
 
-  __shared__ StepScalars<R> sc;
-  StepScalars<R>            ss;
+  StepScalars<R> ss;
   if (pre)
   {
     ss = *pre;
@@ -162,9 +161,15 @@ hydro2d_tile(const S * __restrict__ Uin, S * __restrict__ Uout, const KParams & 
   }
   else
   {
-    if (!step_scalars<R>(P, clk, step, &sc))
+    StepConsts c; // computed once for the step by the last block of the kernel before
+    if (!step_consts(clk, step, c))
       return;
-    ss = sc;
+    ss.t = c.t;
+    ss.dt = c.dt;
+    ss.dtdx = to_r<R>(c.dtdx);
+    ss.dtdy = to_r<R>(c.dtdy);
+    ss.dtdz = to_r<R>(c.dtdz);
+    ss.active = 1;
   }
   const double        t = ss.t, dt = ss.dt;
   const R             dtdx = ss.dtdx, dtdy = ss.dtdy;
@@ -364,6 +369,7 @@ hydro2d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   hydro2d_tile<S, R, TX, TY, RS, GRAV>(Uin, Uout, P, clk, step, blockIdx.x, blockIdx.y, smem_raw);
+  finalize_step(clk, P, step + 1); // the next step's dt, once its CFL key is complete
 }
 
 // ---------------------------------------------------------------------------
@@ -527,11 +533,11 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   R * sYm = sXp + NV * TY * FX;
   R * sYp = sYm + NV * (TY + 2) * TX;
 
-  __shared__ StepScalars<R> sc;
-  if (!step_scalars<R>(P, clk, step, &sc))
+  StepConsts sc; // computed once for the step by the last block of the kernel before
+  if (!step_consts(clk, step, sc))
     return;
   const double        t = sc.t, dt = sc.dt;
-  const R             dtdx = sc.dtdx, dtdy = sc.dtdy, dtdz = sc.dtdz;
+  const R             dtdx = to_r<R>(sc.dtdx), dtdy = to_r<R>(sc.dtdy), dtdz = to_r<R>(sc.dtdz);
   const HydroConst<R> C = hydro_const<R>(P);
   const R             hdt = (R)(0.5 * dt);
   const bool          kick = GRAV && P.grav_hancock; // gravity predictor of the face states
@@ -846,6 +852,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
   block_max_commit<NT>(cand_key((double)tmax), &clk->key[(step + 1) % 3]);
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
     step_commit(clk, step, t, dt);
+  finalize_step(clk, P, step + 1); // the next step's dt, once its CFL key is complete
 }
 
 // ---------------------------------------------------------------------------
@@ -854,7 +861,7 @@ hydro3d_step(const S * __restrict__ Uin, S * __restrict__ Uout, KParams P, DevCl
 // ---------------------------------------------------------------------------
 template <class S, class R, int NV, bool GRAV>
 __global__ void
-hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
+hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key, DevClock * fin, int fin_step)
 {
   const HydroConst<R> C = hydro_const<R>(P);
   R                   tmax = R(-INFINITY);
@@ -874,6 +881,8 @@ hydro_dt_kernel(const S * __restrict__ U, KParams P, unsigned long long * key)
       tmax = fmax(tmax, hydro_invdt<R, NV>(u, C, P));
   });
   block_max_commit<256>(cand_key((double)tmax), key);
+  if (fin)
+    finalize_step(fin, P, fin_step); // the constants of the step this key is for
 }
 
 // Fill the ghost cells of a state in memory (make_boundaries_serial result,

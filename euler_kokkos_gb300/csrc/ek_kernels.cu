@@ -101,17 +101,18 @@ hydro_step_t(int dim, const void * Uin, void * Uout, const KParams & P, DevClock
 
 template <class S, class R>
 cudaError_t
-hydro_dt_t(int dim, const void * U, const KParams & P, unsigned long long * key, cudaStream_t st)
+hydro_dt_t(int dim, const void * U, const KParams & P, unsigned long long * key, DevClock * fin, int fin_step,
+           cudaStream_t st)
 {
   const int blocks = row_blocks(P);
   if (dim == 2 && P.grav)
-    hydro_dt_kernel<S, R, 4, true><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+    hydro_dt_kernel<S, R, 4, true><<<blocks, 256, 0, st>>>((const S *)U, P, key, fin, fin_step);
   else if (dim == 2)
-    hydro_dt_kernel<S, R, 4, false><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+    hydro_dt_kernel<S, R, 4, false><<<blocks, 256, 0, st>>>((const S *)U, P, key, fin, fin_step);
   else if (P.grav)
-    hydro_dt_kernel<S, R, 5, true><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+    hydro_dt_kernel<S, R, 5, true><<<blocks, 256, 0, st>>>((const S *)U, P, key, fin, fin_step);
   else
-    hydro_dt_kernel<S, R, 5, false><<<blocks, 256, 0, st>>>((const S *)U, P, key);
+    hydro_dt_kernel<S, R, 5, false><<<blocks, 256, 0, st>>>((const S *)U, P, key, fin, fin_step);
   return cudaGetLastError();
 }
 } // namespace
@@ -132,17 +133,17 @@ hydro_step(int dim, int prec, const void * Uin, void * Uout, const KParams & P, 
 }
 
 cudaError_t
-hydro_dt(int dim, int prec, const void * U, const KParams & P, unsigned long long * key,
-         cudaStream_t st)
+hydro_dt(int dim, int prec, const void * U, const KParams & P, unsigned long long * key, DevClock * fin,
+         int fin_step, cudaStream_t st)
 {
 #ifdef EK_EXACT_ONLY
   if (prec != 0)
     return cudaErrorNotSupported;
-  return hydro_dt_t<double, double>(dim, U, P, key, st);
+  return hydro_dt_t<double, double>(dim, U, P, key, fin, fin_step, st);
 #else
   if (prec == 0)
-    return hydro_dt_t<double, double>(dim, U, P, key, st);
-  return hydro_dt_t<float, float>(dim, U, P, key, st);
+    return hydro_dt_t<double, double>(dim, U, P, key, fin, fin_step, st);
+  return hydro_dt_t<float, float>(dim, U, P, key, fin, fin_step, st);
 #endif
 }
 

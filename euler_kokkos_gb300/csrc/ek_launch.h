@@ -17,8 +17,9 @@
   /* tmap: tensor map of Uin for the 3D kernel's staged planes, or null */                        \
   cudaError_t hydro_step(int dim, int prec, const void * Uin, void * Uout, const KParams & P,        \
                          DevClock * clk, int step, const CUtensorMap * tmap, cudaStream_t st);      \
+  /* fin: also compute the step constants of step fin_step from key (the last block) */           \
   cudaError_t hydro_dt(int dim, int prec, const void * U, const KParams & P,                       \
-                       unsigned long long * key, cudaStream_t st);                                  \
+                       unsigned long long * key, DevClock * fin, int fin_step, cudaStream_t st);    \
   cudaError_t mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key,         \
                      cudaStream_t st);                                                              \
   /* one MHD step = phase 0 (CFL), 1 (trace), 2 (fluxes, emfs, update) */                         \
