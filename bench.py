@@ -59,6 +59,19 @@ TRAFFIC_PER_CELL = {
     ("mhd2d", "mixed"): 78.7,     # mhd2d_step_kernel<float>: 186.3 + 143.7 MB / 4.19 M cells
 }
 
+# Floating-point operations per cell-update of the reference algorithm
+# (implementationVersion 0, in its own expression order), counted by kind by
+# the op-counting build of the oracle (oracle/ek_opcount.cpp through
+# eko.count_ops) over the first two steps of the named case, the CFL
+# reduction included.  "flops" = add/sub + mul + div + sqrt, one each;
+# "other" = min/max + fabs/copysign + negation + comparison.
+FLOPS_PER_CELL = {
+    "hydro3d": {"flops": 886.945, "other": 196.479, "counted_on": "3D blast 256^3, HLLC, minmod"},
+    "mhd3d": {"flops": 3415.651, "other": 591.732, "counted_on": "3D Orszag-Tang 128^3, HLLD, MC"},
+    "mhd2d": {"flops": 1692.266, "other": 308.399, "counted_on": "2D Orszag-Tang 1024^2, HLLD, MC"},
+    "hydro2d": {"flops": 469.653, "other": 116.702, "counted_on": "2D Kelvin-Helmholtz 128^2, HLLC, MC"},
+}
+
 
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -254,7 +267,7 @@ def cpu_sample(args, seconds=12.0):
                       (n, steps, cores, dt)}
 
 
-def ensemble_workload(ek, P, args, sync, maxt, world):
+def ensemble_workload(ek, P, args, sync, maxt, world, fp32_tflops=None):
     """The batched Kelvin-Helmholtz ensemble: args.ens_n instances with grids
     from {64,96,128,192,256}^2, own shear / density ratio / dt each, FP32 with
     FP64 totals, one persistent kernel per step replayed from a CUDA graph."""
@@ -317,6 +330,11 @@ def ensemble_workload(ek, P, args, sync, maxt, world):
         "persistent_grid": info["grid"], "gpu_launches": launches, "cuda_graph": True,
         "fp64_total_mass_first": float(tot[0, 0]), "t_end_samples": t_last,
         "cpu_baseline": cpu,
+        "flop": None if not fp32_tflops else {
+            "per_cell": FLOPS_PER_CELL["hydro2d"]["flops"], "counted_on": FLOPS_PER_CELL["hydro2d"]["counted_on"],
+            "achieved_tflops": FLOPS_PER_CELL["hydro2d"]["flops"] * value * 1e6 / 1e12,
+            "peak_tflops": fp32_tflops,
+            "frac": FLOPS_PER_CELL["hydro2d"]["flops"] * value * 1e6 / 1e12 / fp32_tflops / world},
         "config": "%d x Hydro_Muscl_2D Kelvin-Helmholtz, N in {64,96,128,192,256}^2, shear U[0.2,1], "
                   "density ratio U[1.5,3], periodic x / reflecting y, HLLC, MC, CFL 0.8, own dt" % len(cases),
     }
@@ -407,6 +425,10 @@ def main():
     peaks, peak_kind = load_peaks()
     hbm = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
 
+    # CUDA-core FMA rates of this GPU (TFLOP/s, 2 FLOPs per FMA), the
+    # denominators of the FLOP roofline
+    fma_peak = {"mixed": ek.measure_fma_rate(ek.EK_PREC_MIXED), "fp64": ek.measure_fma_rate(ek.EK_PREC_FP64)}
+
     ini, U0 = P.blast_3d(n=args.n, nsteps=10 ** 6)
     with ClockSampler(local) as clk:
         mixed = measure_workload(ek, "hydro3d", ek.EK_PREC_MIXED, ini, U0, args.steps, args.warmup, sync)
@@ -434,7 +456,27 @@ def main():
                 "frac": achieved / hbm if achieved else None,
                 "traffic": TRAFFIC_PER_CELL[key] * meas["cells"] if key in TRAFFIC_PER_CELL else None,
                 "kernel_ms": kms, "peak_source": peak_kind,
-                "algorithmic_bytes_per_cell": BYTES_PER_CELL[key]}
+                "algorithmic_bytes_per_cell": BYTES_PER_CELL[key],
+                **flop_roofline(meas, key)}
+
+    def flop_roofline(meas, key):
+        """The step against both ceilings: HBM (algorithmic bytes at the measured
+        copy rate) and CUDA-core FLOPs (the reference's op count at the FMA rate
+        measured above), whole-step time."""
+        fl = FLOPS_PER_CELL.get(key[0])
+        if not fl or not meas["ms"]:
+            return {}
+        rate = meas["cells"] * meas["steps"] / (meas["ms"] / 1e3)  # cell-updates/s
+        peak = fma_peak[key[1]]
+        bound_hbm = hbm * 1e9 / BYTES_PER_CELL[key]
+        bound_flop = peak * 1e12 / fl["flops"]
+        return {"flop": {"per_cell": fl["flops"], "other_fp_ops_per_cell": fl["other"],
+                         "counted_on": fl["counted_on"], "achieved_tflops": fl["flops"] * rate / 1e12,
+                         "peak_tflops": peak, "frac": fl["flops"] * rate / 1e12 / peak,
+                         "peak_source": "CUDA-core FMA rate measured in this run (%s)" %
+                                        ("FP64" if key[1] == "fp64" else "FP32")},
+                "bound_gcell_s": {"hbm": bound_hbm / 1e9, "flop": bound_flop / 1e9},
+                "frac_of_min_bound": rate / min(bound_hbm, bound_flop)}
 
     workloads = {}
     if not args.no_mhd:
@@ -486,7 +528,7 @@ def main():
         }
 
     if not args.no_ensemble:
-        workloads["kh_ensemble_%d" % args.ens_n] = ensemble_workload(ek, P, args, sync, maxt, world)
+        workloads["kh_ensemble_%d" % args.ens_n] = ensemble_workload(ek, P, args, sync, maxt, world, fma_peak["mixed"])
 
     line = None
     if rank == 0:
@@ -518,7 +560,7 @@ def main():
             "fp64": {
                 "value": v64, "unit": UNIT, "ms_per_step": ms_fp64 / fp64["steps"],
                 "roofline": roofline(fp64, ("hydro3d", "fp64")),
-                "note": "FP64 drop-in (FMA contraction); GB300 FP64 FMA rate measured at 1.19 TFLOP/s",
+                "note": "FP64 drop-in (FMA contraction); FP64 FMA rate of this GPU: %.2f TFLOP/s" % fma_peak["fp64"],
             },
             "mixed_over_fp64": value / v64,
             "l1_rel_err_rho_mixed_vs_fp64": l1,

@@ -143,6 +143,7 @@ def load_library():
         "ek_solver_set_state": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
         "ek_solver_get_state": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
         "ek_solver_set_gravity_field": (ctypes.c_int, [c_p, c_p, ctypes.c_int]),
+        "ek_measure_fma_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
         "ek_selftest_bounded_wait": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                                     ctypes.POINTER(ctypes.c_double)]),
         "ek_solver_compute_dt": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_double)]),
@@ -197,6 +198,15 @@ def selftest_bounded_wait(limit_us: int = 2000):
     _check(L.ek_selftest_bounded_wait(int(limit_us), ctypes.byref(expired), ctypes.byref(elapsed)),
            "selftest_bounded_wait")
     return bool(expired.value), elapsed.value
+
+
+def measure_fma_rate(precision: int) -> float:
+    """CUDA-core FMA throughput of the current device in TFLOP/s (2 FLOPs per
+    FMA): FP64 for EK_PREC_FP64, FP32 otherwise."""
+    L = load_library()
+    t = ctypes.c_double()
+    _check(L.ek_measure_fma_rate(int(precision), ctypes.byref(t)), "measure_fma_rate")
+    return t.value
 
 
 def _check(status: int, what: str, allow=()):

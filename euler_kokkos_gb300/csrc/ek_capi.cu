@@ -581,6 +581,61 @@ ek_selftest_bounded_wait(int limit_us, int * expired, double * elapsed_us)
 }
 
 extern "C" ek_status
+ek_measure_fma_rate(int precision, double * tflops)
+{
+  if (!tflops)
+    return fail(EK_ERR_INVALID, "ek_measure_fma_rate: bad argument");
+  int ndev = 0, dev = 0, sms = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(EK_ERR_NO_DEVICE, "no CUDA device available");
+  EK_CUDA(cudaGetDevice(&dev), "fma rate");
+  EK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "fma rate");
+  const bool   f64 = precision == EK_PREC_FP64;
+  const int    blocks = sms * 8;           // 8 resident 256-thread CTAs per SM
+  const int    iters = f64 ? 200 : 4000;   // a few milliseconds at GB300's rates
+  const size_t bytes = (size_t)blocks * 256 * (f64 ? sizeof(double) : sizeof(float));
+  void *       out = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t  e0 = nullptr, e1 = nullptr;
+  cudaError_t  e = cudaMalloc(&out, bytes);
+  if (e == cudaSuccess)
+    e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess)
+    e = cudaEventCreate(&e0);
+  if (e == cudaSuccess)
+    e = cudaEventCreate(&e1);
+  if (e == cudaSuccess)
+    e = ek_fast::fma_rate(f64 ? 0 : 1, blocks, 10, out, st); // warm-up
+  double best = 0.0;
+  for (int r = 0; r < 3 && e == cudaSuccess; ++r)
+  {
+    e = cudaEventRecord(e0, st);
+    if (e == cudaSuccess)
+      e = ek_fast::fma_rate(f64 ? 0 : 1, blocks, iters, out, st);
+    if (e == cudaSuccess)
+      e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess)
+      e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess)
+      e = cudaEventElapsedTime(&ms, e0, e1);
+    const double flops = 2.0 * 8 * 16 * (double)iters * blocks * 256;
+    if (e == cudaSuccess && ms > 0.f && flops / (ms * 1e9) > best)
+      best = flops / (ms * 1e9);
+  }
+  if (e0)
+    cudaEventDestroy(e0);
+  if (e1)
+    cudaEventDestroy(e1);
+  if (st)
+    cudaStreamDestroy(st);
+  cudaFree(out);
+  EK_CUDA(e, "fma rate");
+  *tflops = best;
+  return EK_OK;
+}
+
+extern "C" ek_status
 ek_solver_set_gravity_field(ek_solver * s, const double * G, int layout)
 {
   if (!s || (layout != EK_LAYOUT_LEFT && layout != EK_LAYOUT_RIGHT))

@@ -229,7 +229,45 @@ bounded_wait_kernel(unsigned long long limit_ns, unsigned long long * out)
     atomicAdd(out, 1ull);
   atomicMax(out + 1, dt);
 }
+
+// CUDA-core FMA throughput: every thread runs 8 independent FMA chains
+// (x = x * a + b), 16 steps unrolled per loop trip, so the FMA pipe never
+// waits on a dependency; the sum of the chains is stored so none is dead.
+template <class T>
+__global__ void __launch_bounds__(256)
+fma_rate_kernel(T * out, int iters, T a, T b)
+{
+  T x[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    x[c] = (T)(threadIdx.x + c);
+  for (int i = 0; i < iters; ++i)
+  {
+#pragma unroll
+    for (int u = 0; u < 16; ++u)
+    {
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        x[c] = fma(x[c], a, b);
+    }
+  }
+  T acc = x[0];
+#pragma unroll
+  for (int c = 1; c < 8; ++c)
+    acc += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
 } // namespace
+
+cudaError_t
+fma_rate(int prec, int blocks, int iters, void * out, cudaStream_t st)
+{
+  if (prec == 0)
+    fma_rate_kernel<double><<<blocks, 256, 0, st>>>((double *)out, iters, 0.999, 0.001);
+  else
+    fma_rate_kernel<float><<<blocks, 256, 0, st>>>((float *)out, iters, 0.999f, 0.001f);
+  return cudaGetLastError();
+}
 
 cudaError_t
 selftest_bounded_wait(unsigned long long limit_ns, unsigned long long * out, cudaStream_t st)

@@ -59,6 +59,8 @@ cudaError_t convert_stage(bool to_state, int prec, int layout, double * stage, v
 // The bounded mbarrier wait on a barrier nothing completes (one block):
 // out[0] = number of threads whose wait expired, out[1] = longest wait in ns.
 cudaError_t selftest_bounded_wait(unsigned long long limit_ns, unsigned long long * out, cudaStream_t st);
+// FMA chains for the CUDA-core FLOP rate: blocks x 256 threads x 8 chains x 16 x iters FMAs
+cudaError_t fma_rate(int prec, int blocks, int iters, void * out, cudaStream_t st);
 // Tensor map of a 3D hydro state U (box = the 3D kernel's tile plus halo, all
 // five variables); false when the layout does not allow tensor copies.
 bool hydro3d_tensor_map(int prec, const void * U, const KParams & P, CUtensorMap * out);

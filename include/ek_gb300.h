@@ -174,6 +174,12 @@ ek_status ek_solver_launch_count(ek_solver * s, long long * n);
  * Shows that a copy that never lands ends in an error status, not a hang. */
 ek_status ek_selftest_bounded_wait(int limit_us, int * expired, double * elapsed_us);
 
+/* Diagnostic: the device's CUDA-core FMA throughput in TFLOP/s (2 FLOPs per
+ * FMA), FP64 (precision EK_PREC_FP64) or FP32 (otherwise), measured with
+ * CUDA events over independent FMA chains on every SM (best of 3 launches of
+ * a few milliseconds).  The denominator of the step's FLOP roofline. */
+ek_status ek_measure_fma_rate(int precision, double * tflops);
+
 /* The CUDA stream (cudaStream_t) all work of the solver is issued on. */
 ek_status ek_solver_stream(ek_solver * s, void ** stream);
 

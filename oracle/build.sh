@@ -1,12 +1,15 @@
 #!/bin/sh
 # Builds the C restatement oracle (test infrastructure only) into
-# oracle/_build/libek_oracle.so, and, when the reference sources are present,
+# oracle/_build/libek_oracle.so (and its op-counting build), and, when the reference sources are present,
 # the reference harness into oracle/_ref/ (see Makefile.ref).
 set -e
 here=$(cd "$(dirname "$0")" && pwd)
 mkdir -p "$here/_build"
 ${CC:-gcc} -std=c99 -O2 -ffp-contract=off -fopenmp -fPIC -shared \
   -o "$here/_build/libek_oracle.so" "$here/ek_oracle.c" -lm
+# the op-counting build of the same restatement (FLOPs per cell-update)
+${CXX:-g++} -std=gnu++20 -O2 -ffp-contract=off -fPIC -shared -fpermissive -Wno-unknown-pragmas \
+  -o "$here/_build/libek_oracle_ops.so" "$here/ek_opcount.cpp" -lm
 if [ -d "${EK_REFERENCE:-/root/reference}/src" ] && [ "${EK_SKIP_REF:-0}" = "0" ]; then
   make -s -C "$here" -f Makefile.ref REF="${EK_REFERENCE:-/root/reference}" all
 fi

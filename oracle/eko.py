@@ -27,6 +27,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libek_oracle.so")
+OPS_LIB_PATH = os.path.join(HERE, "_build", "libek_oracle_ops.so")
 REF_RUN = os.path.join(HERE, "_ref", "ref_run")
 REF_RUN_FAST = os.path.join(HERE, "_ref", "ref_run_fast")
 
@@ -375,78 +376,96 @@ def run_reference_deck(ini_text: str, nsteps: int, workdir: str):
 # C restatement
 # --------------------------------------------------------------------------
 _lib = None
+_ops_lib = None
+
+
+def _load(path: str):
+    if not os.path.exists(path):
+        raise FileNotFoundError(path + " (run oracle/build.sh)")
+    L = ctypes.CDLL(path)
+    L.eko_create.restype = ctypes.c_void_p
+    L.eko_create.argtypes = [ctypes.POINTER(eko_params), ctypes.c_void_p, ctypes.c_double]
+    L.eko_destroy.argtypes = [ctypes.c_void_p]
+    L.eko_next_iteration.argtypes = [ctypes.c_void_p]
+    L.eko_finished.argtypes = [ctypes.c_void_p]
+    L.eko_get_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.eko_time.argtypes = [ctypes.c_void_p]
+    L.eko_time.restype = ctypes.c_double
+    L.eko_dt.argtypes = [ctypes.c_void_p]
+    L.eko_dt.restype = ctypes.c_double
+    L.eko_iteration.argtypes = [ctypes.c_void_p]
+    L.eko_set_gravity_field.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.eko_set_gravity_field.restype = ctypes.c_int
+    L.eko_num_threads.restype = ctypes.c_int
+    return L
 
 
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise FileNotFoundError(LIB_PATH + " (run oracle/build.sh)")
-        L = ctypes.CDLL(LIB_PATH)
-        L.eko_create.restype = ctypes.c_void_p
-        L.eko_create.argtypes = [ctypes.POINTER(eko_params), ctypes.c_void_p, ctypes.c_double]
-        L.eko_destroy.argtypes = [ctypes.c_void_p]
-        L.eko_next_iteration.argtypes = [ctypes.c_void_p]
-        L.eko_finished.argtypes = [ctypes.c_void_p]
-        L.eko_get_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
-        L.eko_time.argtypes = [ctypes.c_void_p]
-        L.eko_time.restype = ctypes.c_double
-        L.eko_dt.argtypes = [ctypes.c_void_p]
-        L.eko_dt.restype = ctypes.c_double
-        L.eko_iteration.argtypes = [ctypes.c_void_p]
-        L.eko_set_gravity_field.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
-        L.eko_set_gravity_field.restype = ctypes.c_int
-        L.eko_num_threads.restype = ctypes.c_int
-        _lib = L
+        _lib = _load(LIB_PATH)
     return _lib
+
+
+def ops_lib():
+    """The op-counting build of the restatement (ek_opcount.cpp)."""
+    global _ops_lib
+    if _ops_lib is None:
+        L = _load(OPS_LIB_PATH)
+        L.eko_ops_read.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.eko_ops_read.restype = ctypes.c_int
+        _ops_lib = L
+    return _ops_lib
 
 
 class Oracle:
     """One oracle run: create on an injected state, step, read back."""
 
-    def __init__(self, params: Params, U0: np.ndarray, t0: float = 0.0, gravity_field: np.ndarray | None = None):
+    def __init__(self, params: Params, U0: np.ndarray, t0: float = 0.0, gravity_field: np.ndarray | None = None,
+                 counting: bool = False):
         self.params = params
+        self._L = ops_lib() if counting else lib()
         self._cp = params.to_c()
         U0 = np.ascontiguousarray(U0, dtype=np.float64)
         assert U0.shape == params.shape, (U0.shape, params.shape)
-        self._h = lib().eko_create(ctypes.byref(self._cp), U0.ctypes.data, t0)
+        self._h = self._L.eko_create(ctypes.byref(self._cp), U0.ctypes.data, t0)
         if not self._h:
             raise ValueError("oracle does not support this configuration")
         if gravity_field is not None:
             G = np.ascontiguousarray(gravity_field, dtype=np.float64)
             assert G.shape == (params.dim,) + params.shape[1:], G.shape
-            if lib().eko_set_gravity_field(self._h, G.ctypes.data) != 0:
+            if self._L.eko_set_gravity_field(self._h, G.ctypes.data) != 0:
                 raise ValueError("gravity is not enabled in these parameters")
 
     def close(self):
         if self._h:
-            lib().eko_destroy(self._h)
+            self._L.eko_destroy(self._h)
             self._h = None
 
     def __del__(self):
         self.close()
 
     def next_iteration(self):
-        lib().eko_next_iteration(self._h)
+        self._L.eko_next_iteration(self._h)
 
     def finished(self) -> bool:
-        return bool(lib().eko_finished(self._h))
+        return bool(self._L.eko_finished(self._h))
 
     @property
     def t(self):
-        return lib().eko_time(self._h)
+        return self._L.eko_time(self._h)
 
     @property
     def dt(self):
-        return lib().eko_dt(self._h)
+        return self._L.eko_dt(self._h)
 
     @property
     def iteration(self):
-        return lib().eko_iteration(self._h)
+        return self._L.eko_iteration(self._h)
 
     def state(self) -> np.ndarray:
         U = np.empty(self.params.shape, dtype=np.float64)
-        lib().eko_get_state(self._h, U.ctypes.data)
+        self._L.eko_get_state(self._h, U.ctypes.data)
         return U
 
     def run(self, nsteps: int):
@@ -461,3 +480,29 @@ class Oracle:
 
 def num_threads() -> int:
     return lib().eko_num_threads()
+
+
+OP_KINDS = ("add", "mul", "div", "sqrt", "minmax", "abs", "neg", "cmp")
+
+
+def count_ops(params: Params, U0: np.ndarray, nsteps: int, t0: float = 0.0) -> dict:
+    """Floating-point operations of `nsteps` reference steps (implementationVersion 0,
+    the compute_dt reduction and boundary fill included) on the injected state U0,
+    counted by kind by the op-counting build; "per_cell" divides by the interior
+    cell-updates.  The constructor's own compute_dt is not counted."""
+    o = Oracle(params, U0, t0, counting=True)
+    L = o._L
+    L.eko_ops_reset()
+    done = 0
+    for _ in range(nsteps):
+        if o.finished():
+            break
+        o.next_iteration()
+        done += 1
+    out = (ctypes.c_ulonglong * len(OP_KINDS))()
+    L.eko_ops_read(out, len(OP_KINDS))
+    o.close()
+    counts = {k: int(out[i]) for i, k in enumerate(OP_KINDS)}
+    cells = params.nx * params.ny * (params.nz if params.dim == 3 else 1) * done
+    return {"counts": counts, "steps": done, "cell_updates": cells,
+            "per_cell": {k: v / cells for k, v in counts.items()}}

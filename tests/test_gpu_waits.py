@@ -23,3 +23,12 @@ def test_mbarrier_wait_expires_and_returns(limit_us):
 def test_selftest_arguments_checked():
     with pytest.raises(ek.EkError):
         ek.selftest_bounded_wait(0)
+
+
+def test_fma_rate_diagnostic():
+    # the FLOP roofline's denominators: CUDA-core FMA throughput; GB300 runs
+    # FP64 at a small fraction of the FP32 rate
+    f32 = ek.measure_fma_rate(ek.EK_PREC_MIXED)
+    f64 = ek.measure_fma_rate(ek.EK_PREC_FP64)
+    assert 1.0 < f32 < 500.0 and 0.01 < f64 < 100.0
+    assert f32 > 8 * f64
