@@ -53,10 +53,10 @@ BYTES_PER_CELL = {
 # profiles/); the per-launch traffic of the bench workload is this figure
 # times its interior cells (the traffic of these kernels grows with the cells).
 TRAFFIC_PER_CELL = {
-    ("hydro3d", "mixed"): 38.5,   # hydro3d_step<float>: 159.2 + 113.3 MB / 7.08 M cells
+    ("hydro3d", "mixed"): 38.3,   # hydro3d_step<float>: 158.6 + 112.5 MB / 7.08 M cells
     ("hydro3d", "fp64"): 78.2,    # hydro3d_step<double>: 306.3 + 247.4 MB / 7.08 M cells
-    ("mhd3d", "mixed"): 320.9,    # mhd_update_kernel<float>: 1961.9 + 309.9 MB / 7.08 M cells
-    ("mhd2d", "mixed"): 78.7,     # mhd2d_step_kernel<float>: 186.3 + 143.7 MB / 4.19 M cells
+    ("mhd3d", "mixed"): 325.7,    # mhd_update_kernel<float>: 1981.6 + 323.4 MB / 7.08 M cells
+    ("mhd2d", "mixed"): 78.1,     # mhd2d_step_kernel<float>: 186.4 + 141.0 MB / 4.19 M cells
 }
 
 # Floating-point operations per cell-update of the reference algorithm
