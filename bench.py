@@ -191,6 +191,20 @@ def measure_workload(ek, kind, prec, ini, U0, steps, warmup, sync, profile=True)
     return out
 
 
+def divb_inner(U, gw, margin, dx, dy, dz):
+    """max |div B| (FP64, on the host) of the cells at least `margin` cells
+    inside the interior of a 3D MHD state (face B at the left faces, U[5:8]),
+    one z-plane at a time."""
+    s = slice(gw + margin, U.shape[3] - gw - margin)
+    sp = slice(gw + margin + 1, U.shape[3] - gw - margin + 1)
+    out = 0.0
+    for k in range(gw + margin, U.shape[1] - gw - margin):
+        d = ((U[5, k, s, sp] - U[5, k, s, s]) / dx + (U[6, k, sp, s] - U[6, k, s, s]) / dy +
+             (U[7, k + 1, s, s] - U[7, k, s, s]) / dz)
+        out = max(out, float(np.abs(d).max()))
+    return out
+
+
 def e2e_measure(ek, prec, ini, U0, steps):
     """Reference-facing loop through the C ABI with host buffers in pinned
     memory: set_state (FP64 host array -> device, converted there), one
@@ -393,6 +407,10 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-mhd2d", action="store_true")
     ap.add_argument("--mhd2d-n", type=int, default=4096)
+    ap.add_argument("--no-mhd-blast", action="store_true")
+    ap.add_argument("--mhd-blast-n", type=int, default=256,
+                    help="grid of the low-beta MHD blast (512 = the configured grid; its FP64 run takes ~50 s)")
+    ap.add_argument("--mhd-blast-steps", type=int, default=30)
     ap.add_argument("--ens-n", type=int, default=512)
     ap.add_argument("--ens-steps", type=int, default=200)
     args = ap.parse_args()
@@ -503,6 +521,51 @@ def main():
             "roofline_fp64": roofline(m64, ("mhd3d", "fp64")),
             "config": "MHD_Muscl_3D Orszag-Tang %d^3, HLLD + CT, slope_type 2, CFL 0.8, periodic" % args.n,
         }
+
+    if not args.no_mhd_blast:
+        # low-beta MHD blast with a small transverse field (the configured field
+        # along x alone makes the reference's HLLD divide 0/0 in the first
+        # step); mixed vs FP64 rate, and both forms' states after the
+        # configured steps for the error and div B
+        nb = args.mhd_blast_n
+        ini_b, U0_b = P.mhd_blast_3d(n=nb, nsteps=10 ** 6, by_ratio=0.1)
+        mb = measure_workload(ek, "mhd3d", ek.EK_PREC_MIXED, ini_b, U0_b, args.mhd_steps, 3, sync)
+        mb64 = measure_workload(ek, "mhd3d", ek.EK_PREC_FP64, ini_b, U0_b, max(2, args.mhd_steps // 4), 3, sync,
+                                profile=False)
+        mb.pop("U"), mb64.pop("U")
+        res, inner = {}, {}
+        pb = ek.params_from_ini(ini_b)
+        for name, prec in (("mixed", ek.EK_PREC_MIXED), ("fp64", ek.EK_PREC_FP64)):
+            with ek.Solver(ek.params_from_ini(ini_b, precision=prec)) as s:
+                s.set_state(U0_b)
+                s.run(args.mhd_blast_steps)
+                Ub = s.get_state()
+                res[name] = (Ub[:2, 3:-3, 3:-3, 3:-3].copy(), s.totals(), s.dt_history())
+                inner[name] = divb_inner(Ub, 3, 4, pb.dx, pb.dy, pb.dz)
+                del Ub
+            sync()
+        (ab, totb, dtb), (bb, totb64, dtb64) = res["mixed"], res["fp64"]
+        l1b = [float(np.abs(ab[v] - bb[v]).sum() / np.abs(bb[v]).sum()) for v in (0, 1)]
+        linfb = [float(np.abs(ab[v] - bb[v]).max() / np.abs(bb[v]).max()) for v in (0, 1)]
+        del res, ab, bb, U0_b
+        vb = mb["cells"] * mb["steps"] / (maxt(mb["ms"]) / 1e3) / 1e6 * world
+        vb64 = mb64["cells"] * mb64["steps"] / (maxt(mb64["ms"]) / 1e3) / 1e6 * world
+        workloads["mhd_blast_lowbeta_%d" % nb] = {
+            "value_mixed": vb, "value_fp64": vb64, "unit": UNIT, "mixed_over_fp64": vb / vb64,
+            "ms_per_step_mixed": mb["ms"] / mb["steps"], "ms_per_step_fp64": mb64["ms"] / mb64["steps"],
+            "error_after_steps": len(dtb),
+            "l1_rel_err_rho_E_mixed_vs_fp64": l1b, "linf_rel_err_rho_E_mixed_vs_fp64": linfb,
+            "max_rel_dt_diff": float(np.abs(dtb / dtb64 - 1).max()),
+            "max_divB_mixed": float(totb[2]), "max_divB_fp64": float(totb64[2]),
+            "max_divB_inner_mixed": inner["mixed"], "max_divB_inner_fp64": inner["fp64"],
+            "divB_note": "max over all interior cells, and over the cells 4 or more cells inside "
+                         "(the outflow fill copies face B like cell values, BoundariesFunctors.h:814-831, "
+                         "so the boundary cells hold the rounding size of each form's face-B changes)",
+            "roofline_mixed": roofline(mb, ("mhd3d", "mixed")),
+            "config": "MHD_Muscl_3D low-beta blast %d^3, B = (10, 1, 0)/sqrt(4 pi), p 0.1 / 10 in r 0.1, "
+                      "0.5%% density noise, HLLD + CT, slope_type 2, CFL 0.8, outflow" % nb,
+        }
+        del mb, mb64
 
     if not args.no_mhd2d:
         n2 = args.mhd2d_n

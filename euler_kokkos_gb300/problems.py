@@ -224,19 +224,28 @@ def orszag_tang_2d(n=512, ny=None, nsteps=100, seed=0x0257A6, vz_noise=0.0, slop
 
 
 def mhd_blast_3d(n=512, nsteps=30, seed=0x10B37A, noise=0.005, slope_type=2.0, cfl=0.8,
-                 gamma0=5.0 / 3.0, riemann="hlld"):
+                 gamma0=5.0 / 3.0, riemann="hlld", by_ratio=0.0):
     """Low-beta 3D MHD blast: MHDInitFunctors3D.h:290-365 with uniform
-    B = (10/sqrt(4 pi), 0, 0) on every face (div B = 0 exactly), background
-    rho = 1 + noise*u, p 0.1, sphere r 0.1 at the centre with p 10."""
+    B = (10/sqrt(4 pi), by_ratio * 10/sqrt(4 pi), 0) on every face (div B = 0
+    exactly), background rho = 1 + noise*u, p 0.1, sphere r 0.1 at the centre
+    with p 10.
+
+    by_ratio = 0 is the configuration as specified.  With the field along x
+    only, the x-face fast speed equals the Alfven speed in the quiescent
+    medium, and the reference's HLLD star state divides 0/0
+    (RiemannSolvers_MHD.h:204-221): the run is NaN after its first step.  A
+    small uniform transverse component (by_ratio > 0) keeps the field
+    divergence-free and the plasma beta low, and avoids that degeneracy."""
     gw = 3
     bx = 10.0 / math.sqrt(4 * math.pi)
+    by = by_ratio * bx
     ini = _deck("MHD_Muscl_3D", n, n, n, (2,) * 6, gamma0, cfl, slope_type, riemann, "blast",
                 nsteps, {"blast": {"radius": 0.1, "center_x": 0.5, "center_y": 0.5, "center_z": 0.5,
                                    "density_in": 1.0, "density_out": 1.0, "pressure_in": 10.0,
-                                   "pressure_out": 0.1, "bx_in": bx, "by_in": 0.0, "bz_in": 0.0,
-                                   "bx_out": bx, "by_out": 0.0, "bz_out": 0.0}})
+                                   "pressure_out": 0.1, "bx_in": bx, "by_in": by, "bz_in": 0.0,
+                                   "bx_out": bx, "by_out": by, "bz_out": 0.0}})
     g = _f(gamma0)
-    bxf = _f(bx)
+    bxf, byf = _f(bx), _f(by)
     d = 1.0 / n
     s = n + 2 * gw
     x = _centres(n, gw, 0.0, d)
@@ -249,7 +258,8 @@ def mhd_blast_3d(n=512, nsteps=30, seed=0x10B37A, noise=0.005, slope_type=2.0, c
     U = np.zeros((8, s, s, s))
     U[0] = np.where(inside, 1.0, 1.0 * (1.0 + noise * u))
     U[5] = bxf
-    emag = 0.5 * (bxf * bxf + 0.0 + 0.0)
+    U[6] = byf
+    emag = 0.5 * (bxf * bxf + byf * byf + 0.0)
     U[1] = np.where(inside, _f(10.0) / (g - 1.0) + emag, _f(0.1) / (g - 1.0) + emag)
     return ini, U
 
