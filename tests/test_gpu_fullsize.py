@@ -1,0 +1,92 @@
+"""Parity at the configured workloads' full sizes.
+
+* 2D implode 256^2, 100 steps, FP64: the exact build equals the oracle bit for
+  bit (state and dt sequence); the FMA build is within the drop-in tolerances
+  (dt 1e-13, fields 1e-11 relative L-infinity).
+* 3D blast 256^3, 50 steps: the mixed form is within 1e-5 relative L1 of the
+  FP64 drop-in in density and energy; mass is conserved in both forms while
+  the blast is inside the box (outflow boundaries, nothing has left).
+* 3D MHD Orszag-Tang 256^3, 100 steps: mixed within 1e-5 relative L1 of FP64;
+  periodic box: mass and total energy conserved, max |div B| at FP64
+  round-off in both forms.
+* 512-instance Kelvin-Helmholtz ensemble, 200 steps: sampled instances equal
+  their single-solver runs bit for bit (state and dt sequence).
+"""
+
+import numpy as np
+import pytest
+
+import eko
+import euler_kokkos_gb300 as ek
+from euler_kokkos_gb300 import problems as P
+from helpers import interior, rel_l1, rel_linf
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(ini, U0, nsteps, **over):
+    p = ek.params_from_ini(ini, **over)
+    with ek.Solver(p) as s:
+        s.set_state(U0)
+        tot0 = s.totals()
+        done = s.run(nsteps)
+        return s.get_state(), s.dt_history(), tot0, s.totals(), done
+
+
+def test_implode_256_fp64_matches_oracle():
+    ini, U0 = P.implode_2d(n=256, nsteps=100)
+    Ue, de, _, _, n = _run(ini, U0, 100, exact_fp=1)
+    assert n == 100
+    o = eko.Oracle(eko.params_from_ini(ini), U0)
+    do = o.run(100)
+    Uo = o.state()
+    o.close()
+    assert np.array_equal(de, do)
+    assert np.array_equal(interior(Ue, 2, 2), interior(Uo, 2, 2))
+    Uf, df, _, _, _ = _run(ini, U0, 100)
+    assert np.abs(df / do - 1).max() <= 1e-13
+    assert rel_linf(interior(Uf, 2, 2), interior(Uo, 2, 2)).max() <= 1e-11
+
+
+def test_blast_256_mixed_vs_fp64():
+    ini, U0 = P.blast_3d(n=256, nsteps=50)
+    Um, dm, t0m, t1m, n = _run(ini, U0, 50, precision=ek.EK_PREC_MIXED)
+    U64, d64, t064, t164, _ = _run(ini, U0, 50)
+    assert n == 50
+    err = rel_l1(interior(Um, 2, 3), interior(U64, 2, 3))
+    assert err[0] <= 1e-5 and err[1] <= 1e-5, err
+    assert np.abs(dm / d64 - 1).max() <= 1e-5
+    # FP64 totals of each form: mass conserved (to the form's rounding)
+    assert abs(t164[0] / t064[0] - 1) <= 1e-12
+    assert abs(t1m[0] / t0m[0] - 1) <= 1e-6
+
+
+def test_orszag_tang_256_mixed_vs_fp64_conservation_divb():
+    ini, U0 = P.orszag_tang_3d(n=256, nsteps=100)
+    p = eko.params_from_ini(ini)
+    Um, dm, t0m, t1m, n = _run(ini, U0, 100, precision=ek.EK_PREC_MIXED)
+    U64, d64, t064, t164, _ = _run(ini, U0, 100)
+    assert n == 100
+    err = rel_l1(interior(Um, 3, 3), interior(U64, 3, 3))
+    assert err[0] <= 1e-5 and err[1] <= 1e-5, err
+    assert np.abs(dm / d64 - 1).max() <= 1e-5
+    for a, b, tol in ((t064, t164, 1e-11), (t0m, t1m, 1e-6)):
+        assert abs(b[0] / a[0] - 1) <= tol and abs(b[1] / a[1] - 1) <= tol, (a, b)
+    bscale = np.abs(U0[5:]).max() / p.dx
+    assert t1m[2] <= 1e-12 * bscale and t164[2] <= 1e-12 * bscale, (t1m[2], t164[2], bscale)
+
+
+def test_kh_ensemble_512_matches_single_solvers():
+    cases = P.kh_ensemble(n_inst=512, nsteps=10 ** 6)
+    params = [ek.params_from_ini(ini, precision=ek.EK_PREC_MIXED) for ini, _ in cases]
+    with ek.Ensemble(params) as e:
+        for i, (_, U0) in enumerate(cases):
+            e.set_state(i, U0)
+        e.run(200)
+        e.synchronize()
+        for i in (0, 1, 255, 510, 511):
+            with ek.Solver(params[i]) as s:
+                s.set_state(cases[i][1])
+                s.run(200)
+                assert np.array_equal(e.dt_history(i), s.dt_history()), i
+                assert np.array_equal(e.get_state(i), s.get_state()), i
