@@ -805,13 +805,8 @@ sync_from_clock(ek_solver * s)
     return fail(EK_ERR_CUDA, "a tensor copy of the step kernel did not complete within its 1 s wait limit");
   s->iteration = h.iteration;
   s->t = h.t[h.iteration % 3];
-  if (h.iteration > 0 && h.iteration - 1 < s->dtcap)
-  {
-    EK_CUDA(cudaMemcpyAsync(&s->dt, s->dtlog + (h.iteration - 1), sizeof(double), cudaMemcpyDeviceToHost,
-                            s->stream),
-            "dt read");
-    EK_CUDA(cudaStreamSynchronize(s->stream), "dt read");
-  }
+  if (h.iteration > 0)
+    s->dt = h.last_dt; // the dt of the last step, in the same read (one host round trip per step)
   if (!(s->dt > 0.0) || !std::isfinite(s->dt))
     return fail(EK_ERR_NONFINITE, "time step is not finite and positive (dt = " + std::to_string(s->dt) + ")");
   return EK_OK;
@@ -1345,12 +1340,8 @@ ek_ensemble_time(ek_ensemble * e, int i, double * t, double * dt, int * iteratio
     return st;
   v->iteration = h.iteration;
   v->t = h.t[h.iteration % 3];
-  if (h.iteration > 0 && h.iteration - 1 < v->dtcap)
-  {
-    EK_CUDA(cudaMemcpyAsync(&v->dt, v->dtlog + (h.iteration - 1), sizeof(double), cudaMemcpyDeviceToHost, v->stream),
-            "dt");
-    EK_CUDA(cudaStreamSynchronize(v->stream), "dt");
-  }
+  if (h.iteration > 0)
+    v->dt = h.last_dt;
   return ek_solver_time(v, t, dt, iteration);
 }
 

@@ -91,6 +91,7 @@ struct DevClock
   int                error;     // sticky device error flags
   double *           dtlog;     // dt of each step (capacity dtcap)
   int                dtcap;
+  double             last_dt;   // dt of the last step taken (read with the clock)
   StepConsts         sc[3];     // per slot, by the last block of the CFL kernel
   unsigned int       fin[3];    // blocks of that kernel done (reset by the last)
 };
@@ -521,6 +522,7 @@ step_commit(DevClock * clk, int step, double t, double dt)
   clk->key[(step + 2) % 3] = EK_KEY_LOWEST;
   if (step < clk->dtcap)
     clk->dtlog[step] = dt;
+  clk->last_dt = dt;
   clk->iteration = step + 1;
 }
 

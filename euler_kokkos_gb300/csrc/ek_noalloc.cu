@@ -97,6 +97,7 @@ noalloc_clock_init(ekc::DevClock * clk, double t0, double * dt_slot)
   clk->error = 0;
   clk->dtlog = dt_slot;
   clk->dtcap = 1;
+  clk->last_dt = 0.0;
   *dt_slot = __longlong_as_double(0x7ff8000000000000ll);
 }
 
