@@ -178,8 +178,14 @@ validate(const ek_params & p)
     return fail(EK_ERR_UNSUPPORTED, "Hydro_Muscl_3D: the reference's 3D solver dispatch has no hll branch");
   if (p.mhd && p.riemann != 1 && p.riemann != 2 && p.riemann != 4)
     return fail(EK_ERR_UNSUPPORTED, "MHD: riemann must be llf, hll or hlld");
-  if (p.slope_type != 1.0 && p.slope_type != 2.0)
-    return fail(EK_ERR_UNSUPPORTED, "slope_type must be 1 (minmod) or 2 (MC)");
+  // slope_unsplit_hydro_{2d,3d} (HydroBaseFunctor2D.h:488-516,
+  // HydroBaseFunctor3D.h:498-576) zero the slopes for slope_type 0 and limit
+  // them for 1 and 2; the MHD slope routines (MHDBaseFunctor3D.h:379,
+  // MHDBaseFunctor2D.h:369-420) only handle 1 and 2.  For other values the
+  // reference leaves the slopes unwritten, so they are refused here.
+  if (p.slope_type != 1.0 && p.slope_type != 2.0 && (p.mhd || p.slope_type != 0.0))
+    return fail(EK_ERR_UNSUPPORTED, p.mhd ? "MHD: slope_type must be 1 (minmod) or 2 (MC)"
+                                          : "hydro: slope_type must be 0 (first order), 1 (minmod) or 2 (MC)");
   // implementationVersion (SolverHydroMuscl.cpp:234-293, SolverMHDMuscl.cpp:397-445,
   // 490-560): hydro 1 is version 0's arithmetic split into more kernels (the
   // same bits); hydro 2 adds the face fluxes to the cells with atomics

@@ -48,6 +48,10 @@ CASES = {
     "mhdblast3d_10_nan": (lambda: P.mhd_blast_3d(n=10, nsteps=3), 3),
     # the same low-beta blast with a small transverse field (no 0/0 in HLLD)
     "mhdblast3d_lowbeta_12": (lambda: P.mhd_blast_3d(n=12, nsteps=6, by_ratio=0.1), 6),
+    # hydro slope_type 0: zero slopes, first order (HydroBaseFunctor2D.h:488-502,
+    # HydroBaseFunctor3D.h:498-520)
+    "implode2d_first_order": (lambda: P.implode_2d(n=24, nsteps=10, slope_type=0.0), 10),
+    "blast3d_first_order": (lambda: P.blast_3d(n=10, nsteps=5, slope_type=0.0), 5),
     "ot2d_24": (lambda: P.orszag_tang_2d(n=24, nsteps=8), 8),
     "ot2d_noise_20x16": (lambda: P.orszag_tang_2d(n=20, ny=16, nsteps=6, vz_noise=1e-2), 6),
     "mhd2d_random_periodic": (lambda: P.smooth_random(dim=2, mhd=True, nx=20, ny=14, seed=8,

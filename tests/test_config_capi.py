@@ -128,7 +128,8 @@ def test_create_without_gpu_fails_cleanly():
 def test_create_rejects_unsupported_configurations():
     # validation happens before any device call
     p = ek.params_from_ini(DECK)
-    for bad in (dict(riemann=4), dict(riemann=7), dict(slope_type=3.0), dict(implementation_version=3),
+    for bad in (dict(riemann=4), dict(riemann=7), dict(slope_type=3.0), dict(slope_type=1.5),
+                dict(slope_type=-1.0), dict(implementation_version=3),
                 dict(nx=1, isize=5), dict(exact_fp=1, precision=1)):
         with pytest.raises(ek.EkError) as e:
             ek.Solver(p.copy(**bad))
@@ -143,6 +144,11 @@ def test_create_rejects_unsupported_configurations():
         with pytest.raises(ek.EkError) as e:
             ek.Solver(q)
         assert e.value.status == 2, (dim, v)
+    # the MHD slope routines have no slope_type 0 branch (MHDBaseFunctor3D.h:379)
+    for ini in (P.orszag_tang_3d(n=8, nsteps=1)[0], P.orszag_tang_2d(n=8, nsteps=1)[0]):
+        with pytest.raises(ek.EkError) as e:
+            ek.Solver(ek.params_from_ini(ini).copy(slope_type=0.0))
+        assert e.value.status == 2
 
 
 def test_gravity_sections_parse_like_reference():
