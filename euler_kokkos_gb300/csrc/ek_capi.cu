@@ -243,6 +243,9 @@ make_kparams(const ek_params & p)
   k.idx = (float)(1.0 / p.dx);
   k.idy = (float)(1.0 / p.dy);
   k.idz = (float)(1.0 / (p.dim == 3 ? p.dz : 1.0));
+  k.idxd = 1.0 / p.dx;
+  k.idyd = 1.0 / p.dy;
+  k.idzd = 1.0 / (p.dim == 3 ? p.dz : 1.0);
   k.mhd_stage = p.mhd_stage;
   k.gamma6 = p.gamma6;
   k.smallpp = p.smallpp;

@@ -58,6 +58,7 @@ struct KParams
   // FP64 arithmetic (one FP64 instruction costs 64 FP32 ones on GB300)
   float     gamma0f, smallrf, smallcf, smallpf, slopef;
   float     idx, idy, idz; // 1/dx, 1/dy, 1/dz
+  double    idxd, idyd, idzd; // 1/dx, 1/dy, 1/dz in FP64 (FP64 FMA build's CFL)
   int       mhd_stage;     // MHD update: stage the trace planes in shared memory
   double    gamma6, smallpp; // riemann_approx constants (HydroParams.cpp:353-356)
   float     gamma6f, smallppf;

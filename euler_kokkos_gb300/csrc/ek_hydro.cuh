@@ -14,7 +14,17 @@ template <class R>
 struct HydroConst
 {
   R gamma0, smallr, smallp, smallc, slope_type, gamma6, smallpp;
+  R entho; // 1 / (gamma0 - 1), the value every Riemann solver of the reference computes
 };
+
+// Quotients by a shared denominator: the exact build divides each one, as the
+// reference does; the FMA builds take one reciprocal and multiply (FP64: a
+// division is a sequence of FMAs on GB300's 1/64-rate FP64 pipe).
+#ifdef EK_EXACT_ONLY
+constexpr bool kShareRecip = false;
+#else
+constexpr bool kShareRecip = true;
+#endif
 
 // slope_unsplit_hydro_3d_scalar, one direction (HydroBaseFunctor3D.h:413-462,
 // HydroBaseFunctor2D.h:423-453): minmod (slope_type 1) / MC (slope_type 2)
@@ -51,12 +61,15 @@ __device__ __forceinline__ void
 hydro_prims(const R (&u)[NV], R (&q)[NV], const HydroConst<R> & C)
 {
   const R d = fmax(u[ID], C.smallr);
-  // FP32: one reciprocal of the density for the four quotients
+  // one reciprocal of the density for the four quotients (FP32: approximate;
+  // FP64 exact build: four divisions)
   R id = R(0);
   if constexpr (sizeof(R) == 4)
     id = rcp_a(d);
+  else if constexpr (kShareRecip)
+    id = R(1) / d;
   auto over_d = [&](R x) {
-    if constexpr (sizeof(R) == 4)
+    if constexpr (sizeof(R) == 4 || kShareRecip)
       return x * id;
     else
       return x / d;
@@ -121,8 +134,10 @@ hydro_sources(const R (&q)[NV], const R (&dx)[NV], const R (&dy)[NV], const R (&
   R       ir = R(0);
   if constexpr (sizeof(R) == 4)
     ir = rcp_a(r);
+  else if constexpr (kShareRecip)
+    ir = R(1) / r;
   auto over_r = [&](R x) {
-    if constexpr (sizeof(R) == 4)
+    if constexpr (sizeof(R) == 4 || kShareRecip)
       return x * ir;
     else
       return x / r;
@@ -169,7 +184,7 @@ template <class R, int NV>
 __device__ __forceinline__ void
 hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
 {
-  const R entho = R(1) / (C.gamma0 - R(1));
+  const R entho = C.entho;
   const R rl = fmax(ql[ID], C.smallr);
   const R pl = fmax(ql[IP], rl * C.smallp);
   const R ul = ql[IU];
@@ -215,6 +230,12 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
     ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc;
     ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc;
   }
+  else if constexpr (kShareRecip)
+  {
+    const R irc = R(1) / (rcr + rcl);
+    ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc;
+    ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc;
+  }
   else
   {
     ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
@@ -250,15 +271,33 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
   {
     uo = ustar;
     ptoto = ptotstar;
-    ro = rl * (SL - ul) / (SL - ustar);
-    etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) / (SL - ustar);
+    if constexpr (kShareRecip)
+    {
+      const R is = R(1) / (SL - ustar);
+      ro = rl * (SL - ul) * is;
+      etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) * is;
+    }
+    else
+    {
+      ro = rl * (SL - ul) / (SL - ustar);
+      etoto = ((SL - ul) * etotl - ptotl * ul + ptotstar * ustar) / (SL - ustar);
+    }
   }
   else if (SR > R(0))
   {
     uo = ustar;
     ptoto = ptotstar;
-    ro = rr * (SR - ur) / (SR - ustar);
-    etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) / (SR - ustar);
+    if constexpr (kShareRecip)
+    {
+      const R is = R(1) / (SR - ustar);
+      ro = rr * (SR - ur) * is;
+      etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) * is;
+    }
+    else
+    {
+      ro = rr * (SR - ur) / (SR - ustar);
+      etoto = ((SR - ur) * etotr - ptotr * ur + ptotstar * ustar) / (SR - ustar);
+    }
   }
   else
   {
@@ -285,7 +324,7 @@ cmpflx(const R (&qg)[NV], R (&flux)[NV], const HydroConst<R> & C)
   flux[IV] = flux[ID] * qg[IV];
   if constexpr (NV == 5)
     flux[IW] = flux[ID] * qg[IW];
-  const R entho = R(1) / (C.gamma0 - R(1));
+  const R entho = C.entho;
   R       ekin = R(0.5) * qg[ID] * (qg[IU] * qg[IU] + qg[IV] * qg[IV]);
   if constexpr (NV == 5)
     ekin += R(0.5) * qg[ID] * (qg[IW] * qg[IW]);
@@ -390,7 +429,7 @@ template <class R, int NV>
 __device__ __forceinline__ void
 riemann_llf(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
 {
-  const R entho = R(1) / (C.gamma0 - R(1));
+  const R entho = C.entho;
   const R rl = fmax(ql[ID], C.smallr), ul = ql[IU], pl = fmax(ql[IP], rl * C.smallp);
   const R rr = fmax(qr[ID], C.smallr), ur = qr[IU], pr = fmax(qr[IP], rr * C.smallp);
   const R cl = sqrt(C.gamma0 * pl / rl);
@@ -410,7 +449,7 @@ template <class R, int NV>
 __device__ __forceinline__ void
 riemann_hll(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
 {
-  const R entho = R(1) / (C.gamma0 - R(1));
+  const R entho = C.entho;
   const R rl = fmax(ql[ID], C.smallr), ul = ql[IU], pl = fmax(ql[IP], rl * C.smallp);
   const R rr = fmax(qr[ID], C.smallr), ur = qr[IU], pr = fmax(qr[IP], rr * C.smallp);
   const R cl = sqrt(C.gamma0 * pl / rl);
@@ -455,7 +494,7 @@ hydro_invdt(const R (&u)[NV], const HydroConst<R> & C, const KParams & P)
   const R c = hydro_sound<R>(q[ID], q[IP], C);
   const R vx = c + fabs(q[IU]);
   const R vy = c + fabs(q[IV]);
-  if constexpr (sizeof(R) == 8)
+  if constexpr (sizeof(R) == 8 && !kShareRecip)
   {
     if constexpr (NV == 4)
       return vx / P.dx + vy / P.dy;
@@ -463,6 +502,17 @@ hydro_invdt(const R (&u)[NV], const HydroConst<R> & C, const KParams & P)
     {
       const R vz = c + fabs(q[IW]);
       return vx / P.dx + vy / P.dy + vz / P.dz;
+    }
+  }
+  else if constexpr (sizeof(R) == 8)
+  {
+    // FP64 FMA build: the inverse cell sizes prepared on the host
+    if constexpr (NV == 4)
+      return vx * P.idxd + vy * P.idyd;
+    else
+    {
+      const R vz = c + fabs(q[IW]);
+      return vx * P.idxd + vy * P.idyd + vz * P.idzd;
     }
   }
   else

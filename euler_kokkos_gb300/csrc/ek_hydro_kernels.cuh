@@ -28,6 +28,7 @@ hydro_const(const KParams & P)
     C.slope_type = P.slope_type;
     C.gamma6 = P.gamma6;
     C.smallpp = P.smallpp;
+    C.entho = 1.0 / (P.gamma0 - 1.0);
   }
   else
   {
@@ -38,6 +39,7 @@ hydro_const(const KParams & P)
     C.slope_type = P.slopef;
     C.gamma6 = P.gamma6f;
     C.smallpp = P.smallppf;
+    C.entho = 1.0f / (P.gamma0f - 1.0f);
   }
   return C;
 }
