@@ -83,6 +83,15 @@ struct StepConsts
   double t, dt, dtdx, dtdy, dtdz;
   int    step, active;
 };
+// Quotients by a shared denominator: the exact build divides each one, as the
+// reference does; the FMA builds take one reciprocal and multiply (FP64: a
+// division is a sequence of FMAs on GB300's 1/64-rate FP64 pipe).
+#ifdef EK_EXACT_ONLY
+constexpr bool kShareRecip = false;
+#else
+constexpr bool kShareRecip = true;
+#endif
+
 struct DevClock
 {
   unsigned long long key[3];

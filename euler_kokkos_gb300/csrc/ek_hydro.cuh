@@ -17,14 +17,6 @@ struct HydroConst
   R entho; // 1 / (gamma0 - 1), the value every Riemann solver of the reference computes
 };
 
-// Quotients by a shared denominator: the exact build divides each one, as the
-// reference does; the FMA builds take one reciprocal and multiply (FP64: a
-// division is a sequence of FMAs on GB300's 1/64-rate FP64 pipe).
-#ifdef EK_EXACT_ONLY
-constexpr bool kShareRecip = false;
-#else
-constexpr bool kShareRecip = true;
-#endif
 
 // slope_unsplit_hydro_3d_scalar, one direction (HydroBaseFunctor3D.h:413-462,
 // HydroBaseFunctor2D.h:423-453): minmod (slope_type 1) / MC (slope_type 2)

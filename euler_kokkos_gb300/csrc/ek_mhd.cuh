@@ -21,9 +21,16 @@ mhd_speed_fast(const R (&q)[8], R gamma0)
 {
   const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
   const R b2 = a * a + b * b + c * c;
+  const R bn = DIR == 0 ? a : (DIR == 1 ? b : c);
+  if constexpr (kShareRecip)
+  {
+    const R id = R(1) / d;
+    const R c2 = gamma0 * p * id;
+    const R d2 = R(0.5) * (b2 * id + c2);
+    return sqrt(d2 + sqrt(d2 * d2 - c2 * bn * bn * id));
+  }
   const R c2 = gamma0 * p / d;
   const R d2 = R(0.5) * (b2 / d + c2);
-  const R bn = DIR == 0 ? a : (DIR == 1 ? b : c);
   return sqrt(d2 + sqrt(d2 * d2 - c2 * bn * bn / d));
 }
 
@@ -33,7 +40,8 @@ mhd_speed_fast(const R (&q)[8], R gamma0)
 // max-reduction and dt stay FP64).
 template <class R>
 __device__ __forceinline__ R
-mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz, float idx, float idy, float idz)
+mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz, float idx, float idy, float idz,
+          double idxd, double idyd, double idzd)
 {
   const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
   const R b2 = a * a + b * b + c * c;
@@ -48,6 +56,18 @@ mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz, float idx,
     const float cfz = sqrt_a(d2 + sqrt_a(dd - cr * c * c));
     return (cfx + fabsf(q[IU])) * idx + (cfy + fabsf(q[IV])) * idy + (cfz + fabsf(q[IW])) * idz;
   }
+  if constexpr (kShareRecip)
+  {
+    // FP64 FMA build: one reciprocal of the density, host-prepared 1/dx
+    const R id = R(1) / d;
+    const R c2 = gamma0 * p * id;
+    const R d2 = R(0.5) * (b2 * id + c2);
+    const R dd = d2 * d2, cr = c2 * id;
+    const R cfx = sqrt(d2 + sqrt(dd - cr * a * a));
+    const R cfy = sqrt(d2 + sqrt(dd - cr * b * b));
+    const R cfz = sqrt(d2 + sqrt(dd - cr * c * c));
+    return (cfx + fabs(q[IU])) * idxd + (cfy + fabs(q[IV])) * idyd + (cfz + fabs(q[IW])) * idzd;
+  }
   const R c2 = gamma0 * p / d;
   const R d2 = R(0.5) * (b2 / d + c2);
   const R cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d));
@@ -56,10 +76,7 @@ mhd_invdt(const R (&q)[8], R gamma0, double dx, double dy, double dz, float idx,
   const R vx = cfx + fabs(q[IU]);
   const R vy = cfy + fabs(q[IV]);
   const R vz = cfz + fabs(q[IW]);
-  if constexpr (sizeof(R) == 8)
-    return vx / dx + vy / dy + vz / dz;
-  else
-    return vx * idx + vy * idy + vz * idz;
+  return vx / dx + vy / dy + vz / dz;
 }
 
 // constoprim_mhd (MHDBaseFunctor3D.h:194-242).  u: hydro variables of the
@@ -81,6 +98,13 @@ mhd_constoprim(const R (&u)[5], const R (&bl)[3], const R (&br)[3], R (&q)[8], c
     q[IV] = u[IV] * id;
     q[IW] = u[IW] * id;
   }
+  else if constexpr (kShareRecip)
+  {
+    id = R(1) / q[ID];
+    q[IU] = u[IU] * id;
+    q[IV] = u[IV] * id;
+    q[IW] = u[IW] * id;
+  }
   else
   {
     q[IU] = u[IU] / q[ID];
@@ -93,7 +117,7 @@ mhd_constoprim(const R (&u)[5], const R (&bl)[3], const R (&br)[3], R (&q)[8], c
   const R eken = R(0.5) * (q[IU] * q[IU] + q[IV] * q[IV] + q[IW] * q[IW]);
   const R emag = R(0.5) * (q[IA] * q[IA] + q[IB] * q[IB] + q[IC] * q[IC]);
   R       eint;
-  if constexpr (sizeof(R) == 4)
+  if constexpr (sizeof(R) == 4 || kShareRecip)
     eint = (u[IP] - emag) * id - eken;
   else
     eint = (u[IP] - emag) / q[ID] - eken;
@@ -292,11 +316,16 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   const R sr = fmax(ul, ur) + fmax(cfastl, cfastr);
   const R rcl = rl * (ul - sl);
   const R rcr = rr * (sr - ur);
-  const R ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
-  const R ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+  // FP64 FMA build: one reciprocal per shared denominator (kShareRecip)
+  const R irc = kShareRecip ? R(1) / (rcr + rcl) : R(0);
+  const R ustar = kShareRecip ? (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc
+                              : (rcr * ur + rcl * ul + (ptotl - ptotr)) / (rcr + rcl);
+  const R ptotstar = kShareRecip ? (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc
+                                 : (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
 
   R estar;
-  const R rstarl = rl * (sl - ul) / (sl - ustar);
+  const R isl = kShareRecip ? R(1) / (sl - ustar) : R(0);
+  const R rstarl = kShareRecip ? rl * (sl - ul) * isl : rl * (sl - ul) / (sl - ustar);
   estar = rl * (sl - ul) * (sl - ustar) - a * a;
   const R el = rl * (sl - ul) * (sl - ul) - a * a;
   R       vstarl, wstarl, bstarl, cstarl;
@@ -307,6 +336,14 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
     wstarl = wl;
     cstarl = cl;
   }
+  else if constexpr (kShareRecip)
+  {
+    const R ie = R(1) / estar;
+    vstarl = vl - a * bl * (ustar - ul) * ie;
+    bstarl = bl * el * ie;
+    wstarl = wl - a * cl * (ustar - ul) * ie;
+    cstarl = cl * el * ie;
+  }
   else
   {
     vstarl = vl - a * bl * (ustar - ul) / estar;
@@ -316,12 +353,14 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   }
   const R vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
   const R etotstarl =
-    ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) / (sl - ustar);
+    kShareRecip ? ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) * isl
+                : ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) / (sl - ustar);
   const R sqrrstarl = sqrt(rstarl);
   const R calfvenl = fabs(a) / sqrrstarl;
   const R sal = ustar - calfvenl;
 
-  const R rstarr = rr * (sr - ur) / (sr - ustar);
+  const R isr = kShareRecip ? R(1) / (sr - ustar) : R(0);
+  const R rstarr = kShareRecip ? rr * (sr - ur) * isr : rr * (sr - ur) / (sr - ustar);
   estar = rr * (sr - ur) * (sr - ustar) - a * a;
   const R er = rr * (sr - ur) * (sr - ur) - a * a;
   R       vstarr, wstarr, bstarr, cstarr;
@@ -332,6 +371,14 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
     wstarr = wr;
     cstarr = cr;
   }
+  else if constexpr (kShareRecip)
+  {
+    const R ie = R(1) / estar;
+    vstarr = vr - a * br * (ustar - ur) * ie;
+    bstarr = br * er * ie;
+    wstarr = wr - a * cr * (ustar - ur) * ie;
+    cstarr = cr * er * ie;
+  }
   else
   {
     vstarr = vr - a * br * (ustar - ur) / estar;
@@ -341,7 +388,8 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   }
   const R vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
   const R etotstarr =
-    ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) / (sr - ustar);
+    kShareRecip ? ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) * isr
+                : ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) / (sr - ustar);
   const R sqrrstarr = sqrt(rstarr);
   const R calfvenr = fabs(a) / sqrrstarr;
   const R sar = ustar + calfvenr;
@@ -370,10 +418,13 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   else
   {
     // double-star region (only evaluated when sampled)
+    const R iss = kShareRecip ? R(1) / (sqrrstarl + sqrrstarr) : R(0);
     const R vstarstar =
-      (sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl)) / (sqrrstarl + sqrrstarr);
+      kShareRecip ? (sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl)) * iss
+                  : (sqrrstarl * vstarl + sqrrstarr * vstarr + sgnm * (bstarr - bstarl)) / (sqrrstarl + sqrrstarr);
     const R wstarstar =
-      (sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl)) / (sqrrstarl + sqrrstarr);
+      kShareRecip ? (sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl)) * iss
+                  : (sqrrstarl * wstarl + sqrrstarr * wstarr + sgnm * (cstarr - cstarl)) / (sqrrstarl + sqrrstarr);
     const R bstarstar =
       (sqrrstarl * bstarr + sqrrstarr * bstarl + sgnm * sqrrstarl * sqrrstarr * (vstarr - vstarl)) /
       (sqrrstarl + sqrrstarr);
@@ -661,9 +712,16 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
   {
   auto fast = [gamma0](const EdgeQ<R> & q, bool ydir) {
     const R b2 = q.a * q.a + q.b * q.b + q.c * q.c;
+    const R bn = ydir ? q.b : q.a;
+    if constexpr (kShareRecip)
+    {
+      const R ir = R(1) / q.r;
+      const R c2 = gamma0 * q.p * ir;
+      const R d2 = R(0.5) * (b2 * ir + c2);
+      return sqrt(d2 + sqrt(d2 * d2 - c2 * bn * bn * ir));
+    }
     const R c2 = gamma0 * q.p / q.r;
     const R d2 = R(0.5) * (b2 / q.r + c2);
-    const R bn = ydir ? q.b : q.a;
     return sqrt(d2 + sqrt(d2 * d2 - c2 * bn * bn / q.r));
   };
   const R rLL = LL.r, pLL = LL.p, uLL = LL.u, vLL = LL.v, aLL = LL.a, bLL = LL.b, cLL = LL.c;
@@ -702,38 +760,47 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
     (rcLLy * vLL + rcLRy * vLR + rcRLy * vRL + rcRRy * vRR + (PtotLL - PtotLR + PtotRL - PtotRR)) /
     (rcLLy + rcLRy + rcRLy + rcRRy);
 
-  const R rstarLLx = rLL * (SL - uLL) / (SL - ustar);
-  const R BstarLL = bLL * (SL - uLL) / (SL - ustar);
-  const R rstarLLy = rLL * (SB - vLL) / (SB - vstar);
-  const R AstarLL = aLL * (SB - vLL) / (SB - vstar);
-  const R rstarLL = rLL * (SL - uLL) / (SL - ustar) * (SB - vLL) / (SB - vstar);
+  // quotients by the six shared denominators: divided in the exact build (the
+  // reference's expressions), one reciprocal each in the FMA build
+  const R dSLu = SL - ustar, dSRu = SR - ustar, dSBv = SB - vstar, dSTv = ST - vstar;
+  const R iSLu = kShareRecip ? R(1) / dSLu : R(0), iSRu = kShareRecip ? R(1) / dSRu : R(0);
+  const R iSBv = kShareRecip ? R(1) / dSBv : R(0), iSTv = kShareRecip ? R(1) / dSTv : R(0);
+  auto q_SLu = [&](R x) { return kShareRecip ? x * iSLu : x / dSLu; };
+  auto q_SRu = [&](R x) { return kShareRecip ? x * iSRu : x / dSRu; };
+  auto q_SBv = [&](R x) { return kShareRecip ? x * iSBv : x / dSBv; };
+  auto q_STv = [&](R x) { return kShareRecip ? x * iSTv : x / dSTv; };
+  const R rstarLLx = q_SLu(rLL * (SL - uLL));
+  const R BstarLL = q_SLu(bLL * (SL - uLL));
+  const R rstarLLy = q_SBv(rLL * (SB - vLL));
+  const R AstarLL = q_SBv(aLL * (SB - vLL));
+  const R rstarLL = q_SBv(q_SLu(rLL * (SL - uLL)) * (SB - vLL));
   const R EstarLLx = ustar * BstarLL - vLL * aLL;
   const R EstarLLy = uLL * bLL - vstar * AstarLL;
   const R EstarLL = ustar * BstarLL - vstar * AstarLL;
 
-  const R rstarLRx = rLR * (SL - uLR) / (SL - ustar);
-  const R BstarLR = bLR * (SL - uLR) / (SL - ustar);
-  const R rstarLRy = rLR * (ST - vLR) / (ST - vstar);
-  const R AstarLR = aLR * (ST - vLR) / (ST - vstar);
-  const R rstarLR = rLR * (SL - uLR) / (SL - ustar) * (ST - vLR) / (ST - vstar);
+  const R rstarLRx = q_SLu(rLR * (SL - uLR));
+  const R BstarLR = q_SLu(bLR * (SL - uLR));
+  const R rstarLRy = q_STv(rLR * (ST - vLR));
+  const R AstarLR = q_STv(aLR * (ST - vLR));
+  const R rstarLR = q_STv(q_SLu(rLR * (SL - uLR)) * (ST - vLR));
   const R EstarLRx = ustar * BstarLR - vLR * aLR;
   const R EstarLRy = uLR * bLR - vstar * AstarLR;
   const R EstarLR = ustar * BstarLR - vstar * AstarLR;
 
-  const R rstarRLx = rRL * (SR - uRL) / (SR - ustar);
-  const R BstarRL = bRL * (SR - uRL) / (SR - ustar);
-  const R rstarRLy = rRL * (SB - vRL) / (SB - vstar);
-  const R AstarRL = aRL * (SB - vRL) / (SB - vstar);
-  const R rstarRL = rRL * (SR - uRL) / (SR - ustar) * (SB - vRL) / (SB - vstar);
+  const R rstarRLx = q_SRu(rRL * (SR - uRL));
+  const R BstarRL = q_SRu(bRL * (SR - uRL));
+  const R rstarRLy = q_SBv(rRL * (SB - vRL));
+  const R AstarRL = q_SBv(aRL * (SB - vRL));
+  const R rstarRL = q_SBv(q_SRu(rRL * (SR - uRL)) * (SB - vRL));
   const R EstarRLx = ustar * BstarRL - vRL * aRL;
   const R EstarRLy = uRL * bRL - vstar * AstarRL;
   const R EstarRL = ustar * BstarRL - vstar * AstarRL;
 
-  const R rstarRRx = rRR * (SR - uRR) / (SR - ustar);
-  const R BstarRR = bRR * (SR - uRR) / (SR - ustar);
-  const R rstarRRy = rRR * (ST - vRR) / (ST - vstar);
-  const R AstarRR = aRR * (ST - vRR) / (ST - vstar);
-  const R rstarRR = rRR * (SR - uRR) / (SR - ustar) * (ST - vRR) / (ST - vstar);
+  const R rstarRRx = q_SRu(rRR * (SR - uRR));
+  const R BstarRR = q_SRu(bRR * (SR - uRR));
+  const R rstarRRy = q_STv(rRR * (ST - vRR));
+  const R AstarRR = q_STv(aRR * (ST - vRR));
+  const R rstarRR = q_STv(q_SRu(rRR * (SR - uRR)) * (ST - vRR));
   const R EstarRRx = ustar * BstarRR - vRR * aRR;
   const R EstarRRy = uRR * bRR - vstar * AstarRR;
   const R EstarRR = ustar * BstarRR - vstar * AstarRR;
@@ -751,11 +818,15 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
   const R SAR = fmax(ustar + calfvenR, R(0));
   const R SAB = fmin(vstar - calfvenB, R(0));
   const R SAT = fmax(vstar + calfvenT, R(0));
+  const R dA = SAR - SAL, dB = SAT - SAB;
+  const R iA = kShareRecip ? R(1) / dA : R(0), iB = kShareRecip ? R(1) / dB : R(0);
+  auto q_A = [&](R x) { return kShareRecip ? x * iA : x / dA; };
+  auto q_B = [&](R x) { return kShareRecip ? x * iB : x / dB; };
 
-  const R AstarT = (SAR * AstarRR - SAL * AstarLR) / (SAR - SAL);
-  const R AstarB = (SAR * AstarRL - SAL * AstarLL) / (SAR - SAL);
-  const R BstarR = (SAT * BstarRR - SAB * BstarRL) / (SAT - SAB);
-  const R BstarL = (SAT * BstarLR - SAB * BstarLL) / (SAT - SAB);
+  const R AstarT = q_A(SAR * AstarRR - SAL * AstarLR);
+  const R AstarB = q_A(SAR * AstarRL - SAL * AstarLL);
+  const R BstarR = q_B(SAT * BstarRR - SAB * BstarRL);
+  const R BstarL = q_B(SAT * BstarLR - SAB * BstarLL);
 
   R       E = 0, tmpE = 0;
   const int SB_pos = (int)(1 + copysign(R(1), SB)) / 2, SB_neg = 1 - SB_pos;
@@ -763,23 +834,22 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
   const int SL_pos = (int)(1 + copysign(R(1), SL)) / 2, SL_neg = 1 - SL_pos;
   const int SR_pos = (int)(1 + copysign(R(1), SR)) / 2, SR_neg = 1 - SR_pos;
 
-  tmpE = (SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL) /
-           (SAR - SAL) / (SAT - SAB) -
-         SAT * SAB / (SAT - SAB) * (AstarT - AstarB) + SAR * SAL / (SAR - SAL) * (BstarR - BstarL);
+  tmpE = q_B(q_A(SAL * SAB * EstarRR - SAL * SAT * EstarRL - SAR * SAB * EstarLR + SAR * SAT * EstarLL)) -
+         q_B(SAT * SAB) * (AstarT - AstarB) + q_A(SAR * SAL) * (BstarR - BstarL);
   E += (R)(SB_neg * ST_pos * SL_neg * SR_pos) * tmpE;
 
-  tmpE = (SAR * EstarLLx - SAL * EstarRLx + SAR * SAL * (bRL - bLL)) / (SAR - SAL);
+  tmpE = q_A(SAR * EstarLLx - SAL * EstarRLx + SAR * SAL * (bRL - bLL));
   tmpE = (R)SL_pos * ELL + (R)(SL_neg * SR_neg) * ERL + (R)(SL_neg * SR_pos) * tmpE;
   E += (R)SB_pos * tmpE;
 
-  tmpE = (SAR * EstarLRx - SAL * EstarRRx + SAR * SAL * (bRR - bLR)) / (SAR - SAL);
+  tmpE = q_A(SAR * EstarLRx - SAL * EstarRRx + SAR * SAL * (bRR - bLR));
   tmpE = (R)SL_pos * ELR + (R)(SL_neg * SR_neg) * ERR + (R)(SL_neg * SR_pos) * tmpE;
   E += (R)(SB_neg * ST_neg) * tmpE;
 
-  tmpE = (SAT * EstarLLy - SAB * EstarLRy - SAT * SAB * (aLR - aLL)) / (SAT - SAB);
+  tmpE = q_B(SAT * EstarLLy - SAB * EstarLRy - SAT * SAB * (aLR - aLL));
   E += (R)(SB_neg * ST_pos * SL_pos) * tmpE;
 
-  tmpE = (SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL)) / (SAT - SAB);
+  tmpE = q_B(SAT * EstarRLy - SAB * EstarRRy - SAT * SAB * (aRR - aRL));
   E += (R)(SB_neg * ST_pos * SL_neg * SR_neg) * tmpE;
   return E;
   }

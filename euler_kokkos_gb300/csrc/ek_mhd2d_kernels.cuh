@@ -150,6 +150,15 @@ mhd2d_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step
       cfy = sqrt_a(d2 + sqrt_a(d2 * d2 - cr * b * b));
       tmax = fmax(tmax, (cfx + fabsf(q[IU])) * P.idx + (cfy + fabsf(q[IV])) * P.idy);
     }
+    else if constexpr (kShareRecip)
+    {
+      // FP64 FMA build: one reciprocal of the density, host-prepared 1/dx
+      const R id = R(1) / d, c2 = C.gamma0 * p * id;
+      const R d2 = R(0.5) * (b2 * id + c2), cr = c2 * id;
+      cfx = sqrt(d2 + sqrt(d2 * d2 - cr * a * a));
+      cfy = sqrt(d2 + sqrt(d2 * d2 - cr * b * b));
+      tmax = fmax(tmax, (cfx + fabs(q[IU])) * P.idxd + (cfy + fabs(q[IV])) * P.idyd);
+    }
     else
     {
       const R c2 = C.gamma0 * p / d;

@@ -135,7 +135,7 @@ mhd_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step,
   for_interior_rows(P, [&](int i, int j, int k) {
     R q[8];
     cell_prims_global<S, R>(m, P, C, i, j, k, q);
-    tmax = fmax(tmax, mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz, P.idx, P.idy, P.idz));
+    tmax = fmax(tmax, mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz, P.idx, P.idy, P.idz, P.idxd, P.idyd, P.idzd));
   });
   block_max_commit<256>(cand_key((double)tmax), key ? key : &clk->key[step % 3]);
   if (!key)
@@ -267,9 +267,15 @@ trace_cell_compact(const R * sB, int bslot[4], const R * sQ, int qslot[3], const
   const R C_ = Cc;
   const R sr0 = (-u * drx - dux * r) * dtdx + (-v * dry - dvy * r) * dtdy + (-w * drz - dwz * r) * dtdz;
   R su0, sv0, sw0;
-  if constexpr (sizeof(R) == 4)
+  if constexpr (sizeof(R) == 4 || kShareRecip)
   {
-    const float ir = rcp_a(r);
+    // one reciprocal of the density (FP32: approximate; FP64 FMA build: exact
+    // reciprocal, then products); the exact build divides below
+    R ir;
+    if constexpr (sizeof(R) == 4)
+      ir = rcp_a(r);
+    else
+      ir = R(1) / r;
     su0 = (-u * dux - (dpx + B * dBx + C_ * dCx) * ir) * dtdx + (-v * duy + B * dAy * ir) * dtdy +
           (-w * duz + C_ * dAz * ir) * dtdz;
     sv0 = (-u * dvx + A * dBx * ir) * dtdx + (-v * dvy - (dpy + A * dAy + C_ * dCy) * ir) * dtdy +
