@@ -805,14 +805,17 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
   const R EstarRRy = uRR * bRR - vstar * AstarRR;
   const R EstarRR = ustar * BstarRR - vstar * AstarRR;
 
-  const R calfvenL = fmax5(fabs(aLR) / sqrt(rstarLRx), fabs(AstarLR) / sqrt(rstarLR),
-                           fabs(aLL) / sqrt(rstarLLx), fabs(AstarLL) / sqrt(rstarLL), smallc);
-  const R calfvenR = fmax5(fabs(aRR) / sqrt(rstarRRx), fabs(AstarRR) / sqrt(rstarRR),
-                           fabs(aRL) / sqrt(rstarRLx), fabs(AstarRL) / sqrt(rstarRL), smallc);
-  const R calfvenB = fmax5(fabs(bLL) / sqrt(rstarLLy), fabs(BstarLL) / sqrt(rstarLL),
-                           fabs(bRL) / sqrt(rstarRLy), fabs(BstarRL) / sqrt(rstarRL), smallc);
-  const R calfvenT = fmax5(fabs(bLR) / sqrt(rstarLRy), fabs(BstarLR) / sqrt(rstarLR),
-                           fabs(bRR) / sqrt(rstarRRy), fabs(BstarRR) / sqrt(rstarRR), smallc);
+  // |B| / sqrt(rho*): the reference's quotient in the exact build; one
+  // reciprocal square root (CUDA's rsqrt) in the FMA build
+  auto b_over_sqrt = [](R b, R r) { return kShareRecip ? fabs(b) * rsqrt(r) : fabs(b) / sqrt(r); };
+  const R calfvenL = fmax5(b_over_sqrt(aLR, rstarLRx), b_over_sqrt(AstarLR, rstarLR),
+                           b_over_sqrt(aLL, rstarLLx), b_over_sqrt(AstarLL, rstarLL), smallc);
+  const R calfvenR = fmax5(b_over_sqrt(aRR, rstarRRx), b_over_sqrt(AstarRR, rstarRR),
+                           b_over_sqrt(aRL, rstarRLx), b_over_sqrt(AstarRL, rstarRL), smallc);
+  const R calfvenB = fmax5(b_over_sqrt(bLL, rstarLLy), b_over_sqrt(BstarLL, rstarLL),
+                           b_over_sqrt(bRL, rstarRLy), b_over_sqrt(BstarRL, rstarRL), smallc);
+  const R calfvenT = fmax5(b_over_sqrt(bLR, rstarLRy), b_over_sqrt(BstarLR, rstarLR),
+                           b_over_sqrt(bRR, rstarRRy), b_over_sqrt(BstarRR, rstarRR), smallc);
 
   const R SAL = fmin(ustar - calfvenL, R(0));
   const R SAR = fmax(ustar + calfvenR, R(0));
