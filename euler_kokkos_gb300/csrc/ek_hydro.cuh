@@ -37,6 +37,19 @@ slope1(R q, R qp, R qm, R st)
   const R dlft = st * (q - qm);
   const R drgt = st * (qp - q);
   const R dcen = R(0.5) * (qp - qm);
+  if constexpr (kShareRecip)
+  {
+    // FP64 FMA build: the minima of non-negative values as integer minima of
+    // their bit patterns (same order; a NaN pattern is the larger, as fmin
+    // drops NaN) and the sign by copysign, on the integer pipes instead of
+    // GB300's 1/64-rate FP64 pipe; only the sign of a zero slope can differ
+    auto minpos = [](double a, double b) {
+      return __longlong_as_double(min(__double_as_longlong(a), __double_as_longlong(b)));
+    };
+    const R slop = minpos(fabs(dlft), fabs(drgt));
+    const R dlim = ((dlft * drgt) <= R(0)) ? R(0) : slop;
+    return copysign(minpos(dlim, fabs(dcen)), dcen);
+  }
   const R dsgn = (dcen >= R(0)) ? R(1) : R(-1);
   const R slop = fmin(fabs(dlft), fabs(drgt));
   R       dlim = slop;
