@@ -76,7 +76,8 @@ typedef struct ek_params
   int    nOutput;
   int    nlog;
   int    precision; /* ek_precision; [gb300] precision = fp64 | mixed */
-  int    exact_fp;  /* 1: FP64 kernels built without FMA contraction ([gb300] exact = 1) */
+  int    exact_fp;  /* 1: FP64 kernels with the reference's arithmetic, no FMA contraction and
+                       every division, bitwise equal to it ([gb300] exact = 1) */
   int    kchunk;    /* 3D planes per CTA column (0: automatic; [gb300] kchunk) */
   int    mhd_stage; /* MHD update kernel stages the trace planes in shared memory ([gb300] mhd_stage) */
   char   solver_name[32];
