@@ -250,13 +250,13 @@ ek_status ek_ensemble_info(ek_ensemble * e, long long * interior_cells, int * ti
 ek_status ek_ensemble_stream(ek_ensemble * e, void ** stream);
 
 /* ---------------------------------------------------------------------------
- * One MHD_Muscl_3D step that allocates no device memory (no counterpart in
- * the reference).  For callers that own every byte of device memory in their
- * own pool and hand the step only its two state arrays -- as the reference's
- * SolverMHDMuscl<3>::godunov_unsplit_impl(data_in, data_out)
- * (SolverMHDMuscl.cpp:463-568), which this call computes, receives only two
- * DataArrays -- and for which a cudaMalloc / cudaFree pair per step (each
- * synchronising the device) is not acceptable.
+ * One MHD_Muscl_3D FP64 step on caller-owned device arrays that allocates no
+ * device memory (no counterpart in the reference).  For callers that own
+ * every byte of device memory in their own pool (a Kokkos memory space, an
+ * embedding code that budgets the whole HBM) and hand the step only its two
+ * state arrays, and for which a cudaMalloc / cudaFree pair per step (each
+ * synchronising the device) is not acceptable.  It runs the same kernels as a
+ * step of ek_solver_next_iteration.
  *
  * The step's temporary (the 47 x FP64 per-cell compact trace) lives in one
  * static device array of EK_NOALLOC_SCRATCH_BYTES, held by every GPU context
@@ -273,11 +273,15 @@ ek_status ek_ensemble_stream(ek_ensemble * e, void ** stream);
  * params->exact_fp selects the bitwise-parity build.
  * dt_out: NULL (the call is asynchronous on `stream`) or a host pointer that
  * receives the step's dt (the call then synchronises `stream`;
- * EK_ERR_NONFINITE if dt is not finite and positive).
+ * EK_ERR_NONFINITE if dt is not finite and positive).  An asynchronous call
+ * cannot report its own non-finite dt: the next call records it on the
+ * device and the next call with dt_out returns EK_ERR_NONFINITE for it (that
+ * call's own step is still taken).
  * stream: a cudaStream_t, NULL for the default stream.
  *
- * The first call on each device (that device current) resolves the array's
- * address with cudaGetSymbolAddress: make it before any stream capture.
+ * The first call in each device context (that device current) resolves the
+ * array's address with cudaGetSymbolAddress: make it before any stream
+ * capture.  After cudaDeviceReset the next call resolves it again.
  * Calls on one device share the array, so calls in flight at the same time
  * (other streams, other host threads) race: serialise them (one stream). */
 #define EK_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)

@@ -1,7 +1,8 @@
 #!/bin/sh
 # Builds the C restatement oracle (test infrastructure only) into
 # oracle/_build/libek_oracle.so (and its op-counting build), and, when the reference sources are present,
-# the reference harness into oracle/_ref/ (see Makefile.ref).
+# the reference harness into oracle/_ref/ (see Makefile.ref) when EK_REFERENCE
+# names the reference's source tree.
 set -e
 here=$(cd "$(dirname "$0")" && pwd)
 mkdir -p "$here/_build"
@@ -10,6 +11,7 @@ ${CC:-gcc} -std=c99 -O2 -ffp-contract=off -fopenmp -fPIC -shared \
 # the op-counting build of the same restatement (FLOPs per cell-update)
 ${CXX:-g++} -std=gnu++20 -O2 -ffp-contract=off -fPIC -shared -fpermissive -Wno-unknown-pragmas \
   -o "$here/_build/libek_oracle_ops.so" "$here/ek_opcount.cpp" -lm
-if [ -d "${EK_REFERENCE:-/root/reference}/src" ] && [ "${EK_SKIP_REF:-0}" = "0" ]; then
-  make -s -C "$here" -f Makefile.ref REF="${EK_REFERENCE:-/root/reference}" all
+# the reference harness: only where EK_REFERENCE names the reference's source tree
+if [ -n "${EK_REFERENCE:-}" ] && [ -d "${EK_REFERENCE}/src" ] && [ "${EK_SKIP_REF:-0}" = "0" ]; then
+  make -s -C "$here" -f Makefile.ref REF="${EK_REFERENCE}" all
 fi

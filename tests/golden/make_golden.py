@@ -6,8 +6,9 @@ oracle/build.sh) run on a seeded initial state from euler_kokkos_gb300.problems.
 Stored per case (compressed .npz): the .ini text, the injected initial state
 U0, the final state U, the dt sequence and the final time.
 
-Run from the repository root (needs the reference sources, so only where
-they are present):  python tests/golden/make_golden.py [case ...]
+Run from the repository root, with EK_REFERENCE naming the reference's source
+tree (oracle/build.sh builds the harness from it):
+    EK_REFERENCE=<reference tree> python tests/golden/make_golden.py [case ...]
 (no case names: every case)
 """
 
@@ -128,7 +129,7 @@ DECKS = {
     "deck_implode_2D_v2": ("test_implode_2D.ini", {"nx": 32, "ny": 16}, 10, 2),
     "deck_kelvin_helmholtz_3D_v2": ("test_muscl_kelvin_helmholtz_3D.ini", {"nx": 16, "ny": 16, "nz": 16}, 5, 2),
 }
-SETTINGS = os.path.join(os.environ.get("EK_REFERENCE", "/root/reference"), "settings")
+SETTINGS = os.path.join(os.environ.get("EK_REFERENCE", ""), "settings")
 
 
 def deck_text(fname, mesh, nsteps, version):
@@ -226,6 +227,8 @@ def make_vtk(names):
 
 
 def main():
+    if not os.path.isdir(os.path.join(os.environ.get("EK_REFERENCE", ""), "src")):
+        sys.exit("make_golden: set EK_REFERENCE to the reference's source tree")
     out_dir = os.path.dirname(os.path.abspath(__file__))
     work = tempfile.mkdtemp(prefix="ek_golden_")
     names = sys.argv[1:] or list(CASES) + list(VTK_CASES) + list(DECKS)

@@ -56,3 +56,38 @@ def test_driver_reproduces_reference_bitwise(name, tmp_path):
     assert np.array_equal(interior(out["U"], p.gw, p.dim), interior(g["U"], p.gw, p.dim), equal_nan=True)
     assert out["iteration"] == int(g["iteration"])
     assert np.array_equal(np.array(out["t"]), g["t"], equal_nan=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,nlog", [("blast3d_12", 1), ("ot3d_12", 2)])
+def test_driver_prints_the_reference_log_and_perf_lines(name, nlog, tmp_path):
+    """The step log of next_iteration_impl (SolverHydroMuscl.h:646-652,
+    SolverMHDMuscl.h:752-758: iteration, dt and t before the step, every nlog
+    steps), "final time is" (main.cpp:150-151) and the timer summary with the
+    Perf line (solver_utils.h:15-55)."""
+    import re
+
+    g = load_golden(name)
+    ini = re.sub(r"(?m)^nlog=.*$", "nlog=%d" % nlog, str(g["ini"])) + "\n[gb300]\nexact=1\n"
+    (tmp_path / "case.ini").write_text(ini)
+    p = eko.params_from_ini(ini)
+    eko.write_ekst(str(tmp_path / "u0.ekst"), g["U0"], p.dim, p.gw)
+    dts = g["dts"]
+    r = _run([tmp_path / "case.ini", len(dts), tmp_path / "out.ekst", tmp_path / "u0.ekst"])
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    assert lines[0] == "Start computation...."
+    want, t = [], 0.0
+    for n in range(len(dts)):
+        # m_dt before step n is the previous step's dt (the constructor's for n = 0)
+        if n % nlog == 0:
+            want.append("time step=%7d (dt=% 10.8f t=% 10.8f)" % (n, dts[max(n - 1, 0)], t))
+        t += dts[n]
+    assert [l for l in lines if l.startswith("time step=")] == want
+    assert "final time is %f" % t in lines
+    for label in ("total        time", "godunov      time", "compute dt   time", "boundaries   time",
+                  "comp. prim.  time", "comp. flux   time", "hydro update time", "io           time"):
+        assert any(l.startswith(label + " : ") for l in lines), label
+    perf = [l for l in lines if l.startswith("Perf              : ")]
+    assert len(perf) == 1 and perf[0].endswith(" number of Mcell-updates/s")
+    assert float(perf[0].split(":")[1].split()[0]) > 0

@@ -1,15 +1,20 @@
 """ek_mhd3d_step_noalloc: the MHD_Muscl_3D step on a static device scratch.
 
-The entry point allocates no device memory: its compact-trace temporary lives
-in a fixed-size file-scope device array.  The GPU tests call it through the C
-ABI on caller-owned device arrays (allocated here with torch, as a host code's
-own pool would) and compare two calls in a row with two steps of the solver
-entry point (ek_solver_next_iteration) from the same state.  Both run the same
-kernels, so the interiors and the time steps agree to the last bit; the
-tolerance is written as 0 for the bitwise build and 1e-13 relative for the FMA
-build.  The input's ghost cells are filled with NaN: the step maps ghost
-positions to interior cells through the boundary conditions and never reads
-them.
+The entry point allocates no device memory, for host codes that keep every
+byte of device memory in their own pool and cannot hand the library a trace
+buffer: its compact-trace temporary lives in a fixed-size file-scope device
+array.  The GPU tests call it through the C ABI on caller-owned device arrays
+(allocated here with torch, as a host code's own pool would):
+* two calls in a row against two steps of the solver entry point
+  (ek_solver_next_iteration) from the same state.  Both run the same kernels,
+  so the interiors and the time steps agree to the last bit; the tolerance is
+  written as 0 for the bitwise build and 1e-13 relative for the FMA build;
+* two calls in a row of the bitwise build against two steps of the oracle
+  (the reference algorithm's CPU restatement): equal bit for bit;
+* a non-finite dt of an asynchronous call (no dt pointer) is reported by the
+  next call that asks for its dt.
+The input's ghost cells are filled with NaN: the step maps ghost positions to
+interior cells through the boundary conditions and never reads them.
 
 The CPU tests check the host-side rejections, which happen before any device
 call.  This module is collected last so that it runs both alone and after the
@@ -21,11 +26,13 @@ import ctypes
 import numpy as np
 import pytest
 
+import eko
 import euler_kokkos_gb300 as ek
 from euler_kokkos_gb300 import problems as P
-from helpers import interior
+from helpers import interior, load_golden
 
 EK_OK, EK_ERR_INVALID, EK_ERR_UNSUPPORTED = 0, 1, 2
+EK_ERR_NONFINITE = ek.EK_ERR_NONFINITE
 SCRATCH_BYTES = 64 << 20
 TOL = {1: 0.0, 0: 1e-13}
 
@@ -95,6 +102,69 @@ def test_two_noalloc_steps_match_solver_steps(deck, exact):
         assert np.all(np.isfinite(a))
         err = np.max(np.abs(a - b)) / np.max(np.abs(b))
         assert err <= tol, err
+
+
+def _device_state(U0, gw):
+    import torch
+
+    h = np.full_like(U0, np.nan)
+    h[:, gw:-gw, gw:-gw, gw:-gw] = U0[:, gw:-gw, gw:-gw, gw:-gw]
+    torch.cuda.set_device(0)
+    A = torch.from_numpy(h).to("cuda")
+    B = torch.zeros_like(A)
+    torch.cuda.synchronize()
+    return A, B
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("deck", sorted(_decks()))
+def test_two_noalloc_steps_match_the_oracle_bitwise(deck):
+    ini, U0 = _decks()[deck]
+    p = ek.params_from_ini(ini, exact_fp=1)
+    gw = p.ghost_width
+    o = eko.Oracle(eko.params_from_ini(ini), U0)
+    o.next_iteration()
+    O1, odt0 = o.state(), o.dt
+    o.next_iteration()
+    O2, odt1 = o.state(), o.dt
+    o.close()
+
+    L = _lib()
+    A, B = _device_state(U0, gw)
+    dt0 = _step_noalloc(L, p, A.data_ptr(), B.data_ptr(), 0.0)
+    V1 = B.cpu().numpy()
+    dt1 = _step_noalloc(L, p, B.data_ptr(), A.data_ptr(), 0.0 + dt0)
+    V2 = A.cpu().numpy()
+    assert dt0 == odt0 and dt1 == odt1, (dt0, dt1, odt0, odt1)
+    assert np.array_equal(interior(V1, gw, 3), interior(O1, gw, 3))
+    assert np.array_equal(interior(V2, gw, 3), interior(O2, gw, 3))
+
+
+@pytest.mark.gpu
+def test_asynchronous_nonfinite_dt_is_reported_by_the_next_synchronous_call():
+    # the reference's low-beta MHD blast divides 0/0 in its first step: the
+    # third step's dt is not positive (fixture written by the reference)
+    g = load_golden("mhdblast3d_10_nan")
+    assert not (g["dts"][2] > 0)
+    p = ek.params_from_ini(str(g["ini"]), exact_fp=1)
+    L = _lib()
+    A, B = _device_state(g["U0"], p.ghost_width)
+    C = A.clone()
+    dt0 = _step_noalloc(L, p, A.data_ptr(), B.data_ptr(), 0.0)  # finite, synchronous
+    assert dt0 == g["dts"][0]
+    f = L.ek_mhd3d_step_noalloc
+    # two asynchronous steps; the second one's dt is not positive
+    assert f(ctypes.byref(p), ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(C.data_ptr()), dt0, None, None) == EK_OK
+    assert f(ctypes.byref(p), ctypes.c_void_p(C.data_ptr()), ctypes.c_void_p(A.data_ptr()), 0.0, None, None) == EK_OK
+    dt = ctypes.c_double(0.0)
+    st = f(ctypes.byref(p), ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()), 0.0, ctypes.byref(dt), None)
+    assert st == EK_ERR_NONFINITE and "earlier call" in L.ek_last_error().decode()
+    # reported once: the next synchronous call reports only its own step
+    st = f(ctypes.byref(p), ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(A.data_ptr()), 0.0, ctypes.byref(dt), None)
+    assert st == EK_ERR_NONFINITE and "not finite and positive" in L.ek_last_error().decode()
+    # a finite step afterwards is clean
+    A2, B2 = _device_state(g["U0"], p.ghost_width)
+    assert _step_noalloc(L, p, A2.data_ptr(), B2.data_ptr(), 0.0) == dt0
 
 
 def test_rejects_grid_beyond_the_static_scratch():
