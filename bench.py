@@ -1,12 +1,14 @@
 """Benchmark: Mcell-updates/s of the unsplit MUSCL-Hancock step on one GB300.
 
-Headline workload (the reference's 3D blast config, 256^3): Hydro_Muscl_3D,
-HLLC, minmod, CFL 0.7, outflow boundaries, seeded 1% density noise.  A
-"step" is one full time step (dt reduction, fused fluxes and update) of the
-whole grid.  ``value`` is the mixed-FP32 form; the FP64 drop-in is measured
-on the same workload beside it, with the L1 density error between the two.
-The CT-MHD Orszag-Tang 256^3 workload is measured the same way under
-``workloads``.
+Headline workload (the 3D MHD Orszag-Tang configuration, 256^3):
+MHD_Muscl_3D, HLLD + constrained transport, slope_type 2, CFL 0.8, periodic
+boundaries, seeded 1e-3 noise in v_z.  A "step" is one full time step (CFL
+dt, trace, fluxes, emfs, update and CT update) of the whole grid.  ``value``
+is the mixed-FP32 form; the FP64 drop-in is measured on the same workload
+beside it, and the two forms are compared after the configuration's 100
+steps (L1 / L-inf error, dt sequence, max |div B|).  The 3D hydro blast, the
+2D implode (FP64), the low-beta MHD blast, 2D MHD Orszag-Tang and the
+Kelvin-Helmholtz ensemble are measured under ``workloads``.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -39,6 +41,7 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 
 # algorithmic bytes per cell-update: one read and one write of U
 BYTES_PER_CELL = {
+    ("hydro2d", "fp64"): 2 * 4 * 8,
     ("hydro3d", "mixed"): 2 * 5 * 4,
     ("hydro3d", "fp64"): 2 * 5 * 8,
     ("mhd3d", "mixed"): 2 * (5 * 4 + 3 * 8),
@@ -47,16 +50,27 @@ BYTES_PER_CELL = {
     ("mhd2d", "fp64"): 2 * 8 * 8,
 }
 
-# DRAM bytes (read + write) per interior cell of one launch of the dominant
-# kernel, from ncu captures of `python bench.py --n 192 --steps 3 --warmup 3
-# --mhd-steps 3 --no-cpu --no-ensemble --mhd2d-n 2048` (the summaries are in
-# profiles/); the per-launch traffic of the bench workload is this figure
-# times its interior cells (the traffic of these kernels grows with the cells).
+HEADLINE = "3D MHD Orszag-Tang %d^3 on [0,1]^3, MHD_Muscl_3D, HLLD + CT, slope_type 2, CFL 0.8, periodic"
+
+# the kernels of one step: ek_solver_kernel_time ids and names
+KERNEL_NAMES = {
+    "hydro3d": ((0, "hydro3d_step"),),
+    "hydro2d": ((0, "hydro2d_step"),),
+    "mhd3d": ((2, "mhd_dt_kernel"), (1, "mhd_trace_kernel"), (0, "mhd_update_kernel")),
+    "mhd2d": ((2, "mhd2d_dt_kernel"), (0, "mhd2d_step_kernel")),
+}
+
+# DRAM bytes (read + write) per interior cell of one launch of each kernel,
+# from ncu captures of the same kernels on 192^3 / 2048^2 cases (the summaries
+# are in profiles/); a launch's traffic on the bench workload is this figure
+# times its interior cells (these kernels' traffic grows with the cells).
 TRAFFIC_PER_CELL = {
-    ("hydro3d", "mixed"): 38.3,   # hydro3d_step<float>: 158.6 + 112.5 MB / 7.08 M cells
-    ("hydro3d", "fp64"): 78.2,    # hydro3d_step<double>: 306.3 + 247.4 MB / 7.08 M cells
-    ("mhd3d", "mixed"): 325.7,    # mhd_update_kernel<float>: 1981.6 + 323.4 MB / 7.08 M cells
-    ("mhd2d", "mixed"): 78.1,     # mhd2d_step_kernel<float>: 186.4 + 141.0 MB / 4.19 M cells
+    ("hydro3d", "mixed"): {"hydro3d_step": 38.3},   # 158.6 + 112.5 MB / 7.08 M cells
+    ("hydro3d", "fp64"): {"hydro3d_step": 78.2},    # 306.3 + 247.4 MB / 7.08 M cells
+    ("mhd3d", "mixed"): {"mhd_dt_kernel": 46.0,      # 323 + 3 MB / 7.08 M cells
+                         "mhd_trace_kernel": 259.5,  # 468 + 1369 MB / 7.08 M cells
+                         "mhd_update_kernel": 325.7},  # 1981.6 + 323.4 MB / 7.08 M cells
+    ("mhd2d", "mixed"): {"mhd2d_step_kernel": 78.1},  # 186.4 + 141.0 MB / 4.19 M cells
 }
 
 # Floating-point operations per cell-update of the reference algorithm
@@ -231,11 +245,12 @@ def e2e_measure(ek, prec, ini, U0, steps):
     return {
         "value": cells * steps / dt / 1e6,
         "unit": UNIT,
+        "steps": steps,
         "h2d_bytes_per_step": int(round(h_in.nbytes / steps)),
         "d2h_bytes_per_step": int(round(h_out.nbytes / steps)) + 8,
         "wall_s": dt,
-        "path": "ek_solver_set_state + next_iteration x K + ek_solver_get_state (pinned host FP64 arrays, "
-                "converted on the device)",
+        "path": "ek_solver_set_state + next_iteration x K + ek_solver_get_state (pinned host FP64 arrays%s)" %
+                (", converted on the device" if prec == ek.EK_PREC_MIXED else ""),
     }, h_out
 
 
@@ -249,7 +264,7 @@ def oracle_rate(ini, U0, nsteps):
     done = len(o.run(nsteps))
     dt = time.perf_counter() - t0
     o.close()
-    return p.nx * p.ny * p.nz * done / dt / 1e6, dt, eko.num_threads()
+    return cells_of(p) * done / dt / 1e6, dt, eko.num_threads()
 
 
 def ensure_oracle():
@@ -260,25 +275,24 @@ def ensure_oracle():
                        stdout=subprocess.DEVNULL)
 
 
-def cpu_sample(args, seconds=12.0):
-    """Oracle on a bounded sample of the headline workload: the same problem on
-    the headline grid when the host can do at least 3 steps of it in about
-    `seconds`, else on a smaller grid, with as many steps as fit."""
-    from euler_kokkos_gb300 import problems as P
-
+def cpu_sample(make, n_full, label, seconds=15.0, probe_n=48, min_n=64):
+    """Oracle on a bounded sample of a workload: make(n, nsteps) -> (ini, U0);
+    the workload's own grid when the host can do at least 3 steps of it in
+    about `seconds`, else a smaller grid of the same problem, with as many
+    steps as fit."""
     ensure_oracle()
-    probe_n = 64
-    ini, U0 = P.blast_3d(n=probe_n, nsteps=2)
+    ini, U0 = make(probe_n, 2)
     r, _, _ = oracle_rate(ini, U0, 2)
-    n = args.n
-    while n > 64 and r * 1e6 * seconds / n ** 3 < 3:
+    n = n_full
+    while n > min_n and r * 1e6 * seconds / n ** 3 < 3:
         n //= 2
     steps = max(3, min(50, int(r * 1e6 * seconds / n ** 3)))
-    ini, U0 = P.blast_3d(n=n, nsteps=steps)
+    ini, U0 = make(n, steps)
     rate, dt, cores = oracle_rate(ini, U0, steps)
     return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "3D blast %d^3, %d steps (oracle/ek_oracle.c, OpenMP, %d threads, %.1f s)" %
-                      (n, steps, cores, dt)}
+            "sample": "%s %d^3%s, %d steps (oracle/ek_oracle.c, FP64, OpenMP, %d threads, %.1f s)" %
+                      (label, n, "" if n == n_full else " (bounded sample of the %d^3 workload)" % n_full,
+                       steps, cores, dt)}
 
 
 def ensemble_workload(ek, P, args, sync, maxt, world, fp32_tflops=None):
@@ -357,17 +371,19 @@ def ensemble_workload(ek, P, args, sync, maxt, world, fp32_tflops=None):
 def run_reference(args):
     """--impl reference: the reference algorithm's CPU restatement (the
     reference's own build cannot be compiled on the GPU host: Kokkos is not
-    available offline), all host threads, same workload and metric."""
+    available offline), all host threads, on the headline workload (3D MHD
+    Orszag-Tang) and metric; each step a bounded sample of that workload."""
     from euler_kokkos_gb300 import problems as P
 
     ensure_oracle()
     n_full = args.n
     # probe the host rate to keep the whole run within a few minutes
-    ini, U0 = P.blast_3d(n=48, nsteps=2)
+    ini, U0 = P.orszag_tang_3d(n=32, nsteps=2)
     r, _, cores = oracle_rate(ini, U0, 2)
-    est = (args.steps + args.warmup) * n_full ** 3 / (r * 1e6)
-    n = n_full if est < 150 else 128
-    ini, U0 = P.blast_3d(n=n, nsteps=args.steps + args.warmup)
+    n = n_full
+    while n > 64 and (args.steps + args.warmup) * n ** 3 / (r * 1e6) > 150:
+        n //= 2
+    ini, U0 = P.orszag_tang_3d(n=n, nsteps=args.steps + args.warmup)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import eko
 
@@ -377,16 +393,17 @@ def run_reference(args):
     t0 = time.perf_counter()
     done = len(o.run(args.steps))
     dt = time.perf_counter() - t0
+    o.close()
     cells = p.nx * p.ny * p.nz
     value = cells * done / dt / 1e6
-    sample = "3D blast %d^3%s, %d timed steps after %d warm-up, FP64" % (
+    sample = "3D MHD Orszag-Tang %d^3%s, %d timed steps after %d warm-up, FP64" % (
         n, "" if n == n_full else " (bounded sample of the %d^3 workload)" % n_full, done, args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": done, "warmup": args.warmup, "ms_per_step": dt * 1e3 / max(done, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded 3D blast)",
-        "config": {"workload": "3D Euler blast %d^3, Hydro_Muscl_3D, HLLC, minmod, CFL 0.7, outflow" % n,
+        "data": "synthetic (seeded 3D MHD Orszag-Tang)",
+        "config": {"workload": HEADLINE % n,
                    "engine": "oracle/ek_oracle.c (CPU restatement of the reference step), OpenMP"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -400,16 +417,20 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=256, help="grid size of the headline workload")
-    ap.add_argument("--mhd-steps", type=int, default=20)
-    ap.add_argument("--no-mhd", action="store_true")
+    ap.add_argument("--n", type=int, default=256, help="grid of the headline (3D MHD Orszag-Tang) and the 3D blast")
+    ap.add_argument("--fp64-steps", type=int, default=20, help="timed steps of the FP64 forms")
+    ap.add_argument("--err-steps", type=int, default=100,
+                    help="steps after which the mixed form is compared with FP64 (the configuration's run length)")
+    ap.add_argument("--side-steps", type=int, default=20, help="timed steps of the mixed side workloads")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-blast", action="store_true")
+    ap.add_argument("--no-implode", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-mhd2d", action="store_true")
     ap.add_argument("--mhd2d-n", type=int, default=4096)
     ap.add_argument("--no-mhd-blast", action="store_true")
     ap.add_argument("--mhd-blast-n", type=int, default=256,
-                    help="grid of the low-beta MHD blast (512 = the configured grid; its FP64 run takes ~50 s)")
+                    help="grid of the low-beta MHD blast (512 = the configured grid; its FP64 run takes ~1 min)")
     ap.add_argument("--mhd-blast-steps", type=int, default=30)
     ap.add_argument("--ens-n", type=int, default=512)
     ap.add_argument("--ens-steps", type=int, default=200)
@@ -432,6 +453,7 @@ def main():
     rep = Replicas()
     world = rep.world
     barrier = rep.barrier
+    maxt = rep.max
 
     def sync():
         torch.cuda.synchronize()
@@ -447,35 +469,8 @@ def main():
     # denominators of the FLOP roofline
     fma_peak = {"mixed": ek.measure_fma_rate(ek.EK_PREC_MIXED), "fp64": ek.measure_fma_rate(ek.EK_PREC_FP64)}
 
-    ini, U0 = P.blast_3d(n=args.n, nsteps=10 ** 6)
-    with ClockSampler(local) as clk:
-        mixed = measure_workload(ek, "hydro3d", ek.EK_PREC_MIXED, ini, U0, args.steps, args.warmup, sync)
-    clocks = clk.summary()
-    fp64 = measure_workload(ek, "hydro3d", ek.EK_PREC_FP64, ini, U0, args.steps, args.warmup, sync)
-
-    maxt = rep.max
-
-    ms_mixed, ms_fp64 = maxt(mixed["ms"]), maxt(fp64["ms"])
-    cells = mixed["cells"]
-    value = cells * mixed["steps"] / (ms_mixed / 1e3) / 1e6 * world
-    v64 = cells * fp64["steps"] / (ms_fp64 / 1e3) / 1e6 * world
-
-    # accuracy of the mixed form against the FP64 drop-in after the same steps
-    gw = 2
-    a = mixed["U"][0, gw:-gw, gw:-gw, gw:-gw]
-    b = fp64["U"][0, gw:-gw, gw:-gw, gw:-gw]
-    l1 = float(np.abs(a - b).sum() / np.abs(b).sum())
-    linf = float(np.abs(a - b).max() / np.abs(b).max())
-
-    def roofline(meas, key):
-        kms, kn = meas["kernels"][0]
-        achieved = BYTES_PER_CELL[key] * meas["cells"] / (kms / 1e3) / 1e9 if kms else None
-        return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm if achieved else None,
-                "traffic": TRAFFIC_PER_CELL[key] * meas["cells"] if key in TRAFFIC_PER_CELL else None,
-                "kernel_ms": kms, "peak_source": peak_kind,
-                "algorithmic_bytes_per_cell": BYTES_PER_CELL[key],
-                **flop_roofline(meas, key)}
+    def rate(meas):
+        return meas["cells"] * meas["steps"] / (maxt(meas["ms"]) / 1e3) / 1e6 * world
 
     def flop_roofline(meas, key):
         """The step against both ceilings: HBM (algorithmic bytes at the measured
@@ -484,44 +479,142 @@ def main():
         fl = FLOPS_PER_CELL.get(key[0])
         if not fl or not meas["ms"]:
             return {}
-        rate = meas["cells"] * meas["steps"] / (meas["ms"] / 1e3)  # cell-updates/s
+        r = meas["cells"] * meas["steps"] / (meas["ms"] / 1e3)  # cell-updates/s
         peak = fma_peak[key[1]]
         bound_hbm = hbm * 1e9 / BYTES_PER_CELL[key]
         bound_flop = peak * 1e12 / fl["flops"]
         return {"flop": {"per_cell": fl["flops"], "other_fp_ops_per_cell": fl["other"],
-                         "counted_on": fl["counted_on"], "achieved_tflops": fl["flops"] * rate / 1e12,
-                         "peak_tflops": peak, "frac": fl["flops"] * rate / 1e12 / peak,
+                         "counted_on": fl["counted_on"], "achieved_tflops": fl["flops"] * r / 1e12,
+                         "peak_tflops": peak, "frac": fl["flops"] * r / 1e12 / peak,
                          "peak_source": "CUDA-core FMA rate measured in this run (%s)" %
                                         ("FP64" if key[1] == "fp64" else "FP32")},
                 "bound_gcell_s": {"hbm": bound_hbm / 1e9, "flop": bound_flop / 1e9},
-                "frac_of_min_bound": rate / min(bound_hbm, bound_flop)}
+                "frac_of_min_bound": r / min(bound_hbm, bound_flop)}
+
+    def roofline(meas, key):
+        """HBM roofline of the whole step (every launch of the step) and, beside
+        it, of each kernel: achieved = algorithmic bytes per cell-update x cells
+        / device time (CUDA events on the solver's stream); traffic = ncu DRAM
+        bytes per cell (profiles/) x cells, per step."""
+        cells = meas["cells"]
+        ms_step = meas["ms"] / meas["steps"]
+        algo = BYTES_PER_CELL[key]
+        achieved = algo * cells / (ms_step / 1e3) / 1e9
+        names = KERNEL_NAMES[key[0]]
+        tr = TRAFFIC_PER_CELL.get(key, {})
+        kernels = {}
+        ktot = sum(v[0] for v in meas["kernels"].values() if v[0])
+        for i, name in names:
+            kms, kn = meas["kernels"].get(i, (None, 0))
+            if not kms:
+                continue
+            kernels[name] = {"ms_per_launch": kms, "launches_per_step": kn / meas["steps"],
+                             "share": kms / ktot if ktot else None,
+                             "traffic_per_cell": tr.get(name)}
+        dom = max(kernels, key=lambda k: kernels[k]["ms_per_launch"]) if kernels else None
+        out = {"bound": "hbm", "scope": "whole step (%d launch%s per step)" %
+                                        (len(names), "" if len(names) == 1 else "es"),
+               "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+               "traffic": sum(tr.values()) * cells if tr and all(n in tr for _, n in names) else None,
+               "traffic_per_cell": sum(tr.values()) if tr else None,
+               "algorithmic_bytes_per_cell": algo, "ms_per_step": ms_step, "peak_source": peak_kind,
+               "kernels": kernels}
+        if dom:
+            kms = kernels[dom]["ms_per_launch"]
+            ach = algo * cells / (kms / 1e3) / 1e9
+            out["dominant_kernel"] = {"name": dom, "achieved": ach, "frac": ach / hbm, "kernel_ms": kms,
+                                      "traffic": tr[dom] * cells if dom in tr else None}
+        out.update(flop_roofline(meas, key))
+        return out
+
+    # --- headline: 3D MHD Orszag-Tang, mixed FP32 vs the FP64 drop-in -------
+    n = args.n
+    ini, U0 = P.orszag_tang_3d(n=n, nsteps=10 ** 6)
+    with ClockSampler(local) as clk:
+        mixed = measure_workload(ek, "mhd3d", ek.EK_PREC_MIXED, ini, U0, args.steps, args.warmup, sync)
+    clocks = clk.summary()
+    mixed.pop("U")
+    fp64 = measure_workload(ek, "mhd3d", ek.EK_PREC_FP64, ini, U0, args.fp64_steps, args.warmup, sync)
+    fp64.pop("U")
+    value, v64 = rate(mixed), rate(fp64)
+    ms_mixed = maxt(mixed["ms"])
+
+    # accuracy after the configuration's run length: both forms from U0
+    gw = 3
+    runs = {}
+    for name, prec in (("mixed", ek.EK_PREC_MIXED), ("fp64", ek.EK_PREC_FP64)):
+        with ek.Solver(ek.params_from_ini(ini, precision=prec)) as s:
+            s.set_state(U0)
+            s.run(args.err_steps)
+            Uf = s.get_state()
+            runs[name] = (Uf[:, gw:-gw, gw:-gw, gw:-gw].copy(), s.dt_history(), s.totals())
+            del Uf
+    (am, dm, tm), (af, df, tf) = runs["mixed"], runs["fp64"]
+    nerr = min(len(dm), len(df))
+
+    def l1(v):
+        return float(np.abs(am[v] - af[v]).sum() / np.abs(af[v]).sum())
+
+    def linf(v):
+        return float(np.abs(am[v] - af[v]).max() / np.abs(af[v]).max())
+
+    accuracy = {
+        "after_steps": nerr,
+        "l1_rel_err_mixed_vs_fp64": {"rho": l1(0), "E": l1(1), "Bx": l1(5), "By": l1(6), "Bz": l1(7)},
+        "linf_rel_err_mixed_vs_fp64": {"rho": linf(0), "E": linf(1), "Bx": linf(5), "By": linf(6), "Bz": linf(7)},
+        "max_rel_dt_diff": float(np.abs(dm[:nerr] / df[:nerr] - 1).max()),
+        "max_divB": {"mixed": float(tm[2]), "fp64": float(tf[2])},
+        "target": "L1 rho <= 1e-5 relative; div B at FP64 round-off",
+    }
+    del runs, am, af
 
     workloads = {}
-    if not args.no_mhd:
-        ini_m, U0_m = P.orszag_tang_3d(n=args.n, nsteps=10 ** 6)
-        mm = measure_workload(ek, "mhd3d", ek.EK_PREC_MIXED, ini_m, U0_m, args.mhd_steps, 3, sync)
-        m64 = measure_workload(ek, "mhd3d", ek.EK_PREC_FP64, ini_m, U0_m, max(2, args.mhd_steps // 4), 3, sync)
-        gwm = 3
-        am = mm["U"][0, gwm:-gwm, gwm:-gwm, gwm:-gwm]
-        # error after the same number of steps
-        with ek.Solver(ek.params_from_ini(ini_m, precision=ek.EK_PREC_FP64)) as s64:
-            s64.set_state(U0_m)
-            s64.run(mm["iteration"])
-            bm = s64.get_state()[0, gwm:-gwm, gwm:-gwm, gwm:-gwm]
-        vm = mm["cells"] * mm["steps"] / (maxt(mm["ms"]) / 1e3) / 1e6 * world
-        vm64 = m64["cells"] * m64["steps"] / (maxt(m64["ms"]) / 1e3) / 1e6 * world
-        kt = {name: mm["kernels"][i][0] for i, name in ((0, "update"), (1, "trace"), (2, "cfl"))}
-        workloads["mhd_orszag_tang_%d" % args.n] = {
-            "value_mixed": vm, "value_fp64": vm64, "unit": UNIT, "mixed_over_fp64": vm / vm64,
-            "ms_per_step_mixed": mm["ms"] / mm["steps"], "ms_per_step_fp64": m64["ms"] / m64["steps"],
-            "l1_rel_err_rho_mixed_vs_fp64": float(np.abs(am - bm).sum() / np.abs(bm).sum()),
-            "max_divB_mixed": float(mm["totals"][2]), "max_divB_fp64": float(m64["totals"][2]),
-            "kernel_ms_mixed": kt,
-            "roofline_mixed": roofline(mm, ("mhd3d", "mixed")),
-            "roofline_fp64": roofline(m64, ("mhd3d", "fp64")),
-            "config": "MHD_Muscl_3D Orszag-Tang %d^3, HLLD + CT, slope_type 2, CFL 0.8, periodic" % args.n,
-        }
 
+    # --- 3D hydro blast (C2) --------------------------------------------------
+    if not args.no_blast:
+        ini_b, U0_b = P.blast_3d(n=n, nsteps=10 ** 6)
+        bm = measure_workload(ek, "hydro3d", ek.EK_PREC_MIXED, ini_b, U0_b, args.side_steps, 3, sync)
+        b64 = measure_workload(ek, "hydro3d", ek.EK_PREC_FP64, ini_b, U0_b, args.fp64_steps, 3, sync)
+        with ek.Solver(ek.params_from_ini(ini_b, precision=ek.EK_PREC_FP64)) as s64:
+            s64.set_state(U0_b)
+            s64.run(bm["iteration"])
+            bb = s64.get_state()[0, 2:-2, 2:-2, 2:-2]
+        ab = bm["U"][0, 2:-2, 2:-2, 2:-2]
+        vb, vb64 = rate(bm), rate(b64)
+        e2e_b64 = e2e_measure(ek, ek.EK_PREC_FP64, ini_b, U0_b, args.fp64_steps)[0] if rank == 0 else None
+        workloads["hydro_blast_%d" % n] = {
+            "value_mixed": vb, "value_fp64": vb64, "unit": UNIT, "mixed_over_fp64": vb / vb64,
+            "ms_per_step_mixed": bm["ms"] / bm["steps"], "ms_per_step_fp64": b64["ms"] / b64["steps"],
+            "l1_rel_err_rho_mixed_vs_fp64": float(np.abs(ab - bb).sum() / np.abs(bb).sum()),
+            "error_after_steps": bm["iteration"],
+            "roofline_mixed": roofline(bm, ("hydro3d", "mixed")),
+            "roofline_fp64": roofline(b64, ("hydro3d", "fp64")),
+            "e2e_fp64": e2e_b64,
+            "config": "Hydro_Muscl_3D blast %d^3, HLLC, minmod, CFL 0.7, outflow, 1%% density noise" % n,
+        }
+        del bm, b64, ab, bb, U0_b
+
+    # --- 2D implode FP64 (C1) -------------------------------------------------
+    if not args.no_implode:
+        ini_i, U0_i = P.implode_2d(n=256, nsteps=100)
+        im = measure_workload(ek, "hydro2d", ek.EK_PREC_FP64, ini_i, U0_i, 100, 3, sync)
+        vi = rate(im)
+        e2e_i = e2e_measure(ek, ek.EK_PREC_FP64, ini_i, U0_i, 100)[0] if rank == 0 else None
+        cpu_i = None
+        if rank == 0 and not args.no_cpu:
+            ensure_oracle()
+            ri, dti, cores = oracle_rate(ini_i, U0_i, 100)
+            cpu_i = {"value": ri, "unit": UNIT, "cores": cores, "kind": "port",
+                     "sample": "the whole configuration: 2D implode 256^2, 100 steps (%.2f s)" % dti}
+        workloads["hydro_implode2d_256"] = {
+            "value_fp64": vi, "unit": UNIT, "steps": im["steps"], "ms_per_step_fp64": im["ms"] / im["steps"],
+            "roofline_fp64": roofline(im, ("hydro2d", "fp64")),
+            "e2e_fp64": e2e_i, "cpu_baseline": cpu_i,
+            "config": "Hydro_Muscl_2D implode 256^2, HLLC, minmod, CFL 0.8, reflecting walls, 100 steps, FP64",
+        }
+        del im
+
+    # --- 3D MHD low-beta blast (C5) -------------------------------------------
     if not args.no_mhd_blast:
         # low-beta MHD blast with a small transverse field (the configured field
         # along x alone makes the reference's HLLD divide 0/0 in the first
@@ -529,9 +622,9 @@ def main():
         # configured steps for the error and div B
         nb = args.mhd_blast_n
         ini_b, U0_b = P.mhd_blast_3d(n=nb, nsteps=10 ** 6, by_ratio=0.1)
-        mb = measure_workload(ek, "mhd3d", ek.EK_PREC_MIXED, ini_b, U0_b, args.mhd_steps, 3, sync)
-        mb64 = measure_workload(ek, "mhd3d", ek.EK_PREC_FP64, ini_b, U0_b, max(2, args.mhd_steps // 4), 3, sync,
-                                profile=False)
+        mb = measure_workload(ek, "mhd3d", ek.EK_PREC_MIXED, ini_b, U0_b, args.side_steps, 3, sync)
+        mb64 = measure_workload(ek, "mhd3d", ek.EK_PREC_FP64, ini_b, U0_b, max(5, args.fp64_steps // 4), 3,
+                                sync, profile=False)
         mb.pop("U"), mb64.pop("U")
         res, inner = {}, {}
         pb = ek.params_from_ini(ini_b)
@@ -548,8 +641,7 @@ def main():
         l1b = [float(np.abs(ab[v] - bb[v]).sum() / np.abs(bb[v]).sum()) for v in (0, 1)]
         linfb = [float(np.abs(ab[v] - bb[v]).max() / np.abs(bb[v]).max()) for v in (0, 1)]
         del res, ab, bb, U0_b
-        vb = mb["cells"] * mb["steps"] / (maxt(mb["ms"]) / 1e3) / 1e6 * world
-        vb64 = mb64["cells"] * mb64["steps"] / (maxt(mb64["ms"]) / 1e3) / 1e6 * world
+        vb, vb64 = rate(mb), rate(mb64)
         workloads["mhd_blast_lowbeta_%d" % nb] = {
             "value_mixed": vb, "value_fp64": vb64, "unit": UNIT, "mixed_over_fp64": vb / vb64,
             "ms_per_step_mixed": mb["ms"] / mb["steps"], "ms_per_step_fp64": mb64["ms"] / mb64["steps"],
@@ -570,21 +662,19 @@ def main():
     if not args.no_mhd2d:
         n2 = args.mhd2d_n
         ini_2, U0_2 = P.orszag_tang_2d(n=n2, nsteps=10 ** 6)
-        m2 = measure_workload(ek, "mhd2d", ek.EK_PREC_MIXED, ini_2, U0_2, args.mhd_steps, 3, sync)
-        m264 = measure_workload(ek, "mhd2d", ek.EK_PREC_FP64, ini_2, U0_2, max(2, args.mhd_steps // 4), 3, sync)
+        m2 = measure_workload(ek, "mhd2d", ek.EK_PREC_MIXED, ini_2, U0_2, args.side_steps, 3, sync)
+        m264 = measure_workload(ek, "mhd2d", ek.EK_PREC_FP64, ini_2, U0_2, max(5, args.fp64_steps // 4), 3, sync)
         a2 = m2["U"][0, 0, 3:-3, 3:-3]
         with ek.Solver(ek.params_from_ini(ini_2, precision=ek.EK_PREC_FP64)) as s64:
             s64.set_state(U0_2)
             s64.run(m2["iteration"])
             b2 = s64.get_state()[0, 0, 3:-3, 3:-3]
-        v2 = m2["cells"] * m2["steps"] / (maxt(m2["ms"]) / 1e3) / 1e6 * world
-        v264 = m264["cells"] * m264["steps"] / (maxt(m264["ms"]) / 1e3) / 1e6 * world
+        v2, v264 = rate(m2), rate(m264)
         workloads["mhd2d_orszag_tang_%d" % n2] = {
             "value_mixed": v2, "value_fp64": v264, "unit": UNIT, "mixed_over_fp64": v2 / v264,
             "ms_per_step_mixed": m2["ms"] / m2["steps"], "ms_per_step_fp64": m264["ms"] / m264["steps"],
             "l1_rel_err_rho_mixed_vs_fp64": float(np.abs(a2 - b2).sum() / np.abs(b2).sum()),
             "max_divB_mixed": float(m2["totals"][2]), "max_divB_fp64": float(m264["totals"][2]),
-            "kernel_ms_mixed": {name: m2["kernels"][i][0] for i, name in ((0, "step"), (2, "cfl"))},
             "roofline_mixed": roofline(m2, ("mhd2d", "mixed")),
             "roofline_fp64": roofline(m264, ("mhd2d", "fp64")),
             "config": "MHD_Muscl_2D Orszag-Tang %d^2, HLLD + CT, slope_type 2, CFL 0.8, periodic" % n2,
@@ -596,7 +686,11 @@ def main():
     line = None
     if rank == 0:
         e2e, _ = e2e_measure(ek, ek.EK_PREC_MIXED, ini, U0, args.steps)
-        cpu = None if args.no_cpu else cpu_sample(args)
+        e2e64, _ = e2e_measure(ek, ek.EK_PREC_FP64, ini, U0, args.fp64_steps)
+        cpu = None
+        if not args.no_cpu:
+            cpu = cpu_sample(lambda m, k: P.orszag_tang_3d(n=m, nsteps=k), n, "3D MHD Orszag-Tang",
+                             probe_n=32)
         launches = mixed["launches"]
         line = {
             "metric": METRIC,
@@ -610,25 +704,26 @@ def main():
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": "f32",
-            "data": "synthetic: seeded 3D blast (rho 1 + 1% splitmix noise, p 0.1 / 10 sphere r 0.1)",
+            "data": "synthetic: seeded 3D MHD Orszag-Tang (rho 25/(36 pi), p 5/(12 pi), v = (-sin 2 pi y, "
+                    "sin 2 pi x, 1e-3 splitmix noise), face B from A_z)",
             "config": {
-                "workload": "3D Euler blast %d^3 on [0,1]^3, Hydro_Muscl_3D, HLLC, minmod, CFL 0.7, outflow; "
-                            "mixed FP32 (FP64 dt, totals, cancellation islands)" % args.n,
-                "grid": [args.n] * 3,
-                "l2_policy": "no flush: the FP32 state (%.0f MB) is larger than the 129 MB L2" %
-                             (5 * 4 * mixed["ghost_cells"] / 1e6),
+                "workload": (HEADLINE % n) + "; mixed FP32 (FP64 face B and CT update, dt, totals, "
+                                             "cancellation islands)",
+                "grid": [n] * 3,
+                "l2_policy": "no flush: the mixed state (%.0f MB) is larger than the 129 MB L2" %
+                             ((5 * 4 + 3 * 8) * mixed["ghost_cells"] / 1e6),
                 "parallelism": "replicas" if world > 1 else "single GPU",
-                "kernel": "hydro3d_step<float> (fused: ghost map, primitives, slopes, trace, HLLC, update, next-dt)",
+                "kernels": [k for _, k in KERNEL_NAMES["mhd3d"]],
             },
             "fp64": {
-                "value": v64, "unit": UNIT, "ms_per_step": ms_fp64 / fp64["steps"],
-                "roofline": roofline(fp64, ("hydro3d", "fp64")),
+                "value": v64, "unit": UNIT, "steps": fp64["steps"], "ms_per_step": maxt(fp64["ms"]) / fp64["steps"],
+                "roofline": roofline(fp64, ("mhd3d", "fp64")),
+                "e2e": e2e64,
                 "note": "FP64 drop-in (FMA contraction); FP64 FMA rate of this GPU: %.2f TFLOP/s" % fma_peak["fp64"],
             },
             "mixed_over_fp64": value / v64,
-            "l1_rel_err_rho_mixed_vs_fp64": l1,
-            "linf_rel_err_rho_mixed_vs_fp64": linf,
-            "roofline": roofline(mixed, ("hydro3d", "mixed")),
+            "accuracy": accuracy,
+            "roofline": roofline(mixed, ("mhd3d", "mixed")),
             "reference_formula_mcell_s": mixed["ghost_cells"] * mixed["steps"] / (ms_mixed / 1e3) / 1e6 * world,
             "cpu_baseline": cpu,
             "e2e": e2e,

@@ -3,6 +3,16 @@
 * 2D implode 256^2, 100 steps, FP64: the exact build equals the oracle bit for
   bit (state and dt sequence); the FMA build is within the drop-in tolerances
   (dt 1e-13, fields 1e-11 relative L-infinity).
+* FP64 drop-in against the oracle (the reference algorithm's CPU restatement,
+  OpenMP on the host cores) from the same injected state, at the 3D configs'
+  full sizes: the exact build equals the oracle bit for bit after 5 steps
+  (16-plane z-chunk seams through the whole depth); the FMA build's dt
+  sequence is within 1e-13 relative and density, energy (and for MHD the face
+  fields) within 1e-11 relative L-infinity after the run:
+  - 3D blast 256^3, 50 steps;
+  - 3D MHD Orszag-Tang 256^3, OT_STEPS steps (the config's 100 by default;
+    EK_FULLSIZE_OT_STEPS lowers it where the host cores are slow: the oracle
+    runs this case at a few Mcell-updates/s).
 * 3D blast 256^3, 50 steps: the mixed form is within 1e-5 relative L1 of the
   FP64 drop-in in density and energy; mass is conserved in both forms while
   the blast is inside the box (outflow boundaries, nothing has left).
@@ -13,6 +23,8 @@
   their single-solver runs bit for bit (state and dt sequence).
 """
 
+import os
+
 import numpy as np
 import pytest
 
@@ -22,6 +34,54 @@ from euler_kokkos_gb300 import problems as P
 from helpers import interior, rel_l1, rel_linf
 
 pytestmark = pytest.mark.gpu
+
+OT_STEPS = int(os.environ.get("EK_FULLSIZE_OT_STEPS", "100"))
+EXACT_STEPS = 5
+FP64_DT_TOL, FP64_FIELD_TOL = 1e-13, 1e-11
+
+
+def _oracle_snapshots(ini, U0, nsteps):
+    """Oracle state and dt sequence after EXACT_STEPS and after nsteps steps."""
+    o = eko.Oracle(eko.params_from_ini(ini), U0)
+    try:
+        d5 = o.run(EXACT_STEPS)
+        U5 = o.state()
+        dn = o.run(nsteps - EXACT_STEPS)
+        return {"U5": U5, "dts5": np.asarray(d5), "U": o.state(),
+                "dts": np.concatenate([np.asarray(d5), np.asarray(dn)])}
+    finally:
+        o.close()
+
+
+@pytest.fixture(scope="module")
+def blast_256():
+    ini, U0 = P.blast_3d(n=256, nsteps=50)
+    return ini, U0, _oracle_snapshots(ini, U0, 50)
+
+
+@pytest.fixture(scope="module")
+def orszag_tang_256():
+    ini, U0 = P.orszag_tang_3d(n=256, nsteps=OT_STEPS)
+    return ini, U0, _oracle_snapshots(ini, U0, OT_STEPS)
+
+
+def _check_fp64_drop_in(ini, U0, ref, nsteps, gw, nvar_checked):
+    # exact build: bitwise after EXACT_STEPS steps
+    Ue, de, _, _, n = _run(ini, U0, EXACT_STEPS, exact_fp=1)
+    assert n == EXACT_STEPS
+    assert np.array_equal(de, ref["dts5"])
+    assert np.array_equal(interior(Ue, gw, 3), interior(ref["U5"], gw, 3))
+    del Ue
+    # FMA build: the drop-in tolerances after the whole run
+    Uf, df, _, _, n = _run(ini, U0, nsteps)
+    assert n == nsteps
+    dt_err = np.abs(df / ref["dts"] - 1).max()
+    assert dt_err <= FP64_DT_TOL, dt_err
+    err = rel_linf(interior(Uf, gw, 3), interior(ref["U"], gw, 3))
+    print("fp64 vs oracle: %d steps, dt rel err %.3g, rel Linf per variable %s" % (nsteps, dt_err, err))
+    # density (0), energy (1), and the face fields (5-7) for MHD
+    checked = [0, 1] + list(range(5, nvar_checked))
+    assert err[checked].max() <= FP64_FIELD_TOL, err
 
 
 def _run(ini, U0, nsteps, **over):
@@ -46,6 +106,16 @@ def test_implode_256_fp64_matches_oracle():
     Uf, df, _, _, _ = _run(ini, U0, 100)
     assert np.abs(df / do - 1).max() <= 1e-13
     assert rel_linf(interior(Uf, 2, 2), interior(Uo, 2, 2)).max() <= 1e-11
+
+
+def test_blast_256_fp64_matches_oracle(blast_256):
+    ini, U0, ref = blast_256
+    _check_fp64_drop_in(ini, U0, ref, 50, 2, 5)
+
+
+def test_orszag_tang_256_fp64_matches_oracle(orszag_tang_256):
+    ini, U0, ref = orszag_tang_256
+    _check_fp64_drop_in(ini, U0, ref, OT_STEPS, 3, 8)
 
 
 def test_blast_256_mixed_vs_fp64():
