@@ -19,8 +19,9 @@
 // State files use the EKST layout (little endian): char magic[8]="EKSTATE1";
 // int64 dim, nbvar, isize, jsize, ksize, ghost, iteration, ndt; double t;
 // double dt[ndt]; double U[isize*jsize*ksize*nbvar] with i fastest, then j,
-// k, var.  With [output] vtk_enabled the final state is also written as the
-// reference's VTK file (save_solution).
+// k, var.  With [run] nOutput != 0 the solution is saved as main.cpp does
+// (first and last state, and whenever should_save_solution() says so; VTK
+// files of the reference's format when [output] vtk_enabled).
 #include <chrono>
 #include <cstdint>
 #include <cstdio>
@@ -28,7 +29,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/ek_gb300.h"
+#include "../../include/ek/solver.hpp"
 
 namespace
 {
@@ -106,71 +107,53 @@ main(int argc, char ** argv)
     }
   }
 
-  ek_solver * s = nullptr;
-  if (ek_solver_create(&p, &s) != EK_OK)
-    return fail("solver");
-  if (ek_solver_set_state(s, U.data(), EK_LAYOUT_LEFT) != EK_OK)
-    return fail("set_state");
-
+  // the reference's loop through the SolverBase-shaped interface (ek/solver.hpp)
   std::vector<double> dts;
-  int                 finished = 0;
-  const int           nlog = p.nlog > 0 ? p.nlog : 1;
-  std::printf("Start computation....\n");
-  const auto t_start = std::chrono::steady_clock::now();
-  double     t_io = 0.0;
-  for (long k = 0; k < nsteps; ++k)
+  double              t = 0.0, t_io = 0.0, t_tot = 0.0;
+  int                 it = 0;
+  try
   {
-    if (ek_solver_finished(s, &finished) != EK_OK)
-      return fail("finished");
-    if (finished)
-      break;
+    ek::Solver s(p);
+    s.set_state(U.data(), EK_LAYOUT_LEFT);
+    if (p.nOutput != 0)
+      s.save_solution(); // main.cpp:118-119
+    std::printf("Start computation....\n");
+    const auto t_start = std::chrono::steady_clock::now();
+    for (long k = 0; k < nsteps && !s.finished(); ++k)
     {
-      // next_iteration_impl's log line: iteration, dt and t before the step
-      double t0, dt0;
-      int    it0;
-      if (ek_solver_time(s, &t0, &dt0, &it0) != EK_OK)
-        return fail("time");
-      if (it0 % nlog == 0)
-        std::printf("time step=%7d (dt=% 10.8f t=% 10.8f)\n", it0, dt0, t0);
+      s.next_iteration(); // step log line, one fused step, ++m_iteration, m_t += m_dt
+      dts.push_back(s.m_dt);
     }
-    const ek_status st = ek_solver_next_iteration(s);
-    double          t, dt;
-    int             it;
-    ek_solver_time(s, &t, &dt, &it);
-    dts.push_back(dt);
-    if (st == EK_ERR_NONFINITE)
-      continue; // the reference keeps stepping on a non-finite dt
-    if (st != EK_OK)
-      return fail("next_iteration");
-  }
+    s.get_state(U.data(), EK_LAYOUT_LEFT);
+    if (p.nOutput != 0)
+    {
+      // the last state (main.cpp:140-142)
+      const auto t_io0 = std::chrono::steady_clock::now();
+      s.save_solution();
+      t_io = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_io0).count();
+    }
+    t_tot = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    t = s.m_t;
+    it = s.m_iteration;
 
-  double t, dt;
-  int    it;
-  if (ek_solver_time(s, &t, &dt, &it) != EK_OK || ek_solver_get_state(s, U.data(), EK_LAYOUT_LEFT) != EK_OK)
-    return fail("final state");
-  if (p.vtk_enabled)
+    // main.cpp:150-153 and print_solver_monitoring_info (solver_utils.h:15-55)
+    std::printf("final time is %f\n", t);
+    const double t_god = t_tot - t_io;
+    std::printf("total        time : %5.3f secondes\n", t_tot);
+    std::printf("godunov      time : %5.3f secondes %5.2f%%\n", t_god, 100 * t_god / t_tot);
+    std::printf("compute dt   time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
+    std::printf("boundaries   time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
+    std::printf("comp. prim.  time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
+    std::printf("comp. flux   time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
+    std::printf("hydro update time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
+    std::printf("io           time : %5.3f secondes %5.2f%%\n", t_io, 100 * t_io / t_tot);
+    std::printf("Perf              : %5.3f number of Mcell-updates/s\n", it * (double)s.m_nCells / t_tot * 1e-6);
+  }
+  catch (const ek::Error & e)
   {
-    const auto t_io0 = std::chrono::steady_clock::now();
-    if (ek_solver_save_vtk(s, 0, "") != EK_OK)
-      return fail("save_vtk");
-    t_io = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_io0).count();
+    std::fprintf(stderr, "ek_main: %s\n", e.what());
+    return 1;
   }
-  ek_solver_destroy(s);
-  const double t_tot = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-
-  // main.cpp:150-153 and print_solver_monitoring_info (solver_utils.h:15-55)
-  std::printf("final time is %f\n", t);
-  const double t_god = t_tot - t_io;
-  const double ncells = (double)p.isize * p.jsize * (p.dim == 3 ? p.ksize : 1);
-  std::printf("total        time : %5.3f secondes\n", t_tot);
-  std::printf("godunov      time : %5.3f secondes %5.2f%%\n", t_god, 100 * t_god / t_tot);
-  std::printf("compute dt   time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
-  std::printf("boundaries   time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
-  std::printf("comp. prim.  time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
-  std::printf("comp. flux   time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
-  std::printf("hydro update time : %5.3f secondes %5.2f%%\n", 0.0, 0.0);
-  std::printf("io           time : %5.3f secondes %5.2f%%\n", t_io, 100 * t_io / t_tot);
-  std::printf("Perf              : %5.3f number of Mcell-updates/s\n", it * ncells / t_tot * 1e-6);
 
   FILE * f = std::fopen(argv[3], "wb");
   if (!f)

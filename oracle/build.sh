@@ -14,4 +14,6 @@ ${CXX:-g++} -std=gnu++20 -O2 -ffp-contract=off -fPIC -shared -fpermissive -Wno-u
 # the reference harness: only where EK_REFERENCE names the reference's source tree
 if [ -n "${EK_REFERENCE:-}" ] && [ -d "${EK_REFERENCE}/src" ] && [ "${EK_SKIP_REF:-0}" = "0" ]; then
   make -s -C "$here" -f Makefile.ref REF="${EK_REFERENCE}" all
+  # where the harness came from, for the tests that build more of the reference
+  printf '%s\n' "${EK_REFERENCE}" > "$here/_ref/reference_path"
 fi

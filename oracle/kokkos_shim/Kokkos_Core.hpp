@@ -182,6 +182,7 @@ public:
   using value_type = typename info::value_type;
   using non_const_value_type = typename std::remove_const<value_type>::type;
   using layout_type = typename shim_detail::LayoutOf<Props...>::type;
+  using array_layout = layout_type;
   static constexpr int rank = info::n_dyn + info::n_static;
   using host_mirror_type = View<DataType, layout_type, HostSpace>;
   using HostMirror = host_mirror_type;
