@@ -72,6 +72,8 @@ struct ek_solver
   double                   kernel_ms[3] = { 0, 0, 0 };
   long long                kernel_n[3] = { 0, 0, 0 };
   bool                     owns = true; // false: a view into an ensemble's buffers
+  // 3D MHD: the step whose CFL the last update kernel computed (-1: none)
+  int                      cfl_step = -1;
 };
 
 static cudaEvent_t
@@ -506,6 +508,7 @@ reset_clock(ek_solver * s, double t0)
   h.error = 0;
   h.dtlog = s->dtlog;
   h.dtcap = s->dtcap;
+  s->cfl_step = -1;
   EK_CUDA(cudaMemcpyAsync(s->clk, &h, sizeof h, cudaMemcpyHostToDevice, s->stream), "clock reset");
   // hydro: slot 0 holds the CFL of the initial state (the constructor's
   // compute_dt()); MHD recomputes dt inside every step
@@ -757,8 +760,8 @@ launch_one(ek_solver * s, int kernel_id, int phase, int step)
     e = s->exact ? ek_exact::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, s->stream)
                  : ek_fast::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, s->stream);
   else if (s->p.mhd)
-    e = s->exact ? ek_exact::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream)
-                 : ek_fast::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream);
+    e = s->exact ? ek_exact::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, true, s->stream)
+                 : ek_fast::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, true, s->stream);
   else
   {
     const CUtensorMap * tm = s->has_tmap ? &s->tmap[step % 2] : nullptr;
@@ -789,11 +792,16 @@ launch_step(ek_solver * s, int step)
       st = launch_one(s, 0, 1, step); // trace, fluxes, emf, update
     return st;
   }
-  ek_status st = launch_one(s, 2, 0, step); // CFL of the step
+  // CFL of the step: only when no update kernel computed it (the first step
+  // after the state was set)
+  ek_status st = EK_OK;
+  if (s->cfl_step != step)
+    st = launch_one(s, 2, 0, step);
   if (st == EK_OK)
     st = launch_one(s, 1, 1, step); // trace
   if (st == EK_OK)
-    st = launch_one(s, 0, 2, step); // fluxes, emfs, update
+    st = launch_one(s, 0, 2, step); // fluxes, emfs, update, and the next step's CFL
+  s->cfl_step = st == EK_OK ? step + 1 : -1;
   return st;
 }
 

@@ -22,9 +22,10 @@
                        unsigned long long * key, DevClock * fin, int fin_step, cudaStream_t st);    \
   cudaError_t mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key,         \
                      cudaStream_t st);                                                              \
-  /* one MHD step = phase 0 (CFL), 1 (trace), 2 (fluxes, emfs, update) */                         \
+  /* one MHD step = phase 0 (CFL), 1 (trace), 2 (fluxes, emfs, update; cfl_next: and the     */ \
+  /* CFL of the updated state, the next step's dt, so its phase 0 is not needed) */               \
   cudaError_t mhd_step(int prec, int phase, const void * Uin, void * Uout, void * work,             \
-                       const KParams & P, DevClock * clk, int step, cudaStream_t st);               \
+                       const KParams & P, DevClock * clk, int step, bool cfl_next, cudaStream_t st); \
   size_t      mhd_work_bytes(int prec, const KParams & P);                                          \
   /* one MHD 2D step = phase 0 (CFL), 1 (fused trace, fluxes, emf, update) */                      \
   cudaError_t mhd2d_step(int prec, int phase, const void * Uin, void * Uout, const KParams & P,     \

@@ -1,16 +1,23 @@
 // CT-MHD 3D step (SolverMHDMuscl<3>::godunov_unsplit_impl v0,
-// SolverMHDMuscl.cpp:461-505) in three launches:
+// SolverMHDMuscl.cpp:461-505) in two launches, plus the CFL kernel before
+// the first step:
 //   1. mhd_dt_kernel     primitive variables of the boundary-mapped state and
 //                        the CFL max-reduction (ComputeDtFunctor3D_MHD); the
 //                        reference computes MHD dt inside the step, after the
-//                        ghost fill (SolverMHDMuscl.cpp:479-484)
+//                        ghost fill (SolverMHDMuscl.cpp:479-484).  Launched for
+//                        the first step only: every update kernel computes the
+//                        next step's CFL from the cells it has just updated
 //   2. mhd_trace_kernel  z-marching: face-field planes, primitive planes and
 //                        edge electric fields in shared memory, limited
 //                        slopes, CT half-step trace -> 47 numbers per cell
 //   3. mhd_update_kernel z-marching: HLLD fluxes (3 faces), 2D-HLLD emfs
 //                        (3 edges), conservative update and CT update of the
-//                        face fields, all from the compact trace
-// The state is read from HBM in 1 and 2 and written once in 3.
+//                        face fields, all from the compact trace; then the
+//                        CFL candidates of the updated cells (their high
+//                        faces at tile edges and domain ends are updated
+//                        redundantly, or follow the boundary condition as the
+//                        next step's ghost fill would) and the next step's dt
+// The state is read from HBM in 2 and 3 and written once in 3.
 #pragma once
 
 #include "ek_mhd.cuh"
@@ -564,12 +571,22 @@ struct UpdTile
 template <class S, class R, int TX, int TY, bool STAGE, int RS>
 __global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_MU_MINB_F32, EK_MU_MINB_F64))
 mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
-                  KParams P, DevClock * clk, int step)
+                  KParams P, DevClock * clk, int step, int cfl_next)
 {
   using T = UpdTile<TX, TY>;
   constexpr int NT = TX * TY;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R * sT = reinterpret_cast<R *>(smem_raw); // [2][T_N][YE][XE] trace planes (STAGE)
+  // next step's CFL (cfl_next): the final face fields of the cells of the
+  // last two finished planes (x / y faces by plane parity, the tile's +1
+  // column / row beside them), and the final hydro variables and z face of
+  // each thread's own cell of the last finished plane
+  double * sBxL = reinterpret_cast<double *>(smem_raw); // [2][TY][TX]
+  double * sByL = sBxL + 2 * TX * TY;                  // [2][TY][TX]
+  double * sBxE = sByL + 2 * TX * TY;                  // [2][TY]  Bx(i0 + TX)
+  double * sByE = sBxE + 2 * TY;                       // [2][TX]  By(j0 + TY)
+  double * sBzF = sByE + 2 * TX;                       // [TY][TX]
+  R *      sFinU = reinterpret_cast<R *>(sBzF + TX * TY); // [5][TY][TX]
+  R *      sT = sFinU + 5 * TX * TY;                   // [2][T_N][YE][XE] trace planes (STAGE)
   R * sFx = sT + (STAGE ? 2 * T_N * T::PL : 0); // [5][TY][TX+1]
   R * sFy = sFx + 5 * T::FXS;               // [5][TY+1][TX]
   R * sFz = sFy + 5 * T::FYS;               // [5][TY][TX]
@@ -621,6 +638,49 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
   const long long tst = STAGE ? (long long)T::PL : st; // field stride
 
   R acc[5];
+  R tmax = R(-INFINITY);
+  // the CFL candidate of the updated cell (gi, gj, kc) from its final
+  // hydro variables u and the final face fields on its low (bl) and high
+  // (br) faces (ConvertToPrimitivesFunctor3D_MHD + ComputeDtFunctor3D_MHD on
+  // the next step's state, as mhd_dt_kernel computes them)
+  auto cfl_cell = [&](const R (&u)[5], const double (&bl)[3], const double (&br)[3]) {
+    R blr[3], brr[3], q[8];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+    {
+      blr[c] = to_r<R>(bl[c]);
+      brr[c] = to_r<R>(br[c]);
+    }
+    mhd_constoprim<R>(u, blr, brr, q, C, [&](double (&a)[3], double (&b)[3]) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+      {
+        a[c] = bl[c];
+        b[c] = br[c];
+      }
+    });
+    tmax = fmax(tmax, mhd_invdt<R>(q, C.gamma0, P.dx, P.dy, P.dz, P.idx, P.idy, P.idz, P.idxd, P.idyd, P.idzd));
+  };
+  // the face field beyond the domain's high end along one axis, as the
+  // next step's ghost fill leaves it: outflow copies the last interior face,
+  // a reflecting wall negates it, periodic takes the CT update there (equal
+  // to the update of the first interior face: same inputs by the mapping)
+  auto high_face = [&](int bc, double own, double ct) {
+    return bc == BC_PERIODIC ? ct : (bc == BC_DIRICHLET ? -own : own);
+  };
+  // CT increments of the face fields, in the expressions of the update below
+  auto ct_add = [&](double b, R ep, R em, R ratio, double dratio) {
+    if constexpr (sizeof(R) == 8)
+      return b + (ep - em) * ratio;
+    else
+      return fma(f2d(ep) - f2d(em), dratio, b);
+  };
+  auto ct_sub = [&](double b, R ep, R em, R ratio, double dratio) {
+    if constexpr (sizeof(R) == 8)
+      return b - (ep - em) * ratio;
+    else
+      return fma(f2d(em) - f2d(ep), dratio, b);
+  };
   load_plane(k0 - 1);
   for (int k = k0; k <= k1; ++k)
   {
@@ -736,6 +796,50 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       bout[0 * st + off] = bx;
       bout[1 * st + off] = by;
       bout[2 * st + off] = bz;
+      if (cfl_next)
+      {
+        const int c = ty * TX + tx;
+        if (k > k0 + 1)
+        {
+          // cell k-2 is complete now that its high z face (this cell's bz)
+          // is final
+          const int par = (k - 2) & 1;
+          R         u[5];
+#pragma unroll
+          for (int v = 0; v < 5; ++v)
+            u[v] = sFinU[v * TX * TY + c];
+          const double bl[3] = { sBxL[par * TX * TY + c], sByL[par * TX * TY + c], sBzF[c] };
+          const double br[3] = { tx + 1 < TX && gi + 1 < P.nx + gw ? sBxL[par * TX * TY + c + 1] : sBxE[par * TY + ty],
+                                 ty + 1 < TY && gj + 1 < P.ny + gw ? sByL[par * TX * TY + c + TX] : sByE[par * TX + tx],
+                                 bz };
+          cfl_cell(u, bl, br);
+        }
+        // this cell's final state for the CFL at the next plane
+        const int par = (k - 1) & 1;
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+          sFinU[v * TX * TY + c] = (R)(S)acc[v];
+        sBxL[par * TX * TY + c] = bx;
+        sByL[par * TX * TY + c] = by;
+        sBzF[c] = bz;
+        if (tx == TX - 1 || gi + 1 == P.nx + gw)
+        {
+          // Bx on the cell's high x face: the tile's edge or the domain's end
+          double b1 = gi + 1 == P.nx + gw ? load_face<S>(mi, P, src_cell(P, gi + 1, gj, k - 1), 0)
+                                          : ldg(mi.b + 0 * st + off + 1);
+          b1 = ct_add(b1, Ezp[ezi + 1 + (TX + 1)], Ezp[ezi + 1], dtdy, ddtdy);
+          b1 = ct_sub(b1, Ey[eyi + 1], Eyp[eyi + 1], dtdz, ddtdz);
+          sBxE[par * TY + ty] = gi + 1 == P.nx + gw ? high_face(P.bc[1], bx, b1) : b1;
+        }
+        if (ty == TY - 1 || gj + 1 == P.ny + gw)
+        {
+          double b1 = gj + 1 == P.ny + gw ? load_face<S>(mi, P, src_cell(P, gi, gj + 1, k - 1), 1)
+                                          : ldg(mi.b + 1 * st + off + P.isize);
+          b1 = ct_sub(b1, Ezp[ezi + (TX + 1) + 1], Ezp[ezi + (TX + 1)], dtdx, ddtdx);
+          b1 = ct_add(b1, Ex[exi + TX], Exp[exi + TX], dtdz, ddtdz);
+          sByE[par * TX + tx] = gj + 1 == P.ny + gw ? high_face(P.bc[3], by, b1) : b1;
+        }
+      }
     }
     if (own && plane)
     {
@@ -773,8 +877,38 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
     }
     __syncthreads(); // trace slot, flux buffers and the older emf planes are reused
   }
+  if (cfl_next)
+  {
+    if (own && k1 > k0)
+    {
+      // the chunk's last cell (k1-1): its high z face is the next chunk's
+      // first face, updated here from the emfs of plane k1
+      const int       c = ty * TX + tx, par = (k1 - 1) & 1;
+      const long long off = (long long)k1 * P.plane + (long long)gj * P.isize + gi;
+      const R *       Ex1 = sEx + (k1 & 1) * T::EXS;
+      const R *       Ey1 = sEy + (k1 & 1) * T::EYS;
+      const int       eyi = ty * (TX + 1) + tx, exi = ty * TX + tx;
+      double          bz1 = k1 == P.nz + gw ? load_face<S>(mi, P, src_cell(P, gi, gj, k1), 2) : ldg(mi.b + 2 * st + off);
+      bz1 = ct_add(bz1, Ey1[eyi + 1], Ey1[eyi], dtdx, ddtdx);
+      bz1 = ct_sub(bz1, Ex1[exi + TX], Ex1[exi], dtdy, ddtdy);
+      if (k1 == P.nz + gw)
+        bz1 = high_face(P.bc[5], sBzF[c], bz1);
+      R u[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+        u[v] = sFinU[v * TX * TY + c];
+      const double bl[3] = { sBxL[par * TX * TY + c], sByL[par * TX * TY + c], sBzF[c] };
+      const double br[3] = { tx + 1 < TX && gi + 1 < P.nx + gw ? sBxL[par * TX * TY + c + 1] : sBxE[par * TY + ty],
+                             ty + 1 < TY && gj + 1 < P.ny + gw ? sByL[par * TX * TY + c + TX] : sByE[par * TX + tx],
+                             bz1 };
+      cfl_cell(u, bl, br);
+    }
+    block_max_commit<NT>(cand_key((double)tmax), &clk->key[(step + 1) % 3]);
+  }
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
     step_commit(clk, step, t, dt);
+  if (cfl_next)
+    finalize_step(clk, P, step + 1); // the next step's dt, once its CFL key is complete
 }
 
 // max |div B| over the interior, face differences with dx normalisation
@@ -808,7 +942,8 @@ template <class R>
 constexpr size_t
 mhd_update_smem(int TX, int TY, bool stage)
 {
-  return sizeof(R) * ((stage ? 2 * T_N * (TX + 2) * (TY + 2) : 0) + 5 * (TX + 1) * TY + 5 * TX * (TY + 1) + 5 * TX * TY +
+  return sizeof(double) * (5 * TX * TY + 2 * TY + 2 * TX) + sizeof(R) * 5 * TX * TY +
+         sizeof(R) * ((stage ? 2 * T_N * (TX + 2) * (TY + 2) : 0) + 5 * (TX + 1) * TY + 5 * TX * (TY + 1) + 5 * TX * TY +
                       2 * (TX + 1) * (TY + 1) + 2 * (TX + 1) * TY + 2 * TX * (TY + 1));
 }
 
@@ -818,7 +953,7 @@ constexpr int MU_TX = EK_MU_TX, MU_TY = EK_MU_TY; // update tile
 template <class S, class R>
 cudaError_t
 mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams & P, DevClock * clk,
-           int step, cudaStream_t st)
+           int step, bool cfl_next, cudaStream_t st)
 {
   // 1. dt of this step into clock slot step % 3
   if (phase == 0)
@@ -851,23 +986,23 @@ mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams 
     if (e != cudaSuccess)
       return e;
     dim3 grid((P.nx + MU_TX - 1) / MU_TX, (P.ny + MU_TY - 1) / MU_TY, (P.nz + P.kchunk - 1) / P.kchunk);
-    k<<<grid, MU_TX * MU_TY, sm, st>>>(Uin, Uout, (const R *)work, P, clk, step);
+    k<<<grid, MU_TX * MU_TY, sm, st>>>(Uin, Uout, (const R *)work, P, clk, step, cfl_next ? 1 : 0);
     return cudaGetLastError();
   }
 }
 
 cudaError_t
 mhd_step(int prec, int phase, const void * Uin, void * Uout, void * work, const KParams & P,
-         DevClock * clk, int step, cudaStream_t st)
+         DevClock * clk, int step, bool cfl_next, cudaStream_t st)
 {
 #ifdef EK_EXACT_ONLY
   if (prec != 0)
     return cudaErrorNotSupported;
-  return mhd_step_t<double, double>(phase, Uin, Uout, work, P, clk, step, st);
+  return mhd_step_t<double, double>(phase, Uin, Uout, work, P, clk, step, cfl_next, st);
 #else
   if (prec == 0)
-    return mhd_step_t<double, double>(phase, Uin, Uout, work, P, clk, step, st);
-  return mhd_step_t<float, float>(phase, Uin, Uout, work, P, clk, step, st);
+    return mhd_step_t<double, double>(phase, Uin, Uout, work, P, clk, step, cfl_next, st);
+  return mhd_step_t<float, float>(phase, Uin, Uout, work, P, clk, step, cfl_next, st);
 #endif
 }
 

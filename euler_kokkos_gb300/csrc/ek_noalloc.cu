@@ -228,8 +228,8 @@ ek_mhd3d_step_noalloc(const ek_params * params, const double * U_in, double * U_
   noalloc_clock_init<<<1, 1, 0, st>>>(clk, t, dt_slot, flags);
   cudaError_t e = cudaGetLastError();
   for (int phase = 0; phase < 3 && e == cudaSuccess; ++phase)
-    e = p.exact_fp ? ek_exact::mhd_step(0, phase, U_in, U_out, trace, kp, clk, 0, st)
-                   : ek_fast::mhd_step(0, phase, U_in, U_out, trace, kp, clk, 0, st);
+    e = p.exact_fp ? ek_exact::mhd_step(0, phase, U_in, U_out, trace, kp, clk, 0, false, st)
+                   : ek_fast::mhd_step(0, phase, U_in, U_out, trace, kp, clk, 0, false, st);
   if (e != cudaSuccess)
     return fail(EK_ERR_CUDA, std::string("ek_mhd3d_step_noalloc: launch: ") + cudaGetErrorString(e));
   if (!dt_out)
