@@ -958,7 +958,7 @@ t_bfslope(int f, int right, int e)
 // MHDBaseFunctor3D.h:905-955; MHDRunFunctors3D.h:1839-1874).
 template <class R, bool PLUS>
 __device__ __forceinline__ void
-face_state_dir(const R * t, long long st, int d, R (&q)[8], R smallr, R smallp)
+face_state_dir(const R * t, int st, int d, R (&q)[8], R smallr, R smallp)
 {
   auto h = [&](int f) {
     const R c = t[f * st], s = t[t_hslope(d, f) * st];
@@ -986,7 +986,7 @@ face_state_dir(const R * t, long long st, int d, R (&q)[8], R smallr, R smallp)
 // result is bit-identical to the per-direction expressions.
 template <class R, int S1, int S2>
 __device__ __forceinline__ EdgeCorner<R>
-edge_corner(const R * t, long long st, int d, int p1, int p2, R smallr, R smallp)
+edge_corner(const R * t, int st, int d, int p1, int p2, R smallr, R smallp)
 {
   auto sg1 = [](R x) { return S1 > 0 ? x : -x; };
   auto sg2 = [](R x) { return S2 > 0 ? x : -x; };

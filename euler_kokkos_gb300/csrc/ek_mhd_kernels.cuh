@@ -49,6 +49,34 @@ mhd_const(const KParams & P)
   return C;
 }
 
+// Compact trace in HBM, blocked by 32 cells along x: the trace cells are
+// [gw-1, n+gw] in each direction (trace-local it, jt, kt from 0); a block holds
+// 32 consecutive cells of one row, field after field ([f][32]), and blocks
+// follow in (it / 32, jt, kt) order.  A cell's 47 fields therefore sit at
+// compile-time offsets f * 32 from the cell's own address: gathering a face
+// or edge state costs one address computation per cell, not one per field
+// (a field-major layout over the whole grid needs a 64-bit product per load).
+constexpr int kTraceLanes = 32;
+struct TraceGrid
+{
+  int nb; // blocks per row: ceil((nx + 2) / 32)
+  int nj; // rows per plane: ny + 2
+};
+__host__ __device__ inline TraceGrid
+trace_grid(const KParams & P)
+{
+  return TraceGrid{ (P.nx + 2 + kTraceLanes - 1) / kTraceLanes, P.ny + 2 };
+}
+// address of the first field of the cell with global indices (i, j, k)
+template <class R>
+__device__ __forceinline__ R *
+trace_cell(R * trace, const TraceGrid & g, int gw, int i, int j, int k)
+{
+  const int it = i - (gw - 1), jt = j - (gw - 1), kt = k - (gw - 1);
+  const long long b = ((long long)kt * g.nj + jt) * g.nb + (it / kTraceLanes);
+  return trace + b * (T_N * kTraceLanes) + (it % kTraceLanes);
+}
+
 // state accessors: hydro planes of type S, face-field planes always FP64
 template <class S>
 struct MhdState
@@ -169,7 +197,7 @@ template <class R, int TX, int TY>
 __device__ __forceinline__ void
 trace_cell_compact(const R * sB, int bslot[4], const R * sQ, int qslot[3], const R * sE,
                    int eslot[2], int tx, int ty, R dtdx, R dtdy, R dtdz, const MhdConst<R> & C,
-                   R * out, long long ost)
+                   R * out)
 {
   using T = TraceTile<TX, TY>;
   // local tile coordinates of the cell in each buffer
@@ -338,7 +366,7 @@ trace_cell_compact(const R * sB, int bslot[4], const R * sQ, int qslot[3], const
   o[T_DCRY] = dCRy;
 #pragma unroll
   for (int f = 0; f < T_N; ++f)
-    out[f * ost] = o[f];
+    out[f * kTraceLanes] = o[f];
 }
 
 template <class S, class R, int TX, int TY>
@@ -369,13 +397,26 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
   const int k0 = gw - 1 + blockIdx.z * P.kchunk;
   const int k1 = min(k0 + P.kchunk, P.nz + gw + 1);
   const int nti = P.nx + 2, ntj = P.ny + 2; // trace cells per row / column
+  // planes whose gathered x/y window [c0-1, c0+TX+1] x [d0-1, d0+TY+1] lies in
+  // the interior need no boundary mapping: plain offsets, no sign flips
+  const bool xy_in = c0 - 1 >= gw && c0 + TX + 1 < P.nx + gw && d0 - 1 >= gw && d0 + TY + 1 < P.ny + gw;
+  auto src = [&](int gi, int gj, int gk) -> SrcCell {
+    if (xy_in && gk >= gw && gk < P.nz + gw)
+    {
+      SrcCell s;
+      s.off = (long long)gk * P.plane + (long long)gj * P.isize + gi;
+      s.fx = s.fy = s.fz = false;
+      return s;
+    }
+    return src_cell(P, gi, gj, gk);
+  };
 
   auto load_B = [&](int gk, int slot) {
     R * dst = sB + slot * T::BP;
     for (int c = threadIdx.x; c < T::BX * T::BY; c += NT)
     {
       const int     x = c % T::BX, y = c / T::BX;
-      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+      const SrcCell s = src(c0 - 1 + x, d0 - 1 + y, gk);
 #pragma unroll
       for (int comp = 0; comp < 3; ++comp)
         dst[(comp * T::BY + y) * T::BX + x] = to_r<R>(load_face<S>(m, P, s, comp));
@@ -387,7 +428,7 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
     for (int c = threadIdx.x; c < T::BX * T::BY; c += NT)
     {
       const int     x = c % T::BX, y = c / T::BX;
-      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+      const SrcCell s = src(c0 - 1 + x, d0 - 1 + y, gk);
 #pragma unroll
       for (int comp = 0; comp < 3; ++comp)
         cp_async<8>(rawB + (comp * T::BY + y) * T::BX + x, m.b + comp * P.vstride + s.off);
@@ -398,7 +439,7 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
     for (int c = threadIdx.x; c < T::BX * T::BY; c += NT)
     {
       const int     x = c % T::BX, y = c / T::BX;
-      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+      const SrcCell s = src(c0 - 1 + x, d0 - 1 + y, gk);
 #pragma unroll
       for (int comp = 0; comp < 3; ++comp)
       {
@@ -411,7 +452,7 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
     for (int c = threadIdx.x; c < T::QX * T::QY; c += NT)
     {
       const int     x = c % T::QX, y = c / T::QX;
-      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+      const SrcCell s = src(c0 - 1 + x, d0 - 1 + y, gk);
 #pragma unroll
       for (int v = 0; v < 5; ++v)
         cp_async<sizeof(S)>(rawU + (v * T::QY + y) * T::QX + x, m.h + v * P.vstride + s.off);
@@ -426,7 +467,7 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
     for (int c = threadIdx.x; c < T::QX * T::QY; c += NT)
     {
       const int     x = c % T::QX, y = c / T::QX;
-      const SrcCell s = src_cell(P, c0 - 1 + x, d0 - 1 + y, gk);
+      const SrcCell s = src(c0 - 1 + x, d0 - 1 + y, gk);
       R             u[5], q[8];
       if (from_raw)
       {
@@ -450,9 +491,9 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
         a[0] = load_face<S>(m, P, s, 0);
         a[1] = load_face<S>(m, P, s, 1);
         a[2] = load_face<S>(m, P, s, 2);
-        b[0] = load_face<S>(m, P, src_cell(P, gi + 1, gj, gk), 0);
-        b[1] = load_face<S>(m, P, src_cell(P, gi, gj + 1, gk), 1);
-        b[2] = load_face<S>(m, P, src_cell(P, gi, gj, gk + 1), 2);
+        b[0] = load_face<S>(m, P, src(gi + 1, gj, gk), 0);
+        b[1] = load_face<S>(m, P, src(gi, gj + 1, gk), 1);
+        b[2] = load_face<S>(m, P, src(gi, gj, gk + 1), 2);
       });
 #pragma unroll
       for (int v = 0; v < 8; ++v)
@@ -518,7 +559,7 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
   const int       tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   const bool      own = (c0 + tx) <= P.nx + gw && (d0 + ty) <= P.ny + gw && (c0 - (gw - 1) + tx) < nti &&
                    (d0 - (gw - 1) + ty) < ntj;
-  const long long ost = P.vstride;
+  const TraceGrid tg = trace_grid(P);
   for (int k = k0; k < k1; ++k)
   {
     // face plane k+2 and hydro plane k+1 were copied during the previous
@@ -541,9 +582,8 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
       int bslot[4] = { bsl(k - 1), bsl(k), bsl(k + 1), bsl(k + 2) };
       int qslot[3] = { qsl(k - 1), qsl(k), qsl(k + 1) };
       int eslot[2] = { esl(k), esl(k + 1) };
-      const long long off = (long long)k * P.plane + (long long)(d0 + ty) * P.isize + (c0 + tx);
       trace_cell_compact<R, TX, TY>(sB, bslot, sQ, qslot, sE, eslot, tx, ty, dtdx, dtdy, dtdz, C,
-                                    trace + off, ost);
+                                    trace_cell(trace, tg, gw, c0 + tx, d0 + ty, k));
     }
     __syncthreads();
   }
@@ -616,6 +656,7 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
   // the trace buffer holds cells [gw-1, n+gw] in each direction
   const int ihi = P.nx + gw, jhi = P.ny + gw;
 
+  const TraceGrid tg = trace_grid(P);
   auto load_plane = [&](int k) {
     if (!STAGE)
       return;
@@ -625,7 +666,7 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       const int f = c / T::PL, r = c - f * T::PL;
       const int x = r % T::XE, y = r / T::XE;
       const int i = min(i0 - 1 + x, ihi), j = min(j0 - 1 + y, jhi);
-      dst[c] = ldg(trace + f * st + (long long)k * P.plane + (long long)j * P.isize + i);
+      dst[c] = ldg(trace_cell(trace, tg, gw, i, j, k) + f * kTraceLanes);
     }
   };
   // trace pointer of cell (i, j) (global indices) of plane k: shared memory
@@ -633,9 +674,9 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
   auto TS = [&](int i, int j, int k) -> const R * {
     if (STAGE)
       return sT + (k & 1) * T_N * T::PL + (j - (j0 - 1)) * T::XE + (i - (i0 - 1));
-    return trace + (long long)k * P.plane + (long long)j * P.isize + i;
+    return trace_cell(trace, tg, gw, i, j, k);
   };
-  const long long tst = STAGE ? (long long)T::PL : st; // field stride
+  constexpr int tst = STAGE ? T::PL : kTraceLanes; // field stride
 
   R acc[5];
   R tmax = R(-INFINITY);
@@ -1026,7 +1067,10 @@ mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key, cu
 size_t
 mhd_work_bytes(int prec, const KParams & P)
 {
-  return (size_t)T_N * (size_t)P.vstride * (prec == 0 ? sizeof(double) : sizeof(float));
+  // blocks of 32 trace cells x 47 fields over (nx+2)/32 x (ny+2) x (nz+2)
+  const TraceGrid g = trace_grid(P);
+  return (size_t)T_N * kTraceLanes * (size_t)g.nb * (size_t)g.nj * (size_t)(P.nz + 2) *
+         (prec == 0 ? sizeof(double) : sizeof(float));
 }
 
 #ifndef EK_EXACT_ONLY

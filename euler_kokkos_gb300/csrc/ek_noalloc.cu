@@ -17,9 +17,10 @@
 // Limits and rules:
 //   * the array is EK_NOALLOC_SCRATCH_BYTES (64 MiB); every GPU context that
 //     loads this library holds it until the process exits;
-//   * FP64 trace = 47 * 8 bytes per cell of the ghosted grid, so grids with
-//     (nx+6)(ny+6)(nz+6) above (64 MiB - 512) / 376 = 178,479 cells (a 50^3
-//     interior is the largest cube) are rejected with EK_ERR_INVALID;
+//   * FP64 trace = 47 * 8 bytes per trace cell, the trace cells being
+//     32 ceil((nx+2)/32) x (ny+2) x (nz+2) (blocks of 32 along x): grids whose
+//     trace exceeds 64 MiB - 512 bytes (a 50^3 interior is the largest cube)
+//     are rejected with EK_ERR_INVALID;
 //   * the first call in each device context resolves the array's address with
 //     cudaGetSymbolAddress (that device current); make that first call before
 //     any stream capture.  The address is cached per device together with the
@@ -191,14 +192,12 @@ ek_mhd3d_step_noalloc(const ek_params * params, const double * U_in, double * U_
     return fail(EK_ERR_UNSUPPORTED, "ek_mhd3d_step_noalloc: the state arrays are FP64 (precision must be fp64)");
   const ekc::KParams kp = ek_internal::make_kparams(p);
   const size_t       trace_bytes = ek_exact::mhd_work_bytes(0, kp);
-  const size_t       cell_bytes = trace_bytes / (size_t)kp.vstride;
   if (trace_bytes > EK_NOALLOC_SCRATCH_BYTES - kTraceOffset)
     return fail(EK_ERR_INVALID,
                 "ek_mhd3d_step_noalloc: grid too large for the static scratch: the trace needs " +
-                    std::to_string(trace_bytes) + " bytes, the scratch holds " +
-                    std::to_string(EK_NOALLOC_SCRATCH_BYTES - kTraceOffset) + " (at most " +
-                    std::to_string((EK_NOALLOC_SCRATCH_BYTES - kTraceOffset) / cell_bytes) +
-                    " cells including ghosts)");
+                    std::to_string(trace_bytes) + " bytes (376 per trace cell, 32 ceil((nx+2)/32) x (ny+2) x "
+                    "(nz+2) cells), the scratch holds " +
+                    std::to_string(EK_NOALLOC_SCRATCH_BYTES - kTraceOffset));
   const size_t state = ek_internal::state_bytes(p, kp);
   const char * a = reinterpret_cast<const char *>(U_in);
   const char * b = reinterpret_cast<const char *>(U_out);

@@ -167,16 +167,30 @@ def test_asynchronous_nonfinite_dt_is_reported_by_the_next_synchronous_call():
     assert _step_noalloc(L, p, A2.data_ptr(), B2.data_ptr(), 0.0) == dt0
 
 
+def _trace_bytes(p):
+    # 47 FP64 values per trace cell; trace cells: 32-cell blocks along x
+    return 47 * 8 * 32 * ((p.nx + 2 + 31) // 32) * (p.ny + 2) * (p.nz + 2)
+
+
 def test_rejects_grid_beyond_the_static_scratch():
     L = _lib()
     ini, _ = P.smooth_random(dim=3, mhd=True, nx=51, ny=51, nz=51, seed=1, nsteps=1)
     p = ek.params_from_ini(ini)
-    assert (p.isize * p.jsize * p.ksize) * 47 * 8 > SCRATCH_BYTES - 512
+    assert _trace_bytes(p) > SCRATCH_BYTES - 512
     # the size check comes before any device call; the pointers are never used
     st = L.ek_mhd3d_step_noalloc(ctypes.byref(p), ctypes.c_void_p(1 << 40), ctypes.c_void_p(1 << 41), 0.0,
                                  None, None)
     assert st == EK_ERR_INVALID
     assert "static scratch" in L.ek_last_error().decode()
+    # a 50^3 interior fits: the call passes the size check (and fails only
+    # later where there is no GPU)
+    ini, _ = P.smooth_random(dim=3, mhd=True, nx=50, ny=50, nz=50, seed=1, nsteps=1)
+    q = ek.params_from_ini(ini)
+    assert _trace_bytes(q) <= SCRATCH_BYTES - 512
+    if not __import__("conftest").gpu_available():
+        st = L.ek_mhd3d_step_noalloc(ctypes.byref(q), ctypes.c_void_p(1 << 40), ctypes.c_void_p(1 << 41), 0.0,
+                                     None, None)
+        assert st != EK_ERR_INVALID, L.ek_last_error().decode()
 
 
 def test_rejects_bad_calls_before_any_device_work():
