@@ -77,6 +77,13 @@ trace_cell(R * trace, const TraceGrid & g, int gw, int i, int j, int k)
   return trace + b * (T_N * kTraceLanes) + (it % kTraceLanes);
 }
 
+// a direction as a type (compile-time specialisation of a gather)
+template <int V>
+struct DirC
+{
+  static constexpr int value = V;
+};
+
 // state accessors: hydro planes of type S, face-field planes always FP64
 template <class S>
 struct MhdState
@@ -751,14 +758,25 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
             f -= T::FXS, d = 1;
         }
         // face normal to d between cell (i,j,k) - e_d and cell (i,j,k)
-        // (MHDRunFunctors3D.h:1839-1874)
-        const int ex = TX + (d == 0 ? 1 : 0);
-        const int i = i0 + f % ex, j = j0 + f / ex;
+        // (MHDRunFunctors3D.h:1839-1874); rows of TX+1 x-faces or TX faces
+        // (constant divisors)
+        const int i = i0 + (d == 0 ? f % (TX + 1) : f % TX), j = j0 + (d == 0 ? f / (TX + 1) : f / TX);
         if (i > ihi - (d != 0 ? 1 : 0) || j > jhi - (d != 1 ? 1 : 0))
           continue;
         R ql[8], qr[8], fl[5];
-        face_state_dir<R, true>(TS(i - (d == 0), j - (d == 1), k - (d == 2)), tst, d, ql, sr, sp);
-        face_state_dir<R, false>(TS(i, j, k), tst, d, qr, sr, sp);
+        // the two face states, gathered with the direction fixed at compile
+        // time (every trace field at a constant offset); one solver call
+        auto gather = [&](auto dc) {
+          constexpr int D = decltype(dc)::value;
+          face_state_dir<R, true>(TS(i - (D == 0), j - (D == 1), k - (D == 2)), tst, D, ql, sr, sp);
+          face_state_dir<R, false>(TS(i, j, k), tst, D, qr, sr, sp);
+        };
+        if (d == 0)
+          gather(DirC<0>());
+        else if (d == 1)
+          gather(DirC<1>());
+        else
+          gather(DirC<2>());
         mhd_riemann<RS, R, 5>(ql, qr, fl, C.gamma0);
         R *       dst = d == 0 ? sFx : (d == 1 ? sFy : sFz);
         const int nd = d == 0 ? T::FXS : (d == 1 ? T::FYS : T::FZS);
@@ -778,19 +796,29 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       // edge along d at the low corner of cell (i,j,k); corners RT, RB, LT, LB
       // lie at -1 along (p1,p2), p1, p2 and nowhere (z-edge: RT(i-1,j-1),
       // RB(i-1,j), LT(i,j-1), LB(i,j); MHDRunFunctors3D.h:2180-2230)
-      const int ex = TX + (d != 0 ? 1 : 0);
-      const int i = i0 + f % ex, j = j0 + f / ex;
+      const int i = i0 + (d == 0 ? f % TX : f % (TX + 1)), j = j0 + (d == 0 ? f / TX : f / (TX + 1));
       if (i > ihi - (d == 0 ? 1 : 0) || j > jhi - (d == 1 ? 1 : 0))
         continue;
-      const int p1 = d == 2 ? 0 : d + 1, p2 = d == 0 ? 2 : d - 1;
-      const int i1 = p1 == 0, j1 = p1 == 1, k1s = p1 == 2;
-      const int i2 = p2 == 0, j2 = p2 == 1, k2s = p2 == 2;
-      const EdgeCorner<R> cRT =
-        edge_corner<R, 1, 1>(TS(i - i1 - i2, j - j1 - j2, k - k1s - k2s), tst, d, p1, p2, sr, sp);
-      const EdgeCorner<R> cRB = edge_corner<R, 1, -1>(TS(i - i1, j - j1, k - k1s), tst, d, p1, p2, sr, sp);
-      const EdgeCorner<R> cLT = edge_corner<R, -1, 1>(TS(i - i2, j - j2, k - k2s), tst, d, p1, p2, sr, sp);
-      const EdgeCorner<R> cLB = edge_corner<R, -1, -1>(TS(i, j, k), tst, d, p1, p2, sr, sp);
-      const R             e = mhd_emf_corners<R>(cRT, cRB, cLT, cLB, C.gamma0, C.smallc);
+      EdgeCorner<R> cRT, cRB, cLT, cLB;
+      // the four corner states, gathered with the direction fixed at compile
+      // time; one emf solver call
+      auto gather = [&](auto dc) {
+        constexpr int D = decltype(dc)::value;
+        constexpr int p1 = D == 2 ? 0 : D + 1, p2 = D == 0 ? 2 : D - 1;
+        constexpr int i1 = p1 == 0, j1 = p1 == 1, k1s = p1 == 2;
+        constexpr int i2 = p2 == 0, j2 = p2 == 1, k2s = p2 == 2;
+        cRT = edge_corner<R, 1, 1>(TS(i - i1 - i2, j - j1 - j2, k - k1s - k2s), tst, D, p1, p2, sr, sp);
+        cRB = edge_corner<R, 1, -1>(TS(i - i1, j - j1, k - k1s), tst, D, p1, p2, sr, sp);
+        cLT = edge_corner<R, -1, 1>(TS(i - i2, j - j2, k - k2s), tst, D, p1, p2, sr, sp);
+        cLB = edge_corner<R, -1, -1>(TS(i, j, k), tst, D, p1, p2, sr, sp);
+      };
+      if (d == 0)
+        gather(DirC<0>());
+      else if (d == 1)
+        gather(DirC<1>());
+      else
+        gather(DirC<2>());
+      const R e = mhd_emf_corners<R>(cRT, cRB, cLT, cLB, C.gamma0, C.smallc);
       (d == 0 ? Ex : (d == 1 ? Ey : Ez))[f] = e;
     }
     __syncthreads();
