@@ -3,6 +3,8 @@
 // the FP64 build without FMA contraction reproduces the reference bit for bit.
 #pragma once
 
+#include <type_traits>
+
 #include "ek_common.cuh"
 
 namespace EK_NS
@@ -950,22 +952,70 @@ t_bfslope(int f, int right, int e)
   return T_DALY + 6 * right + 2 * f + (e < f ? e : e - 1);
 }
 
+// Accessors of a cell's trace fields: A(f) is field f.
+// StrideAcc: field-major storage with stride st (the staged shared-memory
+// planes).  QuadAcc: the HBM trace, 16-byte quads of fields per cell (see
+// trace_cell); the gathers below read compile-time field indices, so only the
+// quads a face or edge state needs are loaded (the others are never used and
+// their loads are removed), one vector load per quad.
+template <class R>
+struct StrideAcc
+{
+  const R * t;
+  int       st;
+  __device__ __forceinline__ R
+  operator()(int f) const
+  {
+    return t[f * st];
+  }
+};
+constexpr int kTraceLanes = 32; // cells per block of the HBM trace
+template <class R>
+using TVec = typename std::conditional<sizeof(R) == 4, float4, double2>::type;
+template <class R>
+constexpr int kTVecN = 16 / (int)sizeof(R); // fields per quad
+template <class R>
+constexpr int kTQuads = (T_N + kTVecN<R> - 1) / kTVecN<R>; // quads per cell
+template <class R>
+struct QuadAcc
+{
+  TVec<R> v[kTQuads<R>];
+  __device__ __forceinline__ explicit QuadAcc(const R * t)
+  {
+#pragma unroll
+    for (int q = 0; q < kTQuads<R>; ++q)
+      v[q] = __ldg(reinterpret_cast<const TVec<R> *>(t + q * kTraceLanes * kTVecN<R>));
+  }
+  __device__ __forceinline__ R
+  operator()(int f) const
+  {
+    const TVec<R> & x = v[f / kTVecN<R>];
+    if constexpr (sizeof(R) == 4)
+    {
+      const int c = f % 4;
+      return c == 0 ? x.x : (c == 1 ? x.y : (c == 2 ? x.z : x.w));
+    }
+    else
+      return f % 2 == 0 ? x.x : x.y;
+  }
+};
+
 // Face state of a cell on its face normal to d (PLUS: the right face, the
-// left state of that face; otherwise the left face), in the face frame the
-// flux functor hands to the Riemann solver: normal velocity in IU and normal
-// field in IA, with the reference's component swaps for y (IU<->IV, IA<->IB)
-// and z (IU<->IW, IA<->IC) faces (trace_unsplit_mhd_3d_simpler,
-// MHDBaseFunctor3D.h:905-955; MHDRunFunctors3D.h:1839-1874).
-template <class R, bool PLUS>
+// left state of that face), in the face frame the flux functor hands to the
+// Riemann solver: normal velocity in IU and normal field in IA, with the
+// reference's component swaps for y (IU<->IV, IA<->IB) and z (IU<->IW,
+// IA<->IC) faces (trace_unsplit_mhd_3d_simpler, MHDBaseFunctor3D.h:905-955;
+// MHDRunFunctors3D.h:1839-1874).
+template <class R, bool PLUS, class ACC>
 __device__ __forceinline__ void
-face_state_dir(const R * t, int st, int d, R (&q)[8], R smallr, R smallp)
+face_state_acc(const ACC & T, int d, R (&q)[8], R smallr, R smallp)
 {
   auto h = [&](int f) {
-    const R c = t[f * st], s = t[t_hslope(d, f) * st];
+    const R c = T(f), s = T(t_hslope(d, f));
     return PLUS ? c + s : c - s;
   };
   auto tb = [&](int f) {
-    const R c = t[(T_A + f) * st], s = t[t_bslope(d, f) * st];
+    const R c = T(T_A + f), s = T(t_bslope(d, f));
     return PLUS ? c + s : c - s;
   };
   q[ID] = h(T_R);
@@ -973,10 +1023,16 @@ face_state_dir(const R * t, int st, int d, R (&q)[8], R smallr, R smallp)
   q[IU] = h(T_U + d);
   q[IV] = h(d == 1 ? T_U : T_V);
   q[IW] = h(d == 2 ? T_U : T_W);
-  q[IA] = t[t_bface(d, PLUS ? 1 : 0) * st];
+  q[IA] = T(t_bface(d, PLUS ? 1 : 0));
   q[IB] = tb(d == 1 ? 0 : 1);
   q[IC] = tb(d == 2 ? 0 : 2);
   floor_state(q, smallr, smallp);
+}
+template <class R, bool PLUS>
+__device__ __forceinline__ void
+face_state_dir(const R * t, int st, int d, R (&q)[8], R smallr, R smallp)
+{
+  face_state_acc<R, PLUS>(StrideAcc<R>{ t, st }, d, q, smallr, smallp);
 }
 
 // One corner of an edge along d (MHDBaseFunctor3D.h:957-1113).  The
@@ -984,24 +1040,28 @@ face_state_dir(const R * t, int st, int d, R (&q)[8], R smallr, R smallp)
 // compute_emf<emfDir> reads them; S1/S2 are the sides (+1 right, -1 left) of
 // the corner along p1/p2.  Each sum keeps the reference's operands, so the
 // result is bit-identical to the per-direction expressions.
-template <class R, int S1, int S2>
+template <class R, int S1, int S2, class ACC>
 __device__ __forceinline__ EdgeCorner<R>
-edge_corner(const R * t, int st, int d, int p1, int p2, R smallr, R smallp)
+edge_corner_acc(const ACC & T, int d, int p1, int p2, R smallr, R smallp)
 {
   auto sg1 = [](R x) { return S1 > 0 ? x : -x; };
   auto sg2 = [](R x) { return S2 > 0 ? x : -x; };
-  auto hyd = [&](int f) {
-    return t[f * st] + (sg1(t[t_hslope(p1, f) * st]) + sg2(t[t_hslope(p2, f) * st]));
-  };
+  auto hyd = [&](int f) { return T(f) + (sg1(T(t_hslope(p1, f))) + sg2(T(t_hslope(p2, f)))); };
   EdgeCorner<R> e;
   e.r = fmax(smallr, hyd(T_R));
   e.p = fmax(smallp, hyd(T_P));
   e.u = hyd(T_U + p1);
   e.v = hyd(T_U + p2);
-  e.a = t[t_bface(p1, S1 > 0) * st] + sg2(t[t_bfslope(p1, S1 > 0, p2) * st]);
-  e.b = t[t_bface(p2, S2 > 0) * st] + sg1(t[t_bfslope(p2, S2 > 0, p1) * st]);
-  e.c = t[(T_A + d) * st] + (sg1(t[t_bslope(p1, d) * st]) + sg2(t[t_bslope(p2, d) * st]));
+  e.a = T(t_bface(p1, S1 > 0)) + sg2(T(t_bfslope(p1, S1 > 0, p2)));
+  e.b = T(t_bface(p2, S2 > 0)) + sg1(T(t_bfslope(p2, S2 > 0, p1)));
+  e.c = T(T_A + d) + (sg1(T(t_bslope(p1, d))) + sg2(T(t_bslope(p2, d))));
   return e;
+}
+template <class R, int S1, int S2>
+__device__ __forceinline__ EdgeCorner<R>
+edge_corner(const R * t, int st, int d, int p1, int p2, R smallr, R smallp)
+{
+  return edge_corner_acc<R, S1, S2>(StrideAcc<R>{ t, st }, d, p1, p2, smallr, smallp);
 }
 
 } // namespace EK_NS

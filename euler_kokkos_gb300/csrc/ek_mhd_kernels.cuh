@@ -51,12 +51,14 @@ mhd_const(const KParams & P)
 
 // Compact trace in HBM, blocked by 32 cells along x: the trace cells are
 // [gw-1, n+gw] in each direction (trace-local it, jt, kt from 0); a block holds
-// 32 consecutive cells of one row, field after field ([f][32]), and blocks
-// follow in (it / 32, jt, kt) order.  A cell's 47 fields therefore sit at
-// compile-time offsets f * 32 from the cell's own address: gathering a face
-// or edge state costs one address computation per cell, not one per field
-// (a field-major layout over the whole grid needs a 64-bit product per load).
-constexpr int kTraceLanes = 32;
+// 32 consecutive cells of one row as 16-byte quads of fields, quad after quad
+// ([quad][32 cells][4 floats or 2 doubles]), and blocks follow in
+// (it / 32, jt, kt) order.  A cell's fields therefore sit at compile-time
+// offsets from the cell's own address, four (two) per 16-byte vector load:
+// gathering a face or edge state costs one address computation per cell and
+// one load per quad (a field-major layout over the whole grid needs a 64-bit
+// product per field).  A warp reading one quad of 32 consecutive cells reads
+// 512 contiguous bytes.
 struct TraceGrid
 {
   int nb; // blocks per row: ceil((nx + 2) / 32)
@@ -68,13 +70,23 @@ trace_grid(const KParams & P)
   return TraceGrid{ (P.nx + 2 + kTraceLanes - 1) / kTraceLanes, P.ny + 2 };
 }
 // address of the first field of the cell with global indices (i, j, k)
+// elements of one 32-cell block (the same for FP32 and FP64: 48 fields)
+template <class R>
+constexpr int kTraceBlock = kTQuads<R> * kTraceLanes * kTVecN<R>;
 template <class R>
 __device__ __forceinline__ R *
 trace_cell(R * trace, const TraceGrid & g, int gw, int i, int j, int k)
 {
   const int it = i - (gw - 1), jt = j - (gw - 1), kt = k - (gw - 1);
   const long long b = ((long long)kt * g.nj + jt) * g.nb + (it / kTraceLanes);
-  return trace + b * (T_N * kTraceLanes) + (it % kTraceLanes);
+  return trace + b * kTraceBlock<R> + (it % kTraceLanes) * kTVecN<R>;
+}
+// element offset of field f from its cell's address
+template <class R>
+__host__ __device__ constexpr int
+trace_field(int f)
+{
+  return (f / kTVecN<R>) * (kTraceLanes * kTVecN<R>) + f % kTVecN<R>;
 }
 
 // a direction as a type (compile-time specialisation of a gather)
@@ -371,9 +383,21 @@ trace_cell_compact(const R * sB, int bslot[4], const R * sQ, int qslot[3], const
   o[T_DCLY] = dCLy;
   o[T_DARY] = dARy, o[T_DARZ] = dARz, o[T_DBRX] = dBRx, o[T_DBRZ] = dBRz, o[T_DCRX] = dCRx,
   o[T_DCRY] = dCRy;
+  // one 16-byte store per quad (the last quad's spare fields are zero)
 #pragma unroll
-  for (int f = 0; f < T_N; ++f)
-    out[f * kTraceLanes] = o[f];
+  for (int q = 0; q < kTQuads<R>; ++q)
+  {
+    R w[kTVecN<R>];
+#pragma unroll
+    for (int c = 0; c < kTVecN<R>; ++c)
+      w[c] = q * kTVecN<R> + c < T_N ? o[q * kTVecN<R> + c] : R(0);
+    TVec<R> x;
+    if constexpr (sizeof(R) == 4)
+      x = make_float4(w[0], w[1], w[2], w[3]);
+    else
+      x = make_double2(w[0], w[1]);
+    *reinterpret_cast<TVec<R> *>(out + q * kTraceLanes * kTVecN<R>) = x;
+  }
 }
 
 template <class S, class R, int TX, int TY>
@@ -673,7 +697,7 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       const int f = c / T::PL, r = c - f * T::PL;
       const int x = r % T::XE, y = r / T::XE;
       const int i = min(i0 - 1 + x, ihi), j = min(j0 - 1 + y, jhi);
-      dst[c] = ldg(trace_cell(trace, tg, gw, i, j, k) + f * kTraceLanes);
+      dst[c] = ldg(trace_cell(trace, tg, gw, i, j, k) + trace_field<R>(f));
     }
   };
   // trace pointer of cell (i, j) (global indices) of plane k: shared memory
@@ -683,7 +707,7 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       return sT + (k & 1) * T_N * T::PL + (j - (j0 - 1)) * T::XE + (i - (i0 - 1));
     return trace_cell(trace, tg, gw, i, j, k);
   };
-  constexpr int tst = STAGE ? T::PL : kTraceLanes; // field stride
+  constexpr int tst = T::PL; // field stride of the staged planes
 
   R acc[5];
   R tmax = R(-INFINITY);
@@ -768,8 +792,18 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
         // time (every trace field at a constant offset); one solver call
         auto gather = [&](auto dc) {
           constexpr int D = decltype(dc)::value;
-          face_state_dir<R, true>(TS(i - (D == 0), j - (D == 1), k - (D == 2)), tst, D, ql, sr, sp);
-          face_state_dir<R, false>(TS(i, j, k), tst, D, qr, sr, sp);
+          const R * tl = TS(i - (D == 0), j - (D == 1), k - (D == 2));
+          const R * tr = TS(i, j, k);
+          if constexpr (STAGE)
+          {
+            face_state_dir<R, true>(tl, tst, D, ql, sr, sp);
+            face_state_dir<R, false>(tr, tst, D, qr, sr, sp);
+          }
+          else
+          {
+            face_state_acc<R, true>(QuadAcc<R>(tl), D, ql, sr, sp);
+            face_state_acc<R, false>(QuadAcc<R>(tr), D, qr, sr, sp);
+          }
         };
         if (d == 0)
           gather(DirC<0>());
@@ -807,10 +841,24 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
         constexpr int p1 = D == 2 ? 0 : D + 1, p2 = D == 0 ? 2 : D - 1;
         constexpr int i1 = p1 == 0, j1 = p1 == 1, k1s = p1 == 2;
         constexpr int i2 = p2 == 0, j2 = p2 == 1, k2s = p2 == 2;
-        cRT = edge_corner<R, 1, 1>(TS(i - i1 - i2, j - j1 - j2, k - k1s - k2s), tst, D, p1, p2, sr, sp);
-        cRB = edge_corner<R, 1, -1>(TS(i - i1, j - j1, k - k1s), tst, D, p1, p2, sr, sp);
-        cLT = edge_corner<R, -1, 1>(TS(i - i2, j - j2, k - k2s), tst, D, p1, p2, sr, sp);
-        cLB = edge_corner<R, -1, -1>(TS(i, j, k), tst, D, p1, p2, sr, sp);
+        const R * tRT = TS(i - i1 - i2, j - j1 - j2, k - k1s - k2s);
+        const R * tRB = TS(i - i1, j - j1, k - k1s);
+        const R * tLT = TS(i - i2, j - j2, k - k2s);
+        const R * tLB = TS(i, j, k);
+        if constexpr (STAGE)
+        {
+          cRT = edge_corner<R, 1, 1>(tRT, tst, D, p1, p2, sr, sp);
+          cRB = edge_corner<R, 1, -1>(tRB, tst, D, p1, p2, sr, sp);
+          cLT = edge_corner<R, -1, 1>(tLT, tst, D, p1, p2, sr, sp);
+          cLB = edge_corner<R, -1, -1>(tLB, tst, D, p1, p2, sr, sp);
+        }
+        else
+        {
+          cRT = edge_corner_acc<R, 1, 1>(QuadAcc<R>(tRT), D, p1, p2, sr, sp);
+          cRB = edge_corner_acc<R, 1, -1>(QuadAcc<R>(tRB), D, p1, p2, sr, sp);
+          cLT = edge_corner_acc<R, -1, 1>(QuadAcc<R>(tLT), D, p1, p2, sr, sp);
+          cLB = edge_corner_acc<R, -1, -1>(QuadAcc<R>(tLB), D, p1, p2, sr, sp);
+        }
       };
       if (d == 0)
         gather(DirC<0>());
@@ -1095,10 +1143,11 @@ mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key, cu
 size_t
 mhd_work_bytes(int prec, const KParams & P)
 {
-  // blocks of 32 trace cells x 47 fields over (nx+2)/32 x (ny+2) x (nz+2)
+  // blocks of 32 trace cells x 48 fields over (nx+2)/32 x (ny+2) x (nz+2)
   const TraceGrid g = trace_grid(P);
-  return (size_t)T_N * kTraceLanes * (size_t)g.nb * (size_t)g.nj * (size_t)(P.nz + 2) *
-         (prec == 0 ? sizeof(double) : sizeof(float));
+  const size_t    blk = prec == 0 ? (size_t)kTraceBlock<double> * sizeof(double)
+                                  : (size_t)kTraceBlock<float> * sizeof(float);
+  return blk * (size_t)g.nb * (size_t)g.nj * (size_t)(P.nz + 2);
 }
 
 #ifndef EK_EXACT_ONLY

@@ -17,7 +17,7 @@
 // Limits and rules:
 //   * the array is EK_NOALLOC_SCRATCH_BYTES (64 MiB); every GPU context that
 //     loads this library holds it until the process exits;
-//   * FP64 trace = 47 * 8 bytes per trace cell, the trace cells being
+//   * FP64 trace = 48 * 8 bytes per trace cell (47 values and one spare), the trace cells being
 //     32 ceil((nx+2)/32) x (ny+2) x (nz+2) (blocks of 32 along x): grids whose
 //     trace exceeds 64 MiB - 512 bytes (a 50^3 interior is the largest cube)
 //     are rejected with EK_ERR_INVALID;
@@ -195,7 +195,7 @@ ek_mhd3d_step_noalloc(const ek_params * params, const double * U_in, double * U_
   if (trace_bytes > EK_NOALLOC_SCRATCH_BYTES - kTraceOffset)
     return fail(EK_ERR_INVALID,
                 "ek_mhd3d_step_noalloc: grid too large for the static scratch: the trace needs " +
-                    std::to_string(trace_bytes) + " bytes (376 per trace cell, 32 ceil((nx+2)/32) x (ny+2) x "
+                    std::to_string(trace_bytes) + " bytes (384 per trace cell, 32 ceil((nx+2)/32) x (ny+2) x "
                     "(nz+2) cells), the scratch holds " +
                     std::to_string(EK_NOALLOC_SCRATCH_BYTES - kTraceOffset));
   const size_t state = ek_internal::state_bytes(p, kp);

@@ -260,7 +260,7 @@ ek_status ek_ensemble_stream(ek_ensemble * e, void ** stream);
  *
  * The step's temporary (the 47 x FP64 per-cell compact trace) lives in one
  * static device array of EK_NOALLOC_SCRATCH_BYTES, held by every GPU context
- * that loads this library until the process exits.  The trace takes 376 bytes
+ * that loads this library until the process exits.  The trace takes 384 bytes
  * for each of 32 ceil((nx+2)/32) x (ny+2) x (nz+2) cells; grids whose trace
  * exceeds EK_NOALLOC_SCRATCH_BYTES - 512 (a 50^3 interior is the largest cube)
  * are rejected: EK_ERR_INVALID.

@@ -168,8 +168,9 @@ def test_asynchronous_nonfinite_dt_is_reported_by_the_next_synchronous_call():
 
 
 def _trace_bytes(p):
-    # 47 FP64 values per trace cell; trace cells: 32-cell blocks along x
-    return 47 * 8 * 32 * ((p.nx + 2 + 31) // 32) * (p.ny + 2) * (p.nz + 2)
+    # 48 FP64 values per trace cell (47 and a spare); trace cells: 32-cell
+    # blocks along x
+    return 48 * 8 * 32 * ((p.nx + 2 + 31) // 32) * (p.ny + 2) * (p.nz + 2)
 
 
 def test_rejects_grid_beyond_the_static_scratch():
