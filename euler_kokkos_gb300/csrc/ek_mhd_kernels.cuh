@@ -77,7 +77,9 @@ template <class R>
 __device__ __forceinline__ R *
 trace_cell(R * trace, const TraceGrid & g, int gw, int i, int j, int k)
 {
-  const int it = i - (gw - 1), jt = j - (gw - 1), kt = k - (gw - 1);
+  // trace-local indices are never negative: unsigned division and remainder
+  // by 32 are a shift and a mask
+  const unsigned it = (unsigned)(i - (gw - 1)), jt = (unsigned)(j - (gw - 1)), kt = (unsigned)(k - (gw - 1));
   const long long b = ((long long)kt * g.nj + jt) * g.nb + (it / kTraceLanes);
   return trace + b * kTraceBlock<R> + (it % kTraceLanes) * kTVecN<R>;
 }

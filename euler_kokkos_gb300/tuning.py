@@ -42,13 +42,13 @@ CANDIDATES = {
     "mhd_trace": [{"EK_MT_TX": "32", "EK_MT_TY": "4"}, {"EK_MT_TX": "16", "EK_MT_TY": "8"}, {"EK_MT_TX": "32", "EK_MT_TY": "8"},
                   {"EK_MT_TX": "64", "EK_MT_TY": "2"}, {"EK_MT_TX": "16", "EK_MT_TY": "4"},
                   {"EK_MT_TX": "32", "EK_MT_TY": "4", "EK_MT_MINB_F32": "6"}, {"EK_MT_TX": "64", "EK_MT_TY": "4"}],
-    "mhd_update": [{"EK_MU_TX": "16", "EK_MU_TY": "8", "EK_MU_MINB_F32": "8"},
+    "mhd_update": [{"EK_MU_TX": "32", "EK_MU_TY": "8", "EK_MU_MINB_F32": "4"},
                    {"EK_MU_TX": "32", "EK_MU_TY": "4", "EK_MU_MINB_F32": "8"},
-                   {"EK_MU_TX": "8", "EK_MU_TY": "16", "EK_MU_MINB_F32": "8"},
+                   {"EK_MU_TX": "16", "EK_MU_TY": "8", "EK_MU_MINB_F32": "8"},
+                   {"EK_MU_TX": "64", "EK_MU_TY": "4", "EK_MU_MINB_F32": "4"},
+                   {"EK_MU_TX": "32", "EK_MU_TY": "16", "EK_MU_MINB_F32": "2"},
                    {"EK_MU_TX": "16", "EK_MU_TY": "16", "EK_MU_MINB_F32": "4"},
-                   {"EK_MU_TX": "32", "EK_MU_TY": "8", "EK_MU_MINB_F32": "4"},
-                   {"EK_MU_TX": "32", "EK_MU_TY": "8", "EK_MU_MINB_F32": "3"},
-                   {"EK_MU_TX": "32", "EK_MU_TY": "8", "EK_MU_MINB_F32": "2"}],
+                   {"EK_MU_TX": "32", "EK_MU_TY": "8", "EK_MU_MINB_F32": "3"}],
     "mhd2d": [{"EK_M2_TX": "16", "EK_M2_TY": "8"}, {"EK_M2_TX": "32", "EK_M2_TY": "8"}, {"EK_M2_TX": "16", "EK_M2_TY": "16"},
               {"EK_M2_TX": "32", "EK_M2_TY": "4"}, {"EK_M2_TX": "8", "EK_M2_TY": "8"},
               {"EK_M2_TX": "16", "EK_M2_TY": "16", "EK_M2_MINB_F32": "3"},
