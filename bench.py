@@ -65,11 +65,11 @@ KERNEL_NAMES = {
 # are in profiles/); a launch's traffic on the bench workload is this figure
 # times its interior cells (these kernels' traffic grows with the cells).
 TRAFFIC_PER_CELL = {
-    ("hydro3d", "mixed"): {"hydro3d_step": 38.3},   # 158.6 + 112.5 MB / 7.08 M cells
+    ("hydro3d", "mixed"): {"hydro3d_step": 38.3},   # 158.6 + 112.7 MB / 7.08 M cells
     ("hydro3d", "fp64"): {"hydro3d_step": 78.2},    # 306.3 + 247.4 MB / 7.08 M cells
-    ("mhd3d", "mixed"): {"mhd_dt_kernel": 46.0,      # 323 + 3 MB / 7.08 M cells
-                         "mhd_trace_kernel": 259.5,  # 468 + 1369 MB / 7.08 M cells
-                         "mhd_update_kernel": 325.7},  # 1981.6 + 323.4 MB / 7.08 M cells
+    ("mhd3d", "mixed"): {"mhd_dt_kernel": 46.0,      # 323 + 3 MB / 7.08 M cells (first step only)
+                         "mhd_trace_kernel": 243.0,  # 375.4 + 1345.0 MB / 7.08 M cells
+                         "mhd_update_kernel": 338.2},  # 2063.4 + 331.1 MB / 7.08 M cells
     ("mhd2d", "mixed"): {"mhd2d_step_kernel": 78.1},  # 186.4 + 141.0 MB / 4.19 M cells
 }
 
@@ -512,11 +512,16 @@ def main():
                              "share": kms / ktot if ktot else None,
                              "traffic_per_cell": tr.get(name)}
         dom = max(kernels, key=lambda k: kernels[k]["ms_per_launch"]) if kernels else None
-        out = {"bound": "hbm", "scope": "whole step (%d launch%s per step)" %
-                                        (len(names), "" if len(names) == 1 else "es"),
+        # DRAM bytes per step: each kernel's traffic per launch times its
+        # launches per step (the CFL kernel of the first step only amortises)
+        step_tr = None
+        if tr and all(n in tr for n in kernels):
+            step_tr = sum(tr[n] * kernels[n]["launches_per_step"] for n in kernels)
+        nl = sum(k["launches_per_step"] for k in kernels.values())
+        out = {"bound": "hbm", "scope": "whole step (%.2f launches per step)" % nl,
                "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-               "traffic": sum(tr.values()) * cells if tr and all(n in tr for _, n in names) else None,
-               "traffic_per_cell": sum(tr.values()) if tr else None,
+               "traffic": step_tr * cells if step_tr is not None else None,
+               "traffic_per_cell": step_tr,
                "algorithmic_bytes_per_cell": algo, "ms_per_step": ms_step, "peak_source": peak_kind,
                "kernels": kernels}
         if dom:
