@@ -72,7 +72,7 @@ struct ek_solver
   double                   kernel_ms[3] = { 0, 0, 0 };
   long long                kernel_n[3] = { 0, 0, 0 };
   bool                     owns = true; // false: a view into an ensemble's buffers
-  // MHD: the step whose CFL the last step kernel computed (-1: none)
+  // 3D MHD: the step whose CFL the last update kernel computed (-1: none)
   int                      cfl_step = -1;
 };
 
@@ -757,8 +757,8 @@ launch_one(ek_solver * s, int kernel_id, int phase, int step)
   }
   cudaError_t e;
   if (s->p.mhd && s->p.dim == 2)
-    e = s->exact ? ek_exact::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, true, s->stream)
-                 : ek_fast::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, true, s->stream);
+    e = s->exact ? ek_exact::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, s->stream)
+                 : ek_fast::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, s->stream);
   else if (s->p.mhd)
     e = s->exact ? ek_exact::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, true, s->stream)
                  : ek_fast::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, true, s->stream);
@@ -785,18 +785,15 @@ launch_step(ek_solver * s, int step)
 {
   if (!s->p.mhd)
     return launch_one(s, 0, 0, step);
-  // CFL of the step: only when no step kernel computed it (the first step
-  // after the state was set)
   if (s->p.dim == 2)
   {
-    ek_status st = EK_OK;
-    if (s->cfl_step != step)
-      st = launch_one(s, 2, 0, step);
+    ek_status st = launch_one(s, 2, 0, step); // CFL of the step
     if (st == EK_OK)
-      st = launch_one(s, 0, 1, step); // trace, fluxes, emf, update, and the next step's CFL
-    s->cfl_step = st == EK_OK ? step + 1 : -1;
+      st = launch_one(s, 0, 1, step); // trace, fluxes, emf, update
     return st;
   }
+  // CFL of the step: only when no update kernel computed it (the first step
+  // after the state was set)
   ek_status st = EK_OK;
   if (s->cfl_step != step)
     st = launch_one(s, 2, 0, step);

@@ -27,10 +27,9 @@
   cudaError_t mhd_step(int prec, int phase, const void * Uin, void * Uout, void * work,             \
                        const KParams & P, DevClock * clk, int step, bool cfl_next, cudaStream_t st); \
   size_t      mhd_work_bytes(int prec, const KParams & P);                                          \
-  /* one MHD 2D step = phase 0 (CFL), 1 (fused trace, fluxes, emf, update; cfl_next: and the  */ \
-  /* next step's CFL) */                                                                          \
+  /* one MHD 2D step = phase 0 (CFL), 1 (fused trace, fluxes, emf, update) */                      \
   cudaError_t mhd2d_step(int prec, int phase, const void * Uin, void * Uout, const KParams & P,     \
-                         DevClock * clk, int step, bool cfl_next, cudaStream_t st);                 \
+                         DevClock * clk, int step, cudaStream_t st);                                \
   cudaError_t mhd2d_dt(int prec, const void * U, const KParams & P, unsigned long long * key,       \
                        cudaStream_t st);                                                            \
   /* one step of every instance of a 2D hydro ensemble (persistent kernel) */                       \

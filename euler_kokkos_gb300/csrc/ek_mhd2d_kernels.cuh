@@ -106,52 +106,6 @@ load_mhd2d_cell(const MhdState<S> & m, const KParams & P, const SrcCell & s, R (
   bz = load_face<S>(m, P, s, 2);
 }
 
-// CFL candidate of one cell: ConvertToPrimitivesFunctor2D_MHD of its hydro
-// variables u, face fields bl0/bl1 (own), br0/br1 (+1 neighbours) and
-// cell-centred bz, then find_speed_info<TWO_D> summed as ComputeDtFunctor2D_MHD
-// does (x and y only, mhd_utils.h:319-366)
-template <class R>
-__device__ __forceinline__ R
-mhd2d_cell_invdt(const R (&u)[5], double bl0, double bl1, double bz, double br0, double br1,
-                 const MhdConst<R> & C, const KParams & P)
-{
-  R bl[3] = { to_r<R>(bl0), to_r<R>(bl1), to_r<R>(bz) };
-  R br[3] = { to_r<R>(br0), to_r<R>(br1), R(0) };
-  R q[8];
-  mhd_constoprim<R>(u, bl, br, q, C, [&](double (&a)[3], double (&b)[3]) {
-    a[0] = bl0, a[1] = bl1, a[2] = bz;
-    b[0] = br0, b[1] = br1, b[2] = 0.0;
-  });
-  const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], cc = q[IC];
-  const R b2 = a * a + b * b + cc * cc;
-  R       cfx, cfy;
-  if constexpr (sizeof(R) == 4)
-  {
-    const float id = rcp_a(d), c2 = C.gamma0 * p * id;
-    const float d2 = 0.5f * (b2 * id + c2), cr = c2 * id;
-    cfx = sqrt_a(d2 + sqrt_a(d2 * d2 - cr * a * a));
-    cfy = sqrt_a(d2 + sqrt_a(d2 * d2 - cr * b * b));
-    return (cfx + fabsf(q[IU])) * P.idx + (cfy + fabsf(q[IV])) * P.idy;
-  }
-  else if constexpr (kShareRecip)
-  {
-    // FP64 FMA build: one reciprocal of the density, host-prepared 1/dx
-    const R id = R(1) / d, c2 = C.gamma0 * p * id;
-    const R d2 = R(0.5) * (b2 * id + c2), cr = c2 * id;
-    cfx = sqrt(d2 + sqrt(d2 * d2 - cr * a * a));
-    cfy = sqrt(d2 + sqrt(d2 * d2 - cr * b * b));
-    return (cfx + fabs(q[IU])) * P.idxd + (cfy + fabs(q[IV])) * P.idyd;
-  }
-  else
-  {
-    const R c2 = C.gamma0 * p / d;
-    const R d2 = R(0.5) * (b2 / d + c2);
-    cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d));
-    cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * b * b / d));
-    return (cfx + fabs(q[IU])) / P.dx + (cfy + fabs(q[IV])) / P.dy;
-  }
-}
-
 // ---------------------------------------------------------------------------
 // 1. CFL reduction of the step
 // ---------------------------------------------------------------------------
@@ -177,7 +131,42 @@ mhd2d_dt_kernel(const void * __restrict__ U, KParams P, DevClock * clk, int step
     const double bl0 = load_face<S>(m, P, s, 0), bl1 = load_face<S>(m, P, s, 1);
     const double br0 = load_face<S>(m, P, src_cell(P, i + 1, j, 0), 0);
     const double br1 = load_face<S>(m, P, src_cell(P, i, j + 1, 0), 1);
-    tmax = fmax(tmax, mhd2d_cell_invdt<R>(u, bl0, bl1, bz, br0, br1, C, P));
+    R            bl[3] = { to_r<R>(bl0), to_r<R>(bl1), to_r<R>(bz) };
+    R            br[3] = { to_r<R>(br0), to_r<R>(br1), R(0) };
+    R            q[8];
+    mhd_constoprim<R>(u, bl, br, q, C, [&](double (&a)[3], double (&b)[3]) {
+      a[0] = bl0, a[1] = bl1, a[2] = bz;
+      b[0] = br0, b[1] = br1, b[2] = 0.0;
+    });
+    // find_speed_info<TWO_D>: x and y only (mhd_utils.h:319-366)
+    const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], cc = q[IC];
+    const R b2 = a * a + b * b + cc * cc;
+    R       cfx, cfy;
+    if constexpr (sizeof(R) == 4)
+    {
+      const float id = rcp_a(d), c2 = C.gamma0 * p * id;
+      const float d2 = 0.5f * (b2 * id + c2), cr = c2 * id;
+      cfx = sqrt_a(d2 + sqrt_a(d2 * d2 - cr * a * a));
+      cfy = sqrt_a(d2 + sqrt_a(d2 * d2 - cr * b * b));
+      tmax = fmax(tmax, (cfx + fabsf(q[IU])) * P.idx + (cfy + fabsf(q[IV])) * P.idy);
+    }
+    else if constexpr (kShareRecip)
+    {
+      // FP64 FMA build: one reciprocal of the density, host-prepared 1/dx
+      const R id = R(1) / d, c2 = C.gamma0 * p * id;
+      const R d2 = R(0.5) * (b2 * id + c2), cr = c2 * id;
+      cfx = sqrt(d2 + sqrt(d2 * d2 - cr * a * a));
+      cfy = sqrt(d2 + sqrt(d2 * d2 - cr * b * b));
+      tmax = fmax(tmax, (cfx + fabs(q[IU])) * P.idxd + (cfy + fabs(q[IV])) * P.idyd);
+    }
+    else
+    {
+      const R c2 = C.gamma0 * p / d;
+      const R d2 = R(0.5) * (b2 / d + c2);
+      cfx = sqrt(d2 + sqrt(d2 * d2 - c2 * a * a / d));
+      cfy = sqrt(d2 + sqrt(d2 * d2 - c2 * b * b / d));
+      tmax = fmax(tmax, (cfx + fabs(q[IU])) / P.dx + (cfy + fabs(q[IV])) / P.dy);
+    }
   });
   block_max_commit<256>(cand_key((double)tmax), key ? key : &clk->key[step % 3]);
   if (!key)
@@ -319,7 +308,7 @@ trace2d_compact(const R * sQ, const R * sB, int qx, int qy, int bx, int by, R dt
 template <class S, class R, int TX, int TY, int RS>
 __global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_M2_MINB_F32, EK_M2_MINB_F64))
 mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KParams P, DevClock * clk,
-                  int step, int cfl_next)
+                  int step)
 {
   using T = Mhd2dTile<TX, TY>;
   constexpr int NT = TX * TY;
@@ -432,16 +421,7 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
   //    MHDRunFunctors2D.h:1572-1700), in the reference's order per variable
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   const int gi = i0 + tx, gj = j0 + ty;
-  const bool own = gi < ihi && gj < jhi;
-  // next step's CFL (cfl_next): the cells' final face fields, shared through
-  // the trace region (no longer read), and the tile's +1 column / row
-  double * sBxL = reinterpret_cast<double *>(smem_raw); // [TY][TX]
-  double * sByL = sBxL + NT;                            // [TY][TX]
-  double * sBxE = sByL + NT;                            // [TY]  Bx(i0 + TX)
-  double * sByE = sBxE + TY;                            // [TX]  By(j0 + TY)
-  R        ufin[5];
-  double   bxf = 0.0, byf = 0.0, bzf = 0.0;
-  if (own)
+  if (gi < ihi && gj < jhi)
   {
     const long long st = P.vstride;
     const long long off = (long long)gj * P.isize + gi;
@@ -502,64 +482,9 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
     bout[0 * st + off] = bx;
     bout[1 * st + off] = by;
     bout[2 * st + off] = bz;
-    if (cfl_next)
-    {
-#pragma unroll
-      for (int v = 0; v < 5; ++v)
-        ufin[v] = (R)(S)u[v];
-      bxf = bx, byf = by, bzf = bz;
-      // the face fields on the cell's high faces, as the next step's ghost
-      // fill leaves them: outflow copies the last interior face, a reflecting
-      // wall negates it, periodic (and the tile edge inside the domain) takes
-      // the CT update there, in the expressions above
-      auto high = [&](int bc, double own_face, double ct) {
-        return bc == BC_PERIODIC ? ct : (bc == BC_DIRICHLET ? -own_face : own_face);
-      };
-      if (tx == TX - 1 || gi + 1 == ihi)
-      {
-        double    b1 = gi + 1 == ihi ? load_face<S>(m, P, src_cell(P, gi + 1, gj, 0), 0) : m.b[0 * st + off + 1];
-        const R   a0 = sE[e0 + 1], a1 = sE[e0 + 1 + TX + 1];
-        if constexpr (sizeof(R) == 8)
-          b1 += (a1 - a0) * dtdy;
-        else
-          b1 = fma(f2d(a1) - f2d(a0), ddtdy, b1);
-        sBxE[ty] = gi + 1 == ihi ? high(P.bc[1], bx, b1) : b1;
-      }
-      if (ty == TY - 1 || gj + 1 == jhi)
-      {
-        double  b1 = gj + 1 == jhi ? load_face<S>(m, P, src_cell(P, gi, gj + 1, 0), 1) : m.b[1 * st + off + P.isize];
-        const R a0 = sE[e0 + TX + 1], a1 = sE[e0 + TX + 2];
-        if constexpr (sizeof(R) == 8)
-          b1 -= (a1 - a0) * dtdx;
-        else
-          b1 = fma(f2d(a0) - f2d(a1), ddtdx, b1);
-        sByE[tx] = gj + 1 == jhi ? high(P.bc[3], by, b1) : b1;
-      }
-    }
-  }
-  if (cfl_next)
-  {
-    // the trace region is free once every thread has passed phase D
-    if (own)
-    {
-      sBxL[ty * TX + tx] = bxf;
-      sByL[ty * TX + tx] = byf;
-    }
-    __syncthreads();
-    R tmax = R(-INFINITY);
-    if (own)
-    {
-      const int    c = ty * TX + tx;
-      const double br0 = tx + 1 < TX && gi + 1 < ihi ? sBxL[c + 1] : sBxE[ty];
-      const double br1 = ty + 1 < TY && gj + 1 < jhi ? sByL[c + TX] : sByE[tx];
-      tmax = mhd2d_cell_invdt<R>(ufin, bxf, byf, bzf, br0, br1, C, P);
-    }
-    block_max_commit<NT>(cand_key((double)tmax), &clk->key[(step + 1) % 3]);
   }
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
     step_commit(clk, step, t, dt);
-  if (cfl_next)
-    finalize_step(clk, P, step + 1); // the next step's dt, once its CFL key is complete
 }
 
 constexpr int M2_TX = EK_M2_TX, M2_TY = EK_M2_TY;
@@ -567,7 +492,7 @@ constexpr int M2_TX = EK_M2_TX, M2_TY = EK_M2_TY;
 template <class S, class R>
 cudaError_t
 mhd2d_step_t(int phase, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
-             bool cfl_next, cudaStream_t st)
+             cudaStream_t st)
 {
   if (phase == 0)
   {
@@ -582,24 +507,23 @@ mhd2d_step_t(int phase, const void * Uin, void * Uout, const KParams & P, DevClo
   if (e != cudaSuccess)
     return e;
   dim3 grid((P.nx + M2_TX - 1) / M2_TX, (P.ny + M2_TY - 1) / M2_TY, 1);
-  k<<<grid, M2_TX * M2_TY, sm, st>>>(Uin, Uout, P, clk, step, cfl_next ? 1 : 0);
+  k<<<grid, M2_TX * M2_TY, sm, st>>>(Uin, Uout, P, clk, step);
   return cudaGetLastError();
 }
 
-// one MHD 2D step = phase 0 (CFL), 1 (fused trace, fluxes, emf, update; with
-// cfl_next also the next step's CFL, so that step needs no phase 0)
+// one MHD 2D step = phase 0 (CFL), 1 (fused trace, fluxes, emf, update)
 cudaError_t
 mhd2d_step(int prec, int phase, const void * Uin, void * Uout, const KParams & P, DevClock * clk,
-           int step, bool cfl_next, cudaStream_t st)
+           int step, cudaStream_t st)
 {
 #ifdef EK_EXACT_ONLY
   if (prec != 0)
     return cudaErrorNotSupported;
-  return mhd2d_step_t<double, double>(phase, Uin, Uout, P, clk, step, cfl_next, st);
+  return mhd2d_step_t<double, double>(phase, Uin, Uout, P, clk, step, st);
 #else
   if (prec == 0)
-    return mhd2d_step_t<double, double>(phase, Uin, Uout, P, clk, step, cfl_next, st);
-  return mhd2d_step_t<float, float>(phase, Uin, Uout, P, clk, step, cfl_next, st);
+    return mhd2d_step_t<double, double>(phase, Uin, Uout, P, clk, step, st);
+  return mhd2d_step_t<float, float>(phase, Uin, Uout, P, clk, step, st);
 #endif
 }
 
