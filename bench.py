@@ -429,8 +429,8 @@ def main():
     ap.add_argument("--no-mhd2d", action="store_true")
     ap.add_argument("--mhd2d-n", type=int, default=4096)
     ap.add_argument("--no-mhd-blast", action="store_true")
-    ap.add_argument("--mhd-blast-n", type=int, default=256,
-                    help="grid of the low-beta MHD blast (512 = the configured grid; its FP64 run takes ~1 min)")
+    ap.add_argument("--mhd-blast-n", type=int, default=512,
+                    help="grid of the low-beta MHD blast (512, the configured grid: its FP64 runs take about a minute)")
     ap.add_argument("--mhd-blast-steps", type=int, default=30)
     ap.add_argument("--ens-n", type=int, default=512)
     ap.add_argument("--ens-steps", type=int, default=200)

@@ -153,8 +153,21 @@ mhd_speed_fast_f32(float d, float p, float a, float b, float c, float bn, float 
   return sqrt_a(d2 + sqrt_a(d2 * d2 - c2 * bn * bn * id));
 }
 
+// The star-state denominators of HLLD, estar = rho (S - u)(S - ustar) - Bn^2,
+// cancel as the state approaches the degenerate one (transverse field near
+// zero, fast speed near the Alfven speed).  In FP32 their quotients
+// (v*, B*, w*, C*) then lose all accuracy and a face flux can blow up the
+// solution; FP64 keeps them accurate, as the reference's FP64 build shows.
+// Below this fraction of Bn^2 (fewer than 7 significant bits left) the face is
+// recomputed in FP64.
+constexpr float kHlldStarTol = 1.0f / 128.0f;
+
+// false: a star-state denominator of this face is ill-conditioned in FP32
+// (|estar| < kHlldStarTol Bn^2), or the reference's degenerate-state test
+// |estar / Bn^2 - 1| <= 1e-8 cannot be decided in FP32; the caller then
+// computes the face in FP64 (flux is not written)
 template <int NF>
-__device__ __forceinline__ void
+__device__ __forceinline__ bool
 mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], float gamma0)
 {
   const float entho = rcp_a(gamma0 - 1.0f);
@@ -184,6 +197,15 @@ mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], floa
   const float ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc;
   const float ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc;
   const float ia2 = rcp_a(a2);
+  {
+    const float el_ = rl * (sl - ul) * (sl - ustar) - a2;
+    const float er_ = rr * (sr - ur) * (sr - ustar) - a2;
+    auto ill = [&](float e) {
+      return fabsf(e) < kHlldStarTol * a2 || (a2 > 0.f && fabsf(e * ia2 - 1.f) <= 1e-6f);
+    };
+    if (ill(el_) || ill(er_))
+      return false;
+  }
 
   const float isl = rcp_a(sl - ustar);
   const float rstarl = rl * (sl - ul) * isl;
@@ -278,6 +300,32 @@ mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], floa
   flux[IW] = ro * uo * wo - a * co;
   if constexpr (NF > 5)
     flux[5] = co * uo - a * wo;
+  return true;
+}
+
+template <class R, int NF>
+__device__ __forceinline__ void
+mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0);
+
+// FP64 island of the FP32 HLLD: a star-state denominator cancels in FP32, so
+// the face is solved in FP64 from the same FP32 states (conversions on the
+// integer pipes, exact).  Out of line: the rare call keeps its FP64 registers
+// out of the calling kernel's hot path.
+template <int NF>
+__device__ __noinline__ void
+mhd_hlld_f64_island(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], float gamma0)
+{
+  double l[8], r[8], f[NF];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+  {
+    l[i] = f2d(ql[i]);
+    r[i] = f2d(qr[i]);
+  }
+  mhd_hlld<double, NF>(l, r, f, f2d(gamma0));
+#pragma unroll
+  for (int i = 0; i < NF; ++i)
+    flux[i] = d2f_rn(f[i]);
 }
 
 // riemann_hlld (RiemannSolvers_MHD.h:130-364), states in the face frame.
@@ -289,7 +337,8 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
 {
   if constexpr (sizeof(R) == 4)
   {
-    mhd_hlld_f32<NF>(ql, qr, flux, gamma0);
+    if (!mhd_hlld_f32<NF>(ql, qr, flux, gamma0))
+      mhd_hlld_f64_island<NF>(ql, qr, flux, gamma0);
     return;
   }
   else
