@@ -56,8 +56,8 @@ HEADLINE = "3D MHD Orszag-Tang %d^3 on [0,1]^3, MHD_Muscl_3D, HLLD + CT, slope_t
 KERNEL_NAMES = {
     "hydro3d": ((0, "hydro3d_step"),),
     "hydro2d": ((0, "hydro2d_step"),),
-    "mhd3d": ((2, "mhd_dt_kernel"), (1, "mhd_trace_kernel"), (0, "mhd_update_kernel")),
-    "mhd2d": ((2, "mhd2d_dt_kernel"), (0, "mhd2d_step_kernel")),
+    "mhd3d": ((2, "mhd_dt_kernel"), (1, "mhd_trace_kernel"), (0, "mhd_update_kernel"), (3, "mhd_repair_kernel")),
+    "mhd2d": ((2, "mhd2d_dt_kernel"), (0, "mhd2d_step_kernel"), (3, "mhd2d_repair_kernel")),
 }
 
 # DRAM bytes (read + write) per interior cell of one launch of each kernel,
@@ -69,8 +69,12 @@ TRAFFIC_PER_CELL = {
     ("hydro3d", "fp64"): {"hydro3d_step": 78.2},    # 306.3 + 247.4 MB / 7.08 M cells
     ("mhd3d", "mixed"): {"mhd_dt_kernel": 46.0,      # 323 + 3 MB / 7.08 M cells (first step only)
                          "mhd_trace_kernel": 243.0,  # 375.4 + 1345.0 MB / 7.08 M cells
-                         "mhd_update_kernel": 338.2},  # 2063.4 + 331.1 MB / 7.08 M cells
-    ("mhd2d", "mixed"): {"mhd2d_step_kernel": 78.1},  # 186.4 + 141.0 MB / 4.19 M cells
+                         "mhd_update_kernel": 338.2,  # 2063.4 + 331.1 MB / 7.08 M cells
+                         # with no tile listed (the Orszag-Tang steps) the
+                         # repair kernel reads the list head only
+                         "mhd_repair_kernel": 0.0},
+    ("mhd2d", "mixed"): {"mhd2d_step_kernel": 78.1,  # 186.4 + 141.0 MB / 4.19 M cells
+                         "mhd2d_repair_kernel": 0.0},
 }
 
 # Floating-point operations per cell-update of the reference algorithm
@@ -194,9 +198,12 @@ def measure_workload(ek, kind, prec, ini, U0, steps, warmup, sync, profile=True)
             s.set_profiling(True)
             s.run(steps)
             s.synchronize()
-            k = {i: s.kernel_time(i) for i in range(3)}
+            k = {i: s.kernel_time(i) for i in range(4)}
             out["kernels"] = {i: (v[0] / v[1] if v[1] else None, v[1]) for i, v in k.items()}
             s.set_profiling(False)
+        # tiles the mixed HLLD form's repair kernel recomputed (warm-up, timed
+        # and profiled steps)
+        out["hlld_repaired_tiles"] = s.hlld_repairs()
         out["U"] = s.get_state()
         out["totals"] = s.totals()
         out["iteration"] = s.m_iteration
@@ -646,6 +653,8 @@ def main():
                 Ub = s.get_state()
                 res[name] = (Ub[:2, 3:-3, 3:-3, 3:-3].copy(), s.totals(), s.dt_history())
                 inner[name] = divb_inner(Ub, 3, 4, pb.dx, pb.dy, pb.dz)
+                if name == "mixed":
+                    repaired = s.hlld_repairs()
                 del Ub
             sync()
         (ab, totb, dtb), (bb, totb64, dtb64) = res["mixed"], res["fp64"]
@@ -659,6 +668,9 @@ def main():
             "error_after_steps": len(dtb),
             "l1_rel_err_rho_E_mixed_vs_fp64": l1b, "linf_rel_err_rho_E_mixed_vs_fp64": linfb,
             "max_rel_dt_diff": float(np.abs(dtb / dtb64 - 1).max()),
+            "hlld_repaired_tiles": {"error_run": repaired, "timed_runs": mb["hlld_repaired_tiles"],
+                                    "note": "tiles recomputed by the repair kernel (faces with ill-conditioned "
+                                            "FP32 HLLD star states solved in FP64)"},
             "max_divB_mixed": float(totb[2]), "max_divB_fp64": float(totb64[2]),
             "max_divB_inner_mixed": inner["mixed"], "max_divB_inner_fp64": inner["fp64"],
             "divB_note": "max over all interior cells, and over the cells 4 or more cells inside "
@@ -685,6 +697,7 @@ def main():
             "value_mixed": v2, "value_fp64": v264, "unit": UNIT, "mixed_over_fp64": v2 / v264,
             "ms_per_step_mixed": m2["ms"] / m2["steps"], "ms_per_step_fp64": m264["ms"] / m264["steps"],
             "l1_rel_err_rho_mixed_vs_fp64": float(np.abs(a2 - b2).sum() / np.abs(b2).sum()),
+            "hlld_repaired_tiles": m2["hlld_repaired_tiles"],
             "max_divB_mixed": float(m2["totals"][2]), "max_divB_fp64": float(m264["totals"][2]),
             "roofline_mixed": roofline(m2, ("mhd2d", "mixed")),
             "roofline_fp64": roofline(m264, ("mhd2d", "fp64")),
@@ -734,6 +747,7 @@ def main():
             },
             "mixed_over_fp64": value / v64,
             "accuracy": accuracy,
+            "hlld_repaired_tiles": mixed["hlld_repaired_tiles"],
             "roofline": roofline(mixed, ("mhd3d", "mixed")),
             "reference_formula_mcell_s": mixed["ghost_cells"] * mixed["steps"] / (ms_mixed / 1e3) / 1e6 * world,
             "cpu_baseline": cpu,

@@ -167,6 +167,7 @@ def load_library():
         "ek_solver_set_profiling": (ctypes.c_int, [c_p, ctypes.c_int]),
         "ek_solver_kernel_time": (ctypes.c_int, [c_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                                  ctypes.POINTER(ctypes.c_longlong)]),
+        "ek_solver_hlld_repairs": (ctypes.c_int, [c_p, ctypes.POINTER(ctypes.c_longlong)]),
         "ek_ensemble_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int, ctypes.POINTER(c_p)]),
         "ek_ensemble_destroy": (ctypes.c_int, [c_p]),
         "ek_ensemble_set_state": (ctypes.c_int, [c_p, ctypes.c_int, c_p, ctypes.c_int]),
@@ -404,6 +405,14 @@ class Solver:
         ms, n = ctypes.c_double(), ctypes.c_longlong()
         _check(self._L.ek_solver_kernel_time(self._h, kernel, ctypes.byref(ms), ctypes.byref(n)), "kernel_time")
         return ms.value, n.value
+
+    def hlld_repairs(self) -> int:
+        """Tiles recomputed by the mixed HLLD form's repair kernel (faces with
+        ill-conditioned FP32 star states solved in FP64) since the state was
+        set; 0 for the other forms."""
+        n = ctypes.c_longlong()
+        _check(self._L.ek_solver_hlld_repairs(self._h, ctypes.byref(n)), "hlld_repairs")
+        return n.value
 
 
 class Ensemble:

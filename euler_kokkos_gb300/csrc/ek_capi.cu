@@ -69,12 +69,21 @@ struct ek_solver
   bool                     profiling = false;
   std::vector<cudaEvent_t> ev_pool;            // recycled events
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
-  double                   kernel_ms[3] = { 0, 0, 0 };
-  long long                kernel_n[3] = { 0, 0, 0 };
+  double                   kernel_ms[4] = { 0, 0, 0, 0 };
+  long long                kernel_n[4] = { 0, 0, 0, 0 };
   bool                     owns = true; // false: a view into an ensemble's buffers
   // 3D MHD: the step whose CFL the last update kernel computed (-1: none)
   int                      cfl_step = -1;
 };
+
+// The mixed MHD form with the HLLD solver: each step ends with the repair pass
+// (the tiles whose FP32 star states were ill-conditioned, recomputed with
+// those faces in FP64); its tile list heads the work buffer.
+static bool
+has_repair(const ek_solver * s)
+{
+  return s->p.mhd && s->prec != 0 && s->kp.riemann == 4;
+}
 
 static cudaEvent_t
 take_event(ek_solver * s)
@@ -320,9 +329,12 @@ ek_solver_create(const ek_params * params, ek_solver ** out)
     e = cudaMalloc((void **)&s->dtlog, sizeof(double) * s->dtcap);
   if (e == cudaSuccess)
     e = cudaMalloc((void **)&s->scratch3, 3 * sizeof(double));
-  if (e == cudaSuccess && p.mhd && p.dim == 3)
+  if (e == cudaSuccess && p.mhd)
   {
-    s->work_bytes = s->exact ? ek_exact::mhd_work_bytes(s->prec, k) : ek_fast::mhd_work_bytes(s->prec, k);
+    if (p.dim == 3)
+      s->work_bytes = s->exact ? ek_exact::mhd_work_bytes(s->prec, k) : ek_fast::mhd_work_bytes(s->prec, k);
+    else
+      s->work_bytes = s->exact ? ek_exact::mhd2d_work_bytes(s->prec, k) : ek_fast::mhd2d_work_bytes(s->prec, k);
     if (s->work_bytes)
       e = cudaMalloc(&s->work, s->work_bytes);
   }
@@ -510,6 +522,9 @@ reset_clock(ek_solver * s, double t0)
   h.dtcap = s->dtcap;
   s->cfl_step = -1;
   EK_CUDA(cudaMemcpyAsync(s->clk, &h, sizeof h, cudaMemcpyHostToDevice, s->stream), "clock reset");
+  // an empty repair list and its tile counter
+  if (has_repair(s))
+    EK_CUDA(cudaMemsetAsync(s->work, 0, 4 * sizeof(int), s->stream), "clock reset");
   // hydro: slot 0 holds the CFL of the initial state (the constructor's
   // compute_dt()); MHD recomputes dt inside every step
   if (!s->p.mhd)
@@ -757,8 +772,8 @@ launch_one(ek_solver * s, int kernel_id, int phase, int step)
   }
   cudaError_t e;
   if (s->p.mhd && s->p.dim == 2)
-    e = s->exact ? ek_exact::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, s->stream)
-                 : ek_fast::mhd2d_step(s->prec, phase, in, outp, s->kp, s->clk, step, s->stream);
+    e = s->exact ? ek_exact::mhd2d_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream)
+                 : ek_fast::mhd2d_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, s->stream);
   else if (s->p.mhd)
     e = s->exact ? ek_exact::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, true, s->stream)
                  : ek_fast::mhd_step(s->prec, phase, in, outp, s->work, s->kp, s->clk, step, true, s->stream);
@@ -790,6 +805,8 @@ launch_step(ek_solver * s, int step)
     ek_status st = launch_one(s, 2, 0, step); // CFL of the step
     if (st == EK_OK)
       st = launch_one(s, 0, 1, step); // trace, fluxes, emf, update
+    if (st == EK_OK && has_repair(s))
+      st = launch_one(s, 3, 2, step); // the listed tiles with FP64 star states
     return st;
   }
   // CFL of the step: only when no update kernel computed it (the first step
@@ -801,6 +818,8 @@ launch_step(ek_solver * s, int step)
     st = launch_one(s, 1, 1, step); // trace
   if (st == EK_OK)
     st = launch_one(s, 0, 2, step); // fluxes, emfs, update, and the next step's CFL
+  if (st == EK_OK && has_repair(s))
+    st = launch_one(s, 3, 3, step); // the listed tiles with FP64 star states; completes the CFL
   s->cfl_step = st == EK_OK ? step + 1 : -1;
   return st;
 }
@@ -1058,7 +1077,7 @@ ek_solver_set_profiling(ek_solver * s, int enable)
     return fail(EK_ERR_INVALID, "ek_solver_set_profiling: null solver");
   drain_events(s);
   s->profiling = enable != 0;
-  for (int i = 0; i < 3; ++i)
+  for (int i = 0; i < 4; ++i)
   {
     s->kernel_ms[i] = 0.0;
     s->kernel_n[i] = 0;
@@ -1069,13 +1088,30 @@ ek_solver_set_profiling(ek_solver * s, int enable)
 extern "C" ek_status
 ek_solver_kernel_time(ek_solver * s, int kernel, double * total_ms, long long * launches)
 {
-  if (!s || kernel < 0 || kernel > 2)
+  if (!s || kernel < 0 || kernel > 3)
     return fail(EK_ERR_INVALID, "ek_solver_kernel_time: bad argument");
   drain_events(s);
   if (total_ms)
     *total_ms = s->kernel_ms[kernel];
   if (launches)
     *launches = s->kernel_n[kernel];
+  return EK_OK;
+}
+
+extern "C" ek_status
+ek_solver_hlld_repairs(ek_solver * s, long long * tiles)
+{
+  if (!s || !tiles)
+    return fail(EK_ERR_INVALID, "ek_solver_hlld_repairs: bad argument");
+  *tiles = 0;
+  if (!has_repair(s))
+    return EK_OK;
+  unsigned long long n = 0;
+  EK_CUDA(cudaMemcpyAsync(&n, static_cast<char *>(s->work) + 2 * sizeof(int), sizeof n, cudaMemcpyDeviceToHost,
+                          s->stream),
+          "hlld repairs");
+  EK_CUDA(cudaStreamSynchronize(s->stream), "hlld repairs");
+  *tiles = (long long)n;
   return EK_OK;
 }
 

@@ -23,13 +23,16 @@
   cudaError_t mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key,         \
                      cudaStream_t st);                                                              \
   /* one MHD step = phase 0 (CFL), 1 (trace), 2 (fluxes, emfs, update; cfl_next: and the     */ \
-  /* CFL of the updated state, the next step's dt, so its phase 0 is not needed) */               \
+  /* CFL of the updated state, the next step's dt, so its phase 0 is not needed), 3 (the      */ \
+  /* repair pass of the mixed HLLD form, which then must follow phase 2) */                      \
   cudaError_t mhd_step(int prec, int phase, const void * Uin, void * Uout, void * work,             \
                        const KParams & P, DevClock * clk, int step, bool cfl_next, cudaStream_t st); \
   size_t      mhd_work_bytes(int prec, const KParams & P);                                          \
-  /* one MHD 2D step = phase 0 (CFL), 1 (fused trace, fluxes, emf, update) */                      \
-  cudaError_t mhd2d_step(int prec, int phase, const void * Uin, void * Uout, const KParams & P,     \
-                         DevClock * clk, int step, cudaStream_t st);                                \
+  /* one MHD 2D step = phase 0 (CFL), 1 (fused trace, fluxes, emf, update), 2 (the repair   */ \
+  /* pass of the mixed HLLD form, which then must follow phase 1) */                               \
+  cudaError_t mhd2d_step(int prec, int phase, const void * Uin, void * Uout, void * work,           \
+                         const KParams & P, DevClock * clk, int step, cudaStream_t st);             \
+  size_t      mhd2d_work_bytes(int prec, const KParams & P);                                        \
   cudaError_t mhd2d_dt(int prec, const void * U, const KParams & P, unsigned long long * key,       \
                        cudaStream_t st);                                                            \
   /* one step of every instance of a 2D hydro ensemble (persistent kernel) */                       \

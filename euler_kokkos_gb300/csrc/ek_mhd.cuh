@@ -158,9 +158,12 @@ mhd_speed_fast_f32(float d, float p, float a, float b, float c, float bn, float 
 // zero, fast speed near the Alfven speed).  In FP32 their quotients
 // (v*, B*, w*, C*) then lose all accuracy and a face flux can blow up the
 // solution; FP64 keeps them accurate, as the reference's FP64 build shows.
-// Below this fraction of Bn^2 (fewer than 7 significant bits left) the face is
-// recomputed in FP64.
-constexpr float kHlldStarTol = 1.0f / 128.0f;
+// Below this fraction of Bn^2 the face is recomputed in FP64: FP32 rounding
+// leaves estar an absolute error of a few 1e-7 Bn^2, so above the threshold the
+// quotients keep a relative accuracy of about 1e-2 or better.  (A threshold of
+// 2^-7 sent a few per cent of the Orszag-Tang faces, where the transverse
+// field crosses zero, to FP64 and cost 10-45 % of the MHD step.)
+constexpr float kHlldStarTol = 1.0f / 16384.0f;
 
 // false: a star-state denominator of this face is ill-conditioned in FP32
 // (|estar| < kHlldStarTol Bn^2), or the reference's degenerate-state test
@@ -303,44 +306,18 @@ mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], floa
   return true;
 }
 
-template <class R, int NF>
-__device__ __forceinline__ void
-mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0);
-
-// FP64 island of the FP32 HLLD: a star-state denominator cancels in FP32, so
-// the face is solved in FP64 from the same FP32 states (conversions on the
-// integer pipes, exact).  Out of line: the rare call keeps its FP64 registers
-// out of the calling kernel's hot path.
-template <int NF>
-__device__ __noinline__ void
-mhd_hlld_f64_island(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], float gamma0)
-{
-  double l[8], r[8], f[NF];
-#pragma unroll
-  for (int i = 0; i < 8; ++i)
-  {
-    l[i] = f2d(ql[i]);
-    r[i] = f2d(qr[i]);
-  }
-  mhd_hlld<double, NF>(l, r, f, f2d(gamma0));
-#pragma unroll
-  for (int i = 0; i < NF; ++i)
-    flux[i] = d2f_rn(f[i]);
-}
-
 // riemann_hlld (RiemannSolvers_MHD.h:130-364), states in the face frame.
 // The 3D update uses the five hydro components of the flux (NF = 5); the 2D
 // update also uses the Bz component, returned in flux[5] when NF = 6.
+// Returns false when the FP32 solver leaves the face to its FP64 island (an
+// ill-conditioned star state, see mhd_hlld_f32): the caller then solves it
+// with mhd_hlld<double> from the same states.
 template <class R, int NF = 5>
-__device__ __forceinline__ void
+__device__ __forceinline__ bool
 mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
 {
   if constexpr (sizeof(R) == 4)
-  {
-    if (!mhd_hlld_f32<NF>(ql, qr, flux, gamma0))
-      mhd_hlld_f64_island<NF>(ql, qr, flux, gamma0);
-    return;
-  }
+    return mhd_hlld_f32<NF>(ql, qr, flux, gamma0);
   else
   {
   const R entho = R(1.0) / (gamma0 - R(1.0));
@@ -503,13 +480,14 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   flux[IW] = ro * uo * wo - a * co;
   if constexpr (NF > 5)
     flux[5] = co * uo - a * wo;
+  return true;
   }
 }
 
 // riemann_mhd (RiemannSolvers_MHD.h:368-389) with the solver fixed at compile
 // time: RS = the reference's riemannSolverType (1 llf, 2 hll, 4 hlld)
 template <int RS, class R, int NF>
-__device__ __forceinline__ void
+__device__ __forceinline__ bool
 mhd_riemann(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0);
 
 // find_mhd_flux (mhd_utils.h:170-231, cIso = 0): conservative state and
@@ -582,8 +560,9 @@ mhd_llf(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
     flux[v] -= vel_info * (uright[v] - uleft[v]) / R(2);
 }
 
+// false: the FP32 HLLD left this face to its FP64 island (mhd_riemann_f64)
 template <int RS, class R, int NF>
-__device__ __forceinline__ void
+__device__ __forceinline__ bool
 mhd_riemann(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
 {
   if constexpr (RS == 1)
@@ -591,7 +570,44 @@ mhd_riemann(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   else if constexpr (RS == 2)
     mhd_hll<R, NF>(ql, qr, flux, gamma0);
   else
-    mhd_hlld<R, NF>(ql, qr, flux, gamma0);
+    return mhd_hlld<R, NF>(ql, qr, flux, gamma0);
+  return true;
+}
+
+// The FP64 island of the FP32 HLLD: the face solved in FP64 from the same
+// FP32 face states (exact conversions).  Only the repair kernels call it, for
+// the faces the FP32 solver declined; the step kernels hold no FP64 HLLD code,
+// which would raise their register count (a 64-register 2D step kernel went
+// to 126) or spill inside their hot loops.  Out of line, states and flux by
+// value.
+struct HlldFlux32
+{
+  float f[6];
+};
+template <int NF>
+__device__ __noinline__ HlldFlux32
+mhd_hlld_f64_island(float4 l0, float4 l1, float4 r0, float4 r1, float gamma0)
+{
+  double l[8] = { f2d(l0.x), f2d(l0.y), f2d(l0.z), f2d(l0.w), f2d(l1.x), f2d(l1.y), f2d(l1.z), f2d(l1.w) };
+  double r[8] = { f2d(r0.x), f2d(r0.y), f2d(r0.z), f2d(r0.w), f2d(r1.x), f2d(r1.y), f2d(r1.z), f2d(r1.w) };
+  double f[NF];
+  mhd_hlld<double, NF>(l, r, f, f2d(gamma0));
+  HlldFlux32 out;
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+    out.f[i] = i < NF ? d2f_rn(f[i < NF ? i : 0]) : 0.f;
+  return out;
+}
+template <int NF>
+__device__ __forceinline__ void
+mhd_hlld_f64_from_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], float gamma0)
+{
+  const HlldFlux32 o = mhd_hlld_f64_island<NF>(make_float4(ql[0], ql[1], ql[2], ql[3]), make_float4(ql[4], ql[5], ql[6], ql[7]),
+                                               make_float4(qr[0], qr[1], qr[2], qr[3]), make_float4(qr[4], qr[5], qr[6], qr[7]),
+                                               gamma0);
+#pragma unroll
+  for (int i = 0; i < NF; ++i)
+    flux[i] = o.f[i];
 }
 
 template <class R>

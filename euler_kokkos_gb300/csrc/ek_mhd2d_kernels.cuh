@@ -305,10 +305,16 @@ trace2d_compact(const R * sQ, const R * sB, int qx, int qy, int bx, int by, R dt
     out[f * ost] = o[f];
 }
 
-template <class S, class R, int TX, int TY, int RS>
-__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_M2_MINB_F32, EK_M2_MINB_F64))
-mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KParams P, DevClock * clk,
-                  int step)
+// One tile of the step: the cells [i0, i0+TX) x [j0, j0+TY) of tile (bx, by),
+// written from the step's input state only.  REPAIR: the faces whose FP32
+// HLLD star state is ill-conditioned are solved in FP64 (the repair kernel);
+// otherwise such a face lists the tile for that kernel (repair list as in
+// the 3D update kernel: [0] count, [1] blocks done, [2..3] tiles repaired,
+// [4..] tiles).
+template <class S, class R, int TX, int TY, int RS, bool REPAIR>
+__device__ __forceinline__ void
+mhd2d_tile(const void * __restrict__ Uin, void * __restrict__ Uout, const KParams & P, const StepConsts & sc,
+           int bx, int by, int * repair)
 {
   using T = Mhd2dTile<TX, TY>;
   constexpr int NT = TX * TY;
@@ -320,16 +326,12 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
   R * sFy = sFx + 6 * T::FXS;               // [6][TY+1][TX]  y fluxes
   R * sE = sFy + 6 * T::FYS;                // [TY+1][TX+1]   z-edge emf
 
-  StepConsts sc;
-  if (!step_consts(clk, step, sc))
-    return;
-  const double      t = sc.t, dt = sc.dt;
   const R           dtdx = to_r<R>(sc.dtdx), dtdy = to_r<R>(sc.dtdy);
   const double      ddtdx = sc.dtdx, ddtdy = sc.dtdy; // FP64 ratios of the face-field update
   const MhdConst<R> C = mhd_const<R>(P);
   const MhdState<S> m = mhd_state<S>(Uin, P);
   const int         gw = P.gw;
-  const int         i0 = gw + blockIdx.x * TX, j0 = gw + blockIdx.y * TY;
+  const int         i0 = gw + bx * TX, j0 = gw + by * TY;
 
   // A. face fields IA, IB of cells [i0-2, i0+TX+2] x [j0-2, j0+TY+2]
   for (int c = threadIdx.x; c < T::BX * T::BY; c += NT)
@@ -381,27 +383,47 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
   const int ihi = P.nx + gw, jhi = P.ny + gw;
   auto      TS = [&](int gi, int gj) { return sT + (gj - (j0 - 1)) * T::XE + (gi - (i0 - 1)); };
   constexpr int NF = T::FXS + T::FYS, NFP = (NF + 31) & ~31;
+  // mixed HLLD: a face whose FP32 star state is ill-conditioned marks the tile
+  constexpr bool kFlag = sizeof(R) == 4 && RS == 4 && !REPAIR;
+  __shared__ int s_dirty;
+  if (threadIdx.x == 0)
+    s_dirty = 0;
+  __syncthreads();
+  // face work item w (x faces, then y faces)
+  auto face = [&](int w) {
+    const int d = w < T::FXS ? 0 : 1;
+    const int f = d == 0 ? w : w - T::FXS;
+    const int ex = TX + (d == 0 ? 1 : 0);
+    const int i = i0 + f % ex, j = j0 + f / ex;
+    if (i > ihi - (d != 0 ? 1 : 0) || j > jhi - (d != 1 ? 1 : 0))
+      return;
+    R ql[8], qr[8], fl[6];
+    face2d_state<R, true>(TS(i - (d == 0), j - (d == 1)), T::PL, d, ql, sr, sp);
+    face2d_state<R, false>(TS(i, j), T::PL, d, qr, sr, sp);
+    if (!mhd_riemann<RS, R, 6>(ql, qr, fl, C.gamma0))
+    {
+      // ill-conditioned star state in FP32 (mixed HLLD only)
+      if constexpr (REPAIR)
+        mhd_hlld_f64_from_f32<6>(ql, qr, fl, C.gamma0);
+      else
+      {
+        s_dirty = 1;
+        return;
+      }
+    }
+    R *       dst = d == 0 ? sFx : sFy;
+    const int nd = d == 0 ? T::FXS : T::FYS;
+#pragma unroll
+    for (int v = 0; v < 6; ++v)
+      dst[v * nd + f] = fl[v];
+  };
   for (int w = threadIdx.x; w < NFP + T::EZS; w += NT)
   {
     if (w < NFP)
     {
       if (w >= NF)
         continue;
-      const int d = w < T::FXS ? 0 : 1;
-      const int f = d == 0 ? w : w - T::FXS;
-      const int ex = TX + (d == 0 ? 1 : 0);
-      const int i = i0 + f % ex, j = j0 + f / ex;
-      if (i > ihi - (d != 0 ? 1 : 0) || j > jhi - (d != 1 ? 1 : 0))
-        continue;
-      R ql[8], qr[8], fl[6];
-      face2d_state<R, true>(TS(i - (d == 0), j - (d == 1)), T::PL, d, ql, sr, sp);
-      face2d_state<R, false>(TS(i, j), T::PL, d, qr, sr, sp);
-      mhd_riemann<RS, R, 6>(ql, qr, fl, C.gamma0);
-      R *       dst = d == 0 ? sFx : sFy;
-      const int nd = d == 0 ? T::FXS : T::FYS;
-#pragma unroll
-      for (int v = 0; v < 6; ++v)
-        dst[v * nd + f] = fl[v];
+      face(w);
       continue;
     }
     // z edge at the low corner of cell (i,j): RT(i-1,j-1), RB(i-1,j), LT(i,j-1), LB(i,j)
@@ -416,7 +438,6 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
     sE[f] = mhd_emf_corners<R>(cRT, cRB, cLT, cLB, C.gamma0, C.smallc);
   }
   __syncthreads();
-
   // E. update (UpdateFunctor2D_MHD then UpdateEmfFunctor2D,
   //    MHDRunFunctors2D.h:1572-1700), in the reference's order per variable
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
@@ -483,21 +504,83 @@ mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KPara
     bout[1 * st + off] = by;
     bout[2 * st + off] = bz;
   }
+  // s_dirty was last written before the barrier that ends phase D
+  if (kFlag && threadIdx.x == 0 && s_dirty)
+    repair[kRepairHead + atomicAdd(&repair[0], 1)] = by * ((P.nx + TX - 1) / TX) + bx;
+}
+
+// One launch per step: the tiles of the grid.  repair: the tile list of the
+// mixed HLLD form (null otherwise), for the repair kernel that follows.
+template <class S, class R, int TX, int TY, int RS>
+__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_M2_MINB_F32, EK_M2_MINB_F64))
+mhd2d_step_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KParams P, DevClock * clk,
+                  int step, int * repair)
+{
+  StepConsts sc;
+  if (!step_consts(clk, step, sc))
+    return;
+  mhd2d_tile<S, R, TX, TY, RS, false>(Uin, Uout, P, sc, blockIdx.x, blockIdx.y, repair);
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
-    step_commit(clk, step, t, dt);
+    step_commit(clk, step, sc.t, sc.dt);
+}
+
+// After the step kernel of the mixed HLLD form: recomputes the tiles it
+// listed with the ill-conditioned faces solved in FP64 (tiles are independent
+// within a step, so this replaces their output), then clears the list.
+template <class S, class R, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_M2_MINB_F32, EK_M2_MINB_F64))
+mhd2d_repair_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, KParams P, DevClock * clk,
+                    int step, int * repair)
+{
+  StepConsts sc;
+  if (!step_consts(clk, step, sc))
+    return;
+  const int n = repair[0];
+  const int gx = (P.nx + TX - 1) / TX;
+  for (int e = blockIdx.x; e < n; e += gridDim.x)
+  {
+    const int tile = repair[kRepairHead + e];
+    mhd2d_tile<S, R, TX, TY, 4, true>(Uin, Uout, P, sc, tile % gx, tile / gx, repair);
+    __syncthreads(); // shared memory of the next tile
+  }
+  repair_list_release(repair);
 }
 
 constexpr int M2_TX = EK_M2_TX, M2_TY = EK_M2_TY;
 
+inline long long
+mhd2d_tiles(const KParams & P)
+{
+  return (long long)((P.nx + M2_TX - 1) / M2_TX) * ((P.ny + M2_TY - 1) / M2_TY);
+}
+
 template <class S, class R>
 cudaError_t
-mhd2d_step_t(int phase, const void * Uin, void * Uout, const KParams & P, DevClock * clk, int step,
-             cudaStream_t st)
+mhd2d_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams & P, DevClock * clk,
+             int step, cudaStream_t st)
 {
   if (phase == 0)
   {
     mhd2d_dt_kernel<S, R><<<row_blocks(P), 256, 0, st>>>(Uin, P, clk, step, nullptr);
     return cudaGetLastError();
+  }
+  // the repair pass of the mixed HLLD form (after phase 1)
+  if (phase == 2)
+  {
+    if constexpr (sizeof(R) == 8)
+      return cudaErrorNotSupported;
+    else
+    {
+      if (P.riemann != 4)
+        return cudaErrorNotSupported;
+      auto        k = mhd2d_repair_kernel<S, R, M2_TX, M2_TY>;
+      const int   sm = (int)mhd2d_smem<R>(M2_TX, M2_TY);
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      if (e != cudaSuccess)
+        return e;
+      k<<<repair_grid(mhd2d_tiles(P)), M2_TX * M2_TY, sm, st>>>(Uin, Uout, P, clk, step, (int *)work);
+      return cudaGetLastError();
+    }
   }
   auto k = P.riemann == 1   ? mhd2d_step_kernel<S, R, M2_TX, M2_TY, 1>
            : P.riemann == 2 ? mhd2d_step_kernel<S, R, M2_TX, M2_TY, 2>
@@ -506,24 +589,34 @@ mhd2d_step_t(int phase, const void * Uin, void * Uout, const KParams & P, DevClo
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   if (e != cudaSuccess)
     return e;
-  dim3 grid((P.nx + M2_TX - 1) / M2_TX, (P.ny + M2_TY - 1) / M2_TY, 1);
-  k<<<grid, M2_TX * M2_TY, sm, st>>>(Uin, Uout, P, clk, step);
+  dim3  grid((P.nx + M2_TX - 1) / M2_TX, (P.ny + M2_TY - 1) / M2_TY, 1);
+  int * repair = sizeof(R) == 4 && P.riemann == 4 ? (int *)work : nullptr;
+  k<<<grid, M2_TX * M2_TY, sm, st>>>(Uin, Uout, P, clk, step, repair);
   return cudaGetLastError();
 }
 
-// one MHD 2D step = phase 0 (CFL), 1 (fused trace, fluxes, emf, update)
+// the repair pass's tile list of the mixed form (cleared by the caller before
+// the first step)
+size_t
+mhd2d_work_bytes(int prec, const KParams & P)
+{
+  return prec == 0 ? 0 : sizeof(int) * (size_t)(kRepairHead + mhd2d_tiles(P));
+}
+
+// one MHD 2D step = phase 0 (CFL), 1 (fused trace, fluxes, emf, update),
+// 2 (the repair pass, mixed HLLD form)
 cudaError_t
-mhd2d_step(int prec, int phase, const void * Uin, void * Uout, const KParams & P, DevClock * clk,
+mhd2d_step(int prec, int phase, const void * Uin, void * Uout, void * work, const KParams & P, DevClock * clk,
            int step, cudaStream_t st)
 {
 #ifdef EK_EXACT_ONLY
   if (prec != 0)
     return cudaErrorNotSupported;
-  return mhd2d_step_t<double, double>(phase, Uin, Uout, P, clk, step, st);
+  return mhd2d_step_t<double, double>(phase, Uin, Uout, work, P, clk, step, st);
 #else
   if (prec == 0)
-    return mhd2d_step_t<double, double>(phase, Uin, Uout, P, clk, step, st);
-  return mhd2d_step_t<float, float>(phase, Uin, Uout, P, clk, step, st);
+    return mhd2d_step_t<double, double>(phase, Uin, Uout, work, P, clk, step, st);
+  return mhd2d_step_t<float, float>(phase, Uin, Uout, work, P, clk, step, st);
 #endif
 }
 

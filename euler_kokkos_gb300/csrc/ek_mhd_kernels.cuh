@@ -641,10 +641,26 @@ struct UpdTile
   static constexpr int EZS = (TX + 1) * (TY + 1), EYS = (TX + 1) * TY, EXS = TX * (TY + 1);
 };
 
-template <class S, class R, int TX, int TY, bool STAGE, int RS>
-__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_MU_MINB_F32, EK_MU_MINB_F64))
-mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
-                  KParams P, DevClock * clk, int step, int cfl_next)
+// The tile list of the HLLD repair pass, at the end of the mixed form's work
+// buffer: [0] tiles listed this step, [1] repair blocks done, [2..3] tiles
+// repaired since the buffer was cleared (64-bit), [4..] the tile indices.
+constexpr int kRepairHead = 4;
+__host__ __device__ inline long long
+repair_tiles(const KParams & P, int TX, int TY)
+{
+  return (long long)((P.nx + TX - 1) / TX) * ((P.ny + TY - 1) / TY) * ((P.nz + P.kchunk - 1) / P.kchunk);
+}
+
+// One tile column of the step: the cells [i0, i0+TX) x [j0, j0+TY) x [k0, k1)
+// of tile (bx, by, bz).  A tile writes only its own cells, from the step's
+// input state and trace.  REPAIR: the faces whose FP32 HLLD star state is
+// ill-conditioned are solved in FP64 (the repair kernel); otherwise such a
+// face lists the tile for that kernel and the tile commits no CFL candidate.
+template <class S, class R, int TX, int TY, bool STAGE, int RS, bool REPAIR>
+__device__ __forceinline__ void
+mhd_update_tile(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
+                const KParams & P, DevClock * clk, int step, int cfl_next, const StepConsts & sc, int bx, int by,
+                int bz, int * repair)
 {
   using T = UpdTile<TX, TY>;
   constexpr int NT = TX * TY;
@@ -667,16 +683,12 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
   R * sEy = sEz + 2 * T::EZS;               // [2][TY][TX+1]
   R * sEx = sEy + 2 * T::EYS;               // [2][TY+1][TX]
 
-  StepConsts sc;
-  if (!step_consts(clk, step, sc))
-    return;
-  const double      t = sc.t, dt = sc.dt;
   const R           dtdx = to_r<R>(sc.dtdx), dtdy = to_r<R>(sc.dtdy), dtdz = to_r<R>(sc.dtdz);
   const double      ddtdx = sc.dtdx, ddtdy = sc.dtdy, ddtdz = sc.dtdz; // FP64 ratios of the CT update
   const MhdConst<R> C = mhd_const<R>(P);
   const int         gw = P.gw;
-  const int         i0 = gw + blockIdx.x * TX, j0 = gw + blockIdx.y * TY;
-  const int         k0 = gw + blockIdx.z * P.kchunk;
+  const int         i0 = gw + bx * TX, j0 = gw + by * TY;
+  const int         k0 = gw + bz * P.kchunk;
   const int         k1 = min(k0 + P.kchunk, P.nz + gw);
   const int         tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   const int         gi = i0 + tx, gj = j0 + ty;
@@ -755,6 +767,12 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
     else
       return fma(f2d(em) - f2d(ep), dratio, b);
   };
+  // mixed HLLD: a face whose FP32 star state is ill-conditioned marks the tile
+  constexpr bool kFlag = sizeof(R) == 4 && RS == 4 && !REPAIR;
+  __shared__ int s_dirty;
+  if (threadIdx.x == 0)
+    s_dirty = 0;
+
   load_plane(k0 - 1);
   for (int k = k0; k <= k1; ++k)
   {
@@ -813,7 +831,17 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
           gather(DirC<1>());
         else
           gather(DirC<2>());
-        mhd_riemann<RS, R, 5>(ql, qr, fl, C.gamma0);
+        if (!mhd_riemann<RS, R, 5>(ql, qr, fl, C.gamma0))
+        {
+          // ill-conditioned star state in FP32 (mixed HLLD only)
+          if constexpr (REPAIR)
+            mhd_hlld_f64_from_f32<5>(ql, qr, fl, C.gamma0);
+          else
+          {
+            s_dirty = 1;
+            continue;
+          }
+        }
         R *       dst = d == 0 ? sFx : (d == 1 ? sFy : sFz);
         const int nd = d == 0 ? T::FXS : (d == 1 ? T::FYS : T::FZS);
 #pragma unroll
@@ -872,7 +900,6 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
       (d == 0 ? Ex : (d == 1 ? Ey : Ez))[f] = e;
     }
     __syncthreads();
-
     const int fz0 = ty * TX + tx;
     if (own && k > k0)
     {
@@ -996,6 +1023,8 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
     }
     __syncthreads(); // trace slot, flux buffers and the older emf planes are reused
   }
+  // block-uniform: the plane loop ended with a barrier
+  const bool dirty = kFlag && s_dirty != 0;
   if (cfl_next)
   {
     if (own && k1 > k0)
@@ -1022,12 +1051,82 @@ mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const
                              bz1 };
       cfl_cell(u, bl, br);
     }
-    block_max_commit<NT>(cand_key((double)tmax), &clk->key[(step + 1) % 3]);
+    if (!dirty)
+      block_max_commit<NT>(cand_key((double)tmax), &clk->key[(step + 1) % 3]);
   }
+  if (dirty && threadIdx.x == 0)
+  {
+    const int gx = (P.nx + TX - 1) / TX, gy = (P.ny + TY - 1) / TY;
+    repair[kRepairHead + atomicAdd(&repair[0], 1)] = (bz * gy + by) * gx + bx;
+  }
+}
+
+// One launch per step: the tile columns of the grid.  repair: the tile list
+// of the mixed HLLD form (null otherwise), whose repair kernel then completes
+// the next step's CFL key.
+template <class S, class R, int TX, int TY, bool STAGE, int RS>
+__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_MU_MINB_F32, EK_MU_MINB_F64))
+mhd_update_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
+                  KParams P, DevClock * clk, int step, int cfl_next, int * repair)
+{
+  StepConsts sc;
+  if (!step_consts(clk, step, sc))
+    return;
+  mhd_update_tile<S, R, TX, TY, STAGE, RS, false>(Uin, Uout, trace, P, clk, step, cfl_next, sc, blockIdx.x,
+                                                   blockIdx.y, blockIdx.z, repair);
   if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
-    step_commit(clk, step, t, dt);
-  if (cfl_next)
+    step_commit(clk, step, sc.t, sc.dt);
+  if (cfl_next && !repair)
     finalize_step(clk, P, step + 1); // the next step's dt, once its CFL key is complete
+}
+
+// The last block of a launch of the repair kernel: true once, after every block
+// has read the tile count; it then clears the list for the next step.
+__device__ __forceinline__ void
+repair_list_release(int * repair)
+{
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    __threadfence();
+    last = atomicAdd(&repair[1], 1) == (int)(gridDim.x * gridDim.y * gridDim.z) - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0)
+  {
+    __threadfence();
+    atomicAdd(reinterpret_cast<unsigned long long *>(repair + 2), (unsigned long long)repair[0]);
+    repair[0] = 0;
+    repair[1] = 0;
+  }
+}
+
+// After the update kernel of the mixed HLLD form: recomputes the tiles it
+// listed, with the faces whose FP32 star state is ill-conditioned solved in
+// FP64 (the rest as in the update kernel, so a tile's other cells are
+// unchanged).  Recomputing a tile replaces its output, as tiles are
+// independent within a step.  Then the next step's CFL key is complete.
+template <class S, class R, int TX, int TY, bool STAGE>
+__global__ void __launch_bounds__(TX * TY, EK_MINB(R, EK_MU_MINB_F32, EK_MU_MINB_F64))
+mhd_repair_kernel(const void * __restrict__ Uin, void * __restrict__ Uout, const R * __restrict__ trace,
+                  KParams P, DevClock * clk, int step, int cfl_next, int * repair)
+{
+  StepConsts sc;
+  if (!step_consts(clk, step, sc))
+    return;
+  const int n = repair[0];
+  const int gx = (P.nx + TX - 1) / TX, gy = (P.ny + TY - 1) / TY;
+  for (int e = blockIdx.x; e < n; e += gridDim.x)
+  {
+    const int tile = repair[kRepairHead + e];
+    mhd_update_tile<S, R, TX, TY, STAGE, 4, true>(Uin, Uout, trace, P, clk, step, cfl_next, sc, tile % gx,
+                                                   (tile / gx) % gy, tile / (gx * gy), repair);
+    __syncthreads(); // shared memory of the next tile
+  }
+  repair_list_release(repair);
+  if (cfl_next)
+    finalize_step(clk, P, step + 1);
 }
 
 // max |div B| over the interior, face differences with dx normalisation
@@ -1069,6 +1168,40 @@ mhd_update_smem(int TX, int TY, bool stage)
 constexpr int MT_TX = EK_MT_TX, MT_TY = EK_MT_TY; // trace tile
 constexpr int MU_TX = EK_MU_TX, MU_TY = EK_MU_TY; // update tile
 
+// bytes of the compact trace in the work buffer (256-byte rounded)
+inline size_t
+mhd_trace_bytes(int prec, const KParams & P)
+{
+  // blocks of 32 trace cells x 48 fields over (nx+2)/32 x (ny+2) x (nz+2)
+  const TraceGrid g = trace_grid(P);
+  const size_t    blk = prec == 0 ? (size_t)kTraceBlock<double> * sizeof(double)
+                                  : (size_t)kTraceBlock<float> * sizeof(float);
+  return (blk * (size_t)g.nb * (size_t)g.nj * (size_t)(P.nz + 2) + 255) & ~(size_t)255;
+}
+// The mixed form's work buffer starts with the repair pass's tile list; the
+// trace follows, 256-byte aligned.  The FP64 form holds the trace alone.
+inline size_t
+mhd_repair_bytes(const KParams & P)
+{
+  return (sizeof(int) * (size_t)(kRepairHead + repair_tiles(P, MU_TX, MU_TY)) + 255) & ~(size_t)255;
+}
+template <class R>
+R *
+mhd_trace_of(void * work, const KParams & P)
+{
+  return reinterpret_cast<R *>(static_cast<char *>(work) + (sizeof(R) == 8 ? 0 : mhd_repair_bytes(P)));
+}
+// blocks of a repair launch: a few per SM (most steps list no tile)
+inline int
+repair_grid(long long tiles)
+{
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 1;
+  const long long g = 2LL * sms;
+  return (int)(tiles < g ? (tiles > 0 ? tiles : 1) : g);
+}
+
 template <class S, class R>
 cudaError_t
 mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams & P, DevClock * clk,
@@ -1090,11 +1223,31 @@ mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams 
       return e;
     const int nt = P.nz + 2;
     dim3      grid((P.nx + 2 + MT_TX - 1) / MT_TX, (P.ny + 2 + MT_TY - 1) / MT_TY, (nt + P.kchunk - 1) / P.kchunk);
-    k<<<grid, MT_TX * MT_TY, sm, st>>>(Uin, (R *)work, P, clk, step);
+    k<<<grid, MT_TX * MT_TY, sm, st>>>(Uin, mhd_trace_of<R>(work, P), P, clk, step);
     return cudaGetLastError();
   }
+  // 4. the repair pass of the mixed HLLD form (after phase 2)
+  if (phase == 3)
+  {
+    if constexpr (sizeof(R) == 8)
+      return cudaErrorNotSupported;
+    else
+    {
+      if (P.riemann != 4)
+        return cudaErrorNotSupported;
+      auto       k = P.mhd_stage ? mhd_repair_kernel<S, R, MU_TX, MU_TY, true> : mhd_repair_kernel<S, R, MU_TX, MU_TY, false>;
+      const int  sm = (int)mhd_update_smem<R>(MU_TX, MU_TY, P.mhd_stage != 0);
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      if (e != cudaSuccess)
+        return e;
+      k<<<repair_grid(repair_tiles(P, MU_TX, MU_TY)), MU_TX * MU_TY, sm, st>>>(
+        Uin, Uout, mhd_trace_of<R>(work, P), P, clk, step, cfl_next ? 1 : 0, (int *)work);
+      return cudaGetLastError();
+    }
+  }
   // 3. fluxes, emfs, update (trace read through L1, or staged in shared memory
-  //    for the HLLD solver); the face Riemann solver is a template parameter
+  //    for the HLLD solver); the face Riemann solver is a template parameter;
+  //    the mixed HLLD form lists tiles for phase 3, which must follow
   {
     auto k = P.riemann == 1   ? mhd_update_kernel<S, R, MU_TX, MU_TY, false, 1>
              : P.riemann == 2 ? mhd_update_kernel<S, R, MU_TX, MU_TY, false, 2>
@@ -1105,7 +1258,8 @@ mhd_step_t(int phase, const void * Uin, void * Uout, void * work, const KParams 
     if (e != cudaSuccess)
       return e;
     dim3 grid((P.nx + MU_TX - 1) / MU_TX, (P.ny + MU_TY - 1) / MU_TY, (P.nz + P.kchunk - 1) / P.kchunk);
-    k<<<grid, MU_TX * MU_TY, sm, st>>>(Uin, Uout, (const R *)work, P, clk, step, cfl_next ? 1 : 0);
+    int * repair = sizeof(R) == 4 && P.riemann == 4 ? (int *)work : nullptr;
+    k<<<grid, MU_TX * MU_TY, sm, st>>>(Uin, Uout, mhd_trace_of<R>(work, P), P, clk, step, cfl_next ? 1 : 0, repair);
     return cudaGetLastError();
   }
 }
@@ -1145,11 +1299,11 @@ mhd_dt(int prec, const void * U, const KParams & P, unsigned long long * key, cu
 size_t
 mhd_work_bytes(int prec, const KParams & P)
 {
-  // blocks of 32 trace cells x 48 fields over (nx+2)/32 x (ny+2) x (nz+2)
-  const TraceGrid g = trace_grid(P);
-  const size_t    blk = prec == 0 ? (size_t)kTraceBlock<double> * sizeof(double)
-                                  : (size_t)kTraceBlock<float> * sizeof(float);
-  return blk * (size_t)g.nb * (size_t)g.nj * (size_t)(P.nz + 2);
+  // the trace; the mixed form's tile list first (cleared by the caller
+  // before the first step)
+  if (prec == 0)
+    return mhd_trace_bytes(0, P);
+  return mhd_repair_bytes(P) + mhd_trace_bytes(1, P);
 }
 
 #ifndef EK_EXACT_ONLY

@@ -264,6 +264,38 @@ def mhd_blast_3d(n=512, nsteps=30, seed=0x10B37A, noise=0.005, slope_type=2.0, c
     return ini, U
 
 
+def mhd_blast_2d(n=1024, nsteps=100, seed=0x10B372, noise=0.005, slope_type=2.0, cfl=0.8,
+                 gamma0=5.0 / 3.0, riemann="hlld", by_ratio=0.1):
+    """Low-beta 2D MHD blast: MHDInitFunctors2D.h:248-340 with uniform
+    B = (10/sqrt(4 pi), by_ratio * 10/sqrt(4 pi), 0) on every face, background
+    rho = 1 + noise*u, p 0.1, disc r 0.1 at the centre with p 10; outflow
+    boundaries.  The transverse component keeps the HLLD star states away from
+    the 0/0 of a field along x only (see mhd_blast_3d)."""
+    gw = 3
+    bx = 10.0 / math.sqrt(4 * math.pi)
+    by = by_ratio * bx
+    ini = _deck("MHD_Muscl_2D", n, n, 1, (2,) * 6, gamma0, cfl, slope_type, riemann, "blast",
+                nsteps, {"blast": {"radius": 0.1, "center_x": 0.5, "center_y": 0.5,
+                                   "density_in": 1.0, "density_out": 1.0, "pressure_in": 10.0,
+                                   "pressure_out": 0.1, "bx_in": bx, "by_in": by, "bz_in": 0.0,
+                                   "bx_out": bx, "by_out": by, "bz_out": 0.0}})
+    g = _f(gamma0)
+    bxf, byf = _f(bx), _f(by)
+    s = n + 2 * gw
+    x = _centres(n, gw, 0.0, 1.0 / n)
+    X, Y = x[None, :], x[:, None]
+    r, c = _f(0.1), _f(0.5)
+    inside = (X - c) * (X - c) + (Y - c) * (Y - c) < r * r
+    u = splitmix_uniform(seed, np.arange(s * s, dtype=np.uint64).reshape(s, s))
+    U = np.zeros((8, 1, s, s))
+    U[0, 0] = np.where(inside, 1.0, 1.0 * (1.0 + noise * u))
+    U[5, 0] = bxf
+    U[6, 0] = byf
+    emag = 0.5 * (bxf * bxf + byf * byf + 0.0)
+    U[1, 0] = np.where(inside, _f(10.0) / (g - 1.0) + emag, _f(0.1) / (g - 1.0) + emag)
+    return ini, U
+
+
 def kelvin_helmholtz_2d(n=128, shear=0.5, ratio=2.0, seed=20261203, nsteps=200, ampl=0.01,
                         pressure=2.5, slope_type=2.0, cfl=0.8, gamma0=1.4, riemann="hllc"):
     """2D Kelvin-Helmholtz, random-perturbation branch of

@@ -188,9 +188,19 @@ ek_status ek_solver_stream(ek_solver * s, void ** stream);
  * every launch of the step kernels (no counterpart in the reference, whose
  * timers wrap whole phases: SolverBase.h:35-45, CudaTimer.h).  Enabling
  * resets the accumulators.  kernel: 0 the fused step kernel (hydro) or the
- * flux/emf/update kernel (MHD), 1 the MHD trace kernel, 2 the MHD CFL kernel. */
+ * flux/emf/update kernel (MHD), 1 the MHD trace kernel, 2 the MHD CFL kernel,
+ * 3 the MHD repair kernel (mixed precision, HLLD). */
 ek_status ek_solver_set_profiling(ek_solver * s, int enable);
 ek_status ek_solver_kernel_time(ek_solver * s, int kernel, double * total_ms, long long * launches);
+
+/* Mixed-precision MHD with the HLLD solver (no counterpart in the reference,
+ * whose HLLD is FP64 throughout): a tile of a step in which a face's FP32
+ * star-state denominator rho (S - u)(S - u*) - Bn^2 is ill-conditioned (below
+ * 2^-14 Bn^2, or at the reference's degenerate-state test) is recomputed by
+ * the step's repair kernel with those faces solved in FP64.  tiles: the tiles
+ * recomputed since the state was set (0 for the other forms); synchronises
+ * the solver's stream. */
+ek_status ek_solver_hlld_repairs(ek_solver * s, long long * tiles);
 
 /* VTK output in the reference's own format: save_VTK_2D / save_VTK_3D
  * (IO_VTK.cpp:24-400, non-MPI), reached by save_solution

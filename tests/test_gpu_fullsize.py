@@ -185,10 +185,15 @@ def test_mhd_blast_lowbeta_512_mixed_vs_fp64():
             n = s.run(30, allow_nonfinite=True)
             assert n == 30
             out[name] = (s.get_state()[:2, 3:-3, 3:-3, 3:-3].copy(), s.dt_history())
+            if name == "mixed":
+                repairs = s.hlld_repairs()
     del U0
     (am, dm), (af, df) = out["mixed"], out["fp64"]
     assert np.abs(dm / df - 1).max() <= 1e-5, np.abs(dm / df - 1).max()
     err = rel_l1(am, af)
-    print("low-beta blast 512^3, 30 steps: L1 rho %.3g E %.3g, max dt diff %.3g" %
-          (err[0], err[1], np.abs(dm / df - 1).max()))
+    print("low-beta blast 512^3, 30 steps: L1 rho %.3g E %.3g, max dt diff %.3g, tiles repaired %d" %
+          (err[0], err[1], np.abs(dm / df - 1).max(), repairs))
+    # the FP32 star states of this case are ill-conditioned on some faces:
+    # the repair pass must have run
+    assert repairs > 0
     assert err[0] <= 1e-5 and err[1] <= 1e-5, err

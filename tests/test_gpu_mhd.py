@@ -132,3 +132,40 @@ def test_mixed_precision_low_beta_blast_error_and_divb():
     for U in (Ug, U64):
         assert _divb_inner(U, p, 4) <= 1e-12 * bscale, (_divb_inner(U, p, 4), bscale)
     assert _divb_inner(U0, p, 0) <= 1e-12 * bscale
+
+
+@pytest.mark.parametrize("kchunk", [0, 6])
+def test_mixed_hlld_repair_pass_low_beta_blast(kchunk):
+    # faces of the low-beta blast whose FP32 HLLD star-state denominator
+    # rho (S - u)(S - u*) - Bn^2 cancels: the update kernel lists their tiles
+    # and the repair kernel (one launch per step) recomputes them with those
+    # faces in FP64.  kchunk 6: partial tile columns along z.
+    ini, U0 = P.mhd_blast_3d(n=64, nsteps=30, by_ratio=0.1)
+    p = ek.params_from_ini(ini, precision=ek.EK_PREC_MIXED, kchunk=kchunk)
+    with ek.Solver(p) as s:
+        s.set_state(U0)
+        s.set_profiling(True)
+        assert s.run(30) == 30
+        Ug, dg, repairs = s.get_state(), s.dt_history(), s.hlld_repairs()
+        _, launches = s.kernel_time(3)
+    U64, d64, _, _ = run_gpu(ini, U0, 30)
+    q = eko.params_from_ini(ini)
+    assert repairs > 0 and launches == 30, (repairs, launches)
+    assert np.all(np.isfinite(Ug))
+    err = rel_l1(interior(Ug, q.gw, 3), interior(U64, q.gw, 3))
+    assert err[0] <= MIXED_L1_TOL and err[1] <= MIXED_L1_TOL, err
+    assert np.abs(dg / d64 - 1).max() <= 1e-5
+
+
+def test_repair_pass_only_for_mixed_hlld():
+    # FP64, and the mixed form with another face solver, have no repair pass
+    ini, U0 = P.orszag_tang_3d(n=16, nsteps=2)
+    for over in ({}, {"precision": ek.EK_PREC_MIXED, "riemann": 2}):
+        p = ek.params_from_ini(ini, **over)
+        with ek.Solver(p) as s:
+            s.set_state(U0)
+            s.set_profiling(True)
+            s.run(2)
+            assert s.hlld_repairs() == 0
+            assert s.kernel_time(3)[1] == 0
+

@@ -21,6 +21,8 @@ pytestmark = pytest.mark.gpu
 
 FP64_LINF_TOL = 1e-11
 MIXED_L1_TOL = 1e-5
+# a low-beta blast whose FP32 HLLD star states cancel on some faces
+REPAIR_2D_N, REPAIR_2D_STEPS = 256, 100
 
 
 def run_gpu(ini, U0, nsteps, **over):
@@ -68,6 +70,7 @@ CASES = [
     ("reflect_outflow", lambda: P.smooth_random(dim=2, mhd=True, nx=33, ny=17, seed=72,
                                                 bc=(1, 2, 2, 1, 1, 1), slope_type=1.0, nsteps=5), 5),
     ("orszag_tang", lambda: P.orszag_tang_2d(n=48, ny=40, nsteps=6, vz_noise=1e-3), 6),
+    ("blast_lowbeta", lambda: P.mhd_blast_2d(n=40, nsteps=6), 6),
 ]
 
 
@@ -98,3 +101,24 @@ def test_fp64_divb_stays_at_roundoff():
     _, _, _, tot = run_gpu(ini, U0, 10)
     bscale = np.abs(U0[5:7]).max() / p.dx
     assert tot[2] <= 1e-12 * bscale, (tot[2], bscale)
+
+
+def test_mixed_hlld_repair_pass_low_beta_blast():
+    # as the 3D case: tiles with ill-conditioned FP32 HLLD star states are
+    # recomputed by the repair kernel with those faces in FP64
+    ini, U0 = P.mhd_blast_2d(n=REPAIR_2D_N, nsteps=REPAIR_2D_STEPS)
+    p = ek.params_from_ini(ini, precision=ek.EK_PREC_MIXED)
+    with ek.Solver(p) as s:
+        s.set_state(U0)
+        s.set_profiling(True)
+        assert s.run(REPAIR_2D_STEPS) == REPAIR_2D_STEPS
+        Ug, dg, repairs = s.get_state(), s.dt_history(), s.hlld_repairs()
+        _, launches = s.kernel_time(3)
+    U64, d64, _, _ = run_gpu(ini, U0, REPAIR_2D_STEPS)
+    q = eko.params_from_ini(ini)
+    assert repairs > 0 and launches == REPAIR_2D_STEPS, (repairs, launches)
+    assert np.all(np.isfinite(Ug))
+    err = rel_l1(interior(Ug, q.gw, 2), interior(U64, q.gw, 2))
+    assert err[0] <= MIXED_L1_TOL and err[1] <= MIXED_L1_TOL, err
+    assert np.abs(dg / d64 - 1).max() <= 1e-5
+
