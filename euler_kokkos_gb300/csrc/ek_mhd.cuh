@@ -161,14 +161,14 @@ mhd_speed_fast_f32(float d, float p, float a, float b, float c, float bn, float 
 // Below this fraction of Bn^2 the face is recomputed in FP64: FP32 rounding
 // leaves estar an absolute error of a few 1e-7 Bn^2, so above the threshold the
 // quotients keep a relative accuracy of about 1e-2 or better.  (A threshold of
-// 2^-7 sent a few per cent of the Orszag-Tang faces, where the transverse
-// field crosses zero, to FP64 and cost 10-45 % of the MHD step.)
+// 2^-7 flags a few per cent of the Orszag-Tang faces, where the transverse
+// field crosses zero; 2^-14 flags none of them.)
 constexpr float kHlldStarTol = 1.0f / 16384.0f;
 
 // false: a star-state denominator of this face is ill-conditioned in FP32
 // (|estar| < kHlldStarTol Bn^2), or the reference's degenerate-state test
-// |estar / Bn^2 - 1| <= 1e-8 cannot be decided in FP32; the caller then
-// computes the face in FP64 (flux is not written)
+// |estar / Bn^2 - 1| <= 1e-8 cannot be decided in FP32; the face is then
+// solved in FP64 (flux is not written)
 template <int NF>
 __device__ __forceinline__ bool
 mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], float gamma0)
@@ -199,29 +199,22 @@ mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], floa
   const float irc = rcp_a(rcr + rcl);
   const float ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc;
   const float ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc;
-  const float ia2 = rcp_a(a2);
-  {
-    const float el_ = rl * (sl - ul) * (sl - ustar) - a2;
-    const float er_ = rr * (sr - ur) * (sr - ustar) - a2;
-    auto ill = [&](float e) {
-      return fabsf(e) < kHlldStarTol * a2 || (a2 > 0.f && fabsf(e * ia2 - 1.f) <= 1e-6f);
-    };
-    if (ill(el_) || ill(er_))
-      return false;
-  }
+  // the star-state denominators; the face goes to FP64 when one is
+  // ill-conditioned, or within 1e-6 of the reference's degenerate-state test
+  // |estar / Bn^2 - 1| <= 1e-8 (which FP32 cannot decide).  So that test is
+  // false for every face solved here, and its branch is not needed below.
+  const float estarl = rl * (sl - ul) * (sl - ustar) - a2;
+  const float estarr = rr * (sr - ur) * (sr - ustar) - a2;
+  auto        ill = [&](float e) { return fabsf(e) < kHlldStarTol * a2 || fabsf(e - a2) <= 1e-6f * a2; };
+  if (ill(estarl) || ill(estarr))
+    return false;
 
   const float isl = rcp_a(sl - ustar);
   const float rstarl = rl * (sl - ul) * isl;
-  float       estar = rl * (sl - ul) * (sl - ustar) - a2;
   const float el = rl * (sl - ul) * (sl - ul) - a2;
   float       vstarl, wstarl, bstarl, cstarl;
-  if (a2 > 0.f && fabsf(estar * ia2 - 1.f) <= 1e-8f)
   {
-    vstarl = vl, bstarl = bl, wstarl = wl, cstarl = cl;
-  }
-  else
-  {
-    const float ie = rcp_a(estar);
+    const float ie = rcp_a(estarl);
     vstarl = vl - a * bl * (ustar - ul) * ie;
     bstarl = bl * el * ie;
     wstarl = wl - a * cl * (ustar - ul) * ie;
@@ -234,16 +227,10 @@ mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], floa
 
   const float isr = rcp_a(sr - ustar);
   const float rstarr = rr * (sr - ur) * isr;
-  estar = rr * (sr - ur) * (sr - ustar) - a2;
   const float er = rr * (sr - ur) * (sr - ur) - a2;
   float       vstarr, wstarr, bstarr, cstarr;
-  if (a2 > 0.f && fabsf(estar * ia2 - 1.f) <= 1e-8f)
   {
-    vstarr = vr, bstarr = br, wstarr = wr, cstarr = cr;
-  }
-  else
-  {
-    const float ie = rcp_a(estar);
+    const float ie = rcp_a(estarr);
     vstarr = vr - a * br * (ustar - ur) * ie;
     bstarr = br * er * ie;
     wstarr = wr - a * cr * (ustar - ur) * ie;

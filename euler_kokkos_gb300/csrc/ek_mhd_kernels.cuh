@@ -1191,15 +1191,14 @@ mhd_trace_of(void * work, const KParams & P)
 {
   return reinterpret_cast<R *>(static_cast<char *>(work) + (sizeof(R) == 8 ? 0 : mhd_repair_bytes(P)));
 }
-// blocks of a repair launch: a few per SM (most steps list no tile)
+// blocks of a repair launch: one per SM (most steps list no tile)
 inline int
 repair_grid(long long tiles)
 {
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     sms = 1;
-  const long long g = 2LL * sms;
-  return (int)(tiles < g ? (tiles > 0 ? tiles : 1) : g);
+  return (int)(tiles < sms ? (tiles > 0 ? tiles : 1) : sms);
 }
 
 template <class S, class R>
