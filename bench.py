@@ -69,7 +69,7 @@ TRAFFIC_PER_CELL = {
     ("hydro3d", "fp64"): {"hydro3d_step": 78.2},    # 306.3 + 247.4 MB / 7.08 M cells
     ("mhd3d", "mixed"): {"mhd_dt_kernel": 46.0,      # 323 + 3 MB / 7.08 M cells (first step only)
                          "mhd_trace_kernel": 243.0,  # 375.4 + 1345.0 MB / 7.08 M cells
-                         "mhd_update_kernel": 338.2,  # 2063.4 + 331.1 MB / 7.08 M cells
+                         "mhd_update_kernel": 335.1,  # 2049.4 + 322.7 MB / 7.08 M cells
                          # with no tile listed (the Orszag-Tang steps) the
                          # repair kernel reads the list head only
                          "mhd_repair_kernel": 0.0},
@@ -525,7 +525,7 @@ def main():
         if tr and all(n in tr for n in kernels):
             step_tr = sum(tr[n] * kernels[n]["launches_per_step"] for n in kernels)
         nl = sum(k["launches_per_step"] for k in kernels.values())
-        out = {"bound": "hbm", "scope": "whole step (%.2f launches per step)" % nl,
+        out = {"bound": "hbm", "scope": ("whole step (%.2f launches per step)" % nl) if kernels else "whole step",
                "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                "traffic": step_tr * cells if step_tr is not None else None,
                "traffic_per_cell": step_tr,

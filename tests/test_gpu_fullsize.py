@@ -25,7 +25,8 @@
 * 3D MHD low-beta blast 512^3 (transverse field), 30 steps: the mixed form
   stays within 1e-5 L1 of FP64 in density and energy and its dt sequence
   within 1e-5.  At this size the FP32 HLLD meets near-degenerate star states
-  (|estar| << Bn^2) that only its FP64 island keeps accurate.
+  (|estar| << Bn^2): the repair kernel recomputes their tiles with those faces
+  in FP64, and the test checks that it did.
 """
 
 import os
