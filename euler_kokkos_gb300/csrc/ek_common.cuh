@@ -297,6 +297,45 @@ sqrt_a(float x)
   return r;
 }
 
+// Packed FP32 pairs: one instruction computes two lanes (sm_100 and later).
+// The mixed form's solvers put the left and right states of a face in the two
+// lanes; each lane rounds as the scalar operation does.
+__device__ __forceinline__ float2
+f2(float a, float b)
+{
+  return make_float2(a, b);
+}
+__device__ __forceinline__ float2
+f2s(float a)
+{
+  return make_float2(a, a);
+}
+__device__ __forceinline__ float2
+add2(float2 a, float2 b)
+{
+  return __fadd2_rn(a, b);
+}
+__device__ __forceinline__ float2
+sub2(float2 a, float2 b)
+{
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a); // b * -1 is exact: one rounding, as a - b
+}
+__device__ __forceinline__ float2
+mul2(float2 a, float2 b)
+{
+  return __fmul2_rn(a, b);
+}
+__device__ __forceinline__ float2
+fma2(float2 a, float2 b, float2 c)
+{
+  return __ffma2_rn(a, b, c);
+}
+__device__ __forceinline__ float2
+neg2(float2 a)
+{
+  return make_float2(-a.x, -a.y);
+}
+
 // FP64 value in the working precision R
 template <class R>
 __device__ __forceinline__ R

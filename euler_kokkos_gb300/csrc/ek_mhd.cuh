@@ -173,73 +173,71 @@ template <int NF>
 __device__ __forceinline__ bool
 mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], float gamma0)
 {
-  const float entho = rcp_a(gamma0 - 1.0f);
-  const float a = 0.5f * (ql[IA] + qr[IA]);
-  const float sgnm = (a >= 0.f) ? 1.f : -1.f;
-  const float a2 = a * a;
-  const float rl = ql[ID], pl = ql[IP], ul = ql[IU], vl = ql[IV], wl = ql[IW], bl = ql[IB], cl = ql[IC];
-  const float ecinl = 0.5f * (ul * ul + vl * vl + wl * wl) * rl;
-  const float emagl = 0.5f * (a2 + bl * bl + cl * cl);
-  const float etotl = pl * entho + ecinl + emagl;
-  const float ptotl = pl + emagl;
-  const float vdotbl = ul * a + vl * bl + wl * cl;
-  const float rr = qr[ID], pr = qr[IP], ur = qr[IU], vr = qr[IV], wr = qr[IW], br = qr[IB], cr = qr[IC];
-  const float ecinr = 0.5f * (ur * ur + vr * vr + wr * wr) * rr;
-  const float emagr = 0.5f * (a2 + br * br + cr * cr);
-  const float etotr = pr * entho + ecinr + emagr;
-  const float ptotr = pr + emagr;
-  const float vdotbr = ur * a + vr * br + wr * cr;
+  // left state in lane x, right state in lane y
+  const float  entho = rcp_a(gamma0 - 1.0f);
+  const float  a = 0.5f * (ql[IA] + qr[IA]);
+  const float  sgnm = (a >= 0.f) ? 1.f : -1.f;
+  const float  a2 = a * a;
+  const float2 A = f2s(a), A2 = f2s(a2), H = f2s(0.5f);
+  const float2 r = f2(ql[ID], qr[ID]), p = f2(ql[IP], qr[IP]), u = f2(ql[IU], qr[IU]);
+  const float2 v = f2(ql[IV], qr[IV]), w = f2(ql[IW], qr[IW]), b = f2(ql[IB], qr[IB]), c = f2(ql[IC], qr[IC]);
+  const float2 bsq = fma2(c, c, fma2(b, b, A2));                         // a^2 + b^2 + c^2
+  const float2 ecin = mul2(mul2(H, fma2(w, w, fma2(v, v, mul2(u, u)))), r);
+  const float2 emag = mul2(H, bsq);
+  const float2 etot = add2(fma2(p, f2s(entho), ecin), emag);
+  const float2 ptot = add2(p, emag);
+  const float2 vdotb = fma2(w, c, fma2(v, b, mul2(u, A)));
 
-  const float cfastl = mhd_speed_fast_f32(rl, pl, a, bl, cl, a, gamma0);
-  const float cfastr = mhd_speed_fast_f32(rr, pr, a, br, cr, a, gamma0);
-  const float sl = fminf(ul, ur) - fmaxf(cfastl, cfastr);
-  const float sr = fmaxf(ul, ur) + fmaxf(cfastl, cfastr);
-  const float rcl = rl * (ul - sl);
-  const float rcr = rr * (sr - ur);
-  const float irc = rcp_a(rcr + rcl);
-  const float ustar = (rcr * ur + rcl * ul + (ptotl - ptotr)) * irc;
-  const float ptotstar = (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) * irc;
+  // fast magnetosonic speeds (find_speed_fast, the normal field a)
+  const float2 id = f2(rcp_a(r.x), rcp_a(r.y));
+  const float2 c2 = mul2(mul2(f2s(gamma0), p), id);
+  const float2 d2 = mul2(H, fma2(bsq, id, c2));
+  const float2 dq = fma2(d2, d2, neg2(mul2(mul2(c2, A2), id)));
+  const float2 cq = add2(d2, f2(sqrt_a(dq.x), sqrt_a(dq.y)));
+  const float  cmax = fmaxf(sqrt_a(cq.x), sqrt_a(cq.y));
+  const float  sl = fminf(u.x, u.y) - cmax;
+  const float  sr = fmaxf(u.x, u.y) + cmax;
+  const float2 S = f2(sl, sr);
+  const float2 su = sub2(S, u);  // S - u
+  const float2 rsu = mul2(r, su); // rho (S - u): -rcl, rcr
+  const float  rcl = -rsu.x, rcr = rsu.y;
+  const float  irc = rcp_a(rcr + rcl);
+  const float  ustar = (rcr * u.y + rcl * u.x + (ptot.x - ptot.y)) * irc;
+  const float  ptotstar = (rcr * ptot.x + rcl * ptot.y + rcl * rcr * (u.x - u.y)) * irc;
+  const float2 US = f2s(ustar);
+  const float2 sus = sub2(S, US);
   // the star-state denominators; the face goes to FP64 when one is
   // ill-conditioned, or within 1e-6 of the reference's degenerate-state test
   // |estar / Bn^2 - 1| <= 1e-8 (which FP32 cannot decide).  So that test is
   // false for every face solved here, and its branch is not needed below.
-  const float estarl = rl * (sl - ul) * (sl - ustar) - a2;
-  const float estarr = rr * (sr - ur) * (sr - ustar) - a2;
-  auto        ill = [&](float e) { return fabsf(e) < kHlldStarTol * a2 || fabsf(e - a2) <= 1e-6f * a2; };
-  if (ill(estarl) || ill(estarr))
+  const float2 estar = fma2(rsu, sus, neg2(A2));
+  auto         ill = [&](float e) { return fabsf(e) < kHlldStarTol * a2 || fabsf(e - a2) <= 1e-6f * a2; };
+  if (ill(estar.x) || ill(estar.y))
     return false;
 
-  const float isl = rcp_a(sl - ustar);
-  const float rstarl = rl * (sl - ul) * isl;
-  const float el = rl * (sl - ul) * (sl - ul) - a2;
-  float       vstarl, wstarl, bstarl, cstarl;
-  {
-    const float ie = rcp_a(estarl);
-    vstarl = vl - a * bl * (ustar - ul) * ie;
-    bstarl = bl * el * ie;
-    wstarl = wl - a * cl * (ustar - ul) * ie;
-    cstarl = cl * el * ie;
-  }
-  const float vdotbstarl = ustar * a + vstarl * bstarl + wstarl * cstarl;
-  const float etotstarl = ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) * isl;
-  const float sqrrstarl = sqrt_a(rstarl);
-  const float sal = ustar - fabsf(a) * rsqrt_a(rstarl);
+  const float2 is = f2(rcp_a(sus.x), rcp_a(sus.y));
+  const float2 rstar = mul2(rsu, is);
+  const float2 e = fma2(rsu, su, neg2(A2)); // rho (S - u)^2 - Bn^2
+  const float2 ie = f2(rcp_a(estar.x), rcp_a(estar.y));
+  const float2 t = mul2(mul2(A, sub2(US, u)), ie);
+  const float2 vstar = fma2(b, neg2(t), v);
+  const float2 bstar = mul2(mul2(b, e), ie);
+  const float2 wstar = fma2(c, neg2(t), w);
+  const float2 cstar = mul2(mul2(c, e), ie);
+  const float2 vdotbstar = fma2(wstar, cstar, fma2(vstar, bstar, mul2(US, A)));
+  const float2 etotstar =
+    mul2(add2(fma2(su, etot, neg2(mul2(ptot, u))), fma2(A, sub2(vdotb, vdotbstar), f2s(ptotstar * ustar))), is);
+  const float  sqrrstarl = sqrt_a(rstar.x), sqrrstarr = sqrt_a(rstar.y);
+  const float  sal = ustar - fabsf(a) * rsqrt_a(rstar.x);
+  const float  sar = ustar + fabsf(a) * rsqrt_a(rstar.y);
 
-  const float isr = rcp_a(sr - ustar);
-  const float rstarr = rr * (sr - ur) * isr;
-  const float er = rr * (sr - ur) * (sr - ur) - a2;
-  float       vstarr, wstarr, bstarr, cstarr;
-  {
-    const float ie = rcp_a(estarr);
-    vstarr = vr - a * br * (ustar - ur) * ie;
-    bstarr = br * er * ie;
-    wstarr = wr - a * cr * (ustar - ur) * ie;
-    cstarr = cr * er * ie;
-  }
-  const float vdotbstarr = ustar * a + vstarr * bstarr + wstarr * cstarr;
-  const float etotstarr = ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) * isr;
-  const float sqrrstarr = sqrt_a(rstarr);
-  const float sar = ustar + fabsf(a) * rsqrt_a(rstarr);
+  const float rl = r.x, ul = u.x, vl = v.x, wl = w.x, bl = b.x, cl = c.x;
+  const float rr = r.y, ur = u.y, vr = v.y, wr = w.y, br = b.y, cr = c.y;
+  const float ptotl = ptot.x, ptotr = ptot.y, etotl = etot.x, etotr = etot.y, vdotbl = vdotb.x, vdotbr = vdotb.y;
+  const float rstarl = rstar.x, rstarr = rstar.y;
+  const float vstarl = vstar.x, vstarr = vstar.y, wstarl = wstar.x, wstarr = wstar.y;
+  const float bstarl = bstar.x, bstarr = bstar.y, cstarl = cstar.x, cstarr = cstar.y;
+  const float vdotbstarl = vdotbstar.x, vdotbstarr = vdotbstar.y, etotstarl = etotstar.x, etotstarr = etotstar.y;
 
   float ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
   if (sl > 0.f)

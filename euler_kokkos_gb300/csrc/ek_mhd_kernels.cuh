@@ -629,16 +629,48 @@ mhd_trace_kernel(const void * __restrict__ U, R * __restrict__ trace, KParams P,
 // Output tile [i0, i0+TX) x [j0, j0+TY) marching over planes [k0, k1).  The
 // compact trace of the cells [i0-1, i0+TX] x [j0-1, j0+TY] of planes k-1 and k
 // is read through L1, or staged in shared memory (STAGE).  Per plane, the
-// faces and edges the tile needs form one flat work list: all faces first
-// (one code path for the three directions, the HLLD solver), then all edges
-// (one code path, the 2D HLLD emf), so a warp runs at most two item kinds
-// and the kernel holds one copy of each solver.
+// faces and edges the tile needs form one work list ordered by rows
+// (UpdTile::item): one code path for the faces of the three directions (the
+// HLLD solver) and one for the edges (the 2D HLLD emf), so the kernel holds
+// one copy of each solver.
 template <int TX, int TY>
 struct UpdTile
 {
   static constexpr int XE = TX + 2, YE = TY + 2, PL = XE * YE; // trace cells per plane
   static constexpr int FXS = (TX + 1) * TY, FYS = TX * (TY + 1), FZS = TX * TY;
   static constexpr int EZS = (TX + 1) * (TY + 1), EYS = (TX + 1) * TY, EXS = TX * (TY + 1);
+  // the work items of a plane: rows 0..TY-1 in groups of RG rows, six kinds
+  // of TX items per row; row TY (y-faces, x-edges, z-edges: TX each); column
+  // TX (x-faces, y-edges: TY each; z-edges: TY + 1)
+  static constexpr int RG = TX < 32 ? 32 / TX : 1;
+  static_assert(TY % RG == 0, "rows per item group must divide TY");
+  static constexpr int NMAIN = 6 * TX * TY, NROW = 3 * TX, NCOL = 3 * TY + 1;
+  static constexpr int NITEMS = NMAIN + NROW + NCOL;
+  __device__ static __forceinline__ void
+  item(int w, int & kind, int & li, int & lj)
+  {
+    if (w < NMAIN)
+    {
+      li = w % TX;
+      const int g = w / TX; // (row group, kind, row in group)
+      kind = (g / RG) % 6;
+      lj = (g / (6 * RG)) * RG + g % RG;
+    }
+    else if (w < NMAIN + NROW)
+    {
+      const int v = w - NMAIN, q = v / TX;
+      li = v % TX;
+      lj = TY;
+      kind = q == 0 ? 2 : (q == 1 ? 4 : 5);
+    }
+    else
+    {
+      const int v = w - NMAIN - NROW;
+      li = TX;
+      kind = v < TY ? 1 : (v < 2 * TY ? 3 : 5);
+      lj = v < TY ? v : (v < 2 * TY ? v - TY : v - 2 * TY);
+    }
+  }
 };
 
 // The tile list of the HLLD repair pass, at the end of the mixed form's work
@@ -782,29 +814,26 @@ mhd_update_tile(const void * __restrict__ Uin, void * __restrict__ Uout, const R
     R * Ez = sEz + (k & 1) * T::EZS;
     R * Ey = sEy + (k & 1) * T::EYS;
     R * Ex = sEx + (k & 1) * T::EXS;
-    // faces (z, x, y; padded to whole warps) then edges (y, x, z); plane k1
-    // only needs its z-faces and its y- and x-edges
-    const int nf = plane ? T::FZS + T::FXS + T::FYS : T::FZS;
-    const int nfp = (nf + 31) & ~31;
-    const int ne = plane ? T::EYS + T::EXS + T::EZS : T::EYS + T::EXS;
-    for (int w = threadIdx.x; w < nfp + ne; w += NT)
+    // Work items (faces and edges) ordered by rows: for each row (or group
+    // of 32 / TX rows), its z-, x- and y-faces, then its y-, x- and z-edges,
+    // TX items each; then row TY and column TX.  A warp's items are of one
+    // kind, and the items that gather a cell's trace run close together, so
+    // the repeated gathers hit L1.  Plane k1 only needs its z-faces and its
+    // y- and x-edges.
+    for (int w = threadIdx.x; w < T::NITEMS; w += NT)
     {
-      if (w < nfp)
+      int kind, li, lj; // kind 0..5: z-, x-, y-face, y-, x-, z-edge
+      T::item(w, kind, li, lj);
+      if (!plane && (kind == 1 || kind == 2 || kind == 5))
+        continue;
+      if (kind < 3)
       {
-        if (w >= nf)
-          continue;
-        int f = w, d = 2;
-        if (f >= T::FZS)
-        {
-          f -= T::FZS;
-          d = 0;
-          if (f >= T::FXS)
-            f -= T::FXS, d = 1;
-        }
         // face normal to d between cell (i,j,k) - e_d and cell (i,j,k)
-        // (MHDRunFunctors3D.h:1839-1874); rows of TX+1 x-faces or TX faces
-        // (constant divisors)
-        const int i = i0 + (d == 0 ? f % (TX + 1) : f % TX), j = j0 + (d == 0 ? f / (TX + 1) : f / TX);
+        // (MHDRunFunctors3D.h:1839-1874); flux index f in rows of TX + 1
+        // x-faces or TX faces
+        const int d = kind == 0 ? 2 : kind - 1;
+        const int f = d == 0 ? lj * (TX + 1) + li : lj * TX + li;
+        const int i = i0 + li, j = j0 + lj;
         if (i > ihi - (d != 0 ? 1 : 0) || j > jhi - (d != 1 ? 1 : 0))
           continue;
         R ql[8], qr[8], fl[5];
@@ -849,18 +878,13 @@ mhd_update_tile(const void * __restrict__ Uin, void * __restrict__ Uout, const R
           dst[v * nd + f] = fl[v];
         continue;
       }
-      int f = w - nfp, d = 1;
-      if (f >= T::EYS)
-      {
-        f -= T::EYS;
-        d = 0;
-        if (f >= T::EXS)
-          f -= T::EXS, d = 2;
-      }
       // edge along d at the low corner of cell (i,j,k); corners RT, RB, LT, LB
       // lie at -1 along (p1,p2), p1, p2 and nowhere (z-edge: RT(i-1,j-1),
-      // RB(i-1,j), LT(i,j-1), LB(i,j); MHDRunFunctors3D.h:2180-2230)
-      const int i = i0 + (d == 0 ? f % TX : f % (TX + 1)), j = j0 + (d == 0 ? f / TX : f / (TX + 1));
+      // RB(i-1,j), LT(i,j-1), LB(i,j); MHDRunFunctors3D.h:2180-2230); emf
+      // index f in rows of TX x-edges or TX + 1 edges
+      const int d = kind == 3 ? 1 : (kind == 4 ? 0 : 2);
+      const int f = d == 0 ? lj * TX + li : lj * (TX + 1) + li;
+      const int i = i0 + li, j = j0 + lj;
       if (i > ihi - (d == 0 ? 1 : 0) || j > jhi - (d == 1 ? 1 : 0))
         continue;
       EdgeCorner<R> cRT, cRB, cLT, cLB;
