@@ -26,13 +26,17 @@ slope1(R q, R qp, R qm, R st)
 {
   if constexpr (sizeof(R) == 4)
   {
-    // the same limiter with the sign taken by copysign and the zero case by
-    // one select (FP32 form; signed zeros may differ)
-    const float dlft = st * (q - qm);
-    const float drgt = st * (qp - q);
-    const float dcen = 0.5f * (qp - qm);
-    const float m = fminf(fminf(fabsf(dlft), fabsf(drgt)), fabsf(dcen));
-    return (dlft * drgt > 0.f) ? copysignf(m, dcen) : 0.f;
+    // the same limiter, FP32 form (signed zeros may differ).  st is 0, 1 or
+    // 2, so scaling by it is exact and min(|st dl|, |st dr|) = st min(|dl|,
+    // |dr|) (0 for first order).
+    // Where dl and dr have one sign, so has dcen, and |dcen| >= min(|dl|,
+    // |dr|) after rounding too (rounding is monotonic): with st = 1 (minmod)
+    // the centred difference never binds.
+    const float dl = q - qm, dr = qp - q;
+    float       m = st * fminf(fabsf(dl), fabsf(dr));
+    if (st != 1.f)
+      m = fminf(m, fabsf(0.5f * (qp - qm)));
+    return (dl * dr > 0.f) ? copysignf(m, dl) : 0.f;
   }
   const R dlft = st * (q - qm);
   const R drgt = st * (qp - q);
@@ -172,13 +176,24 @@ __device__ __forceinline__ void
 hydro_face(const R (&q)[NV], const R (&d)[NV], const R (&s)[NV], R dtd, bool plus, R (&f)[NV],
            R smallr)
 {
-#pragma unroll
-  for (int v = 0; v < NV; ++v)
+  if constexpr (sizeof(R) == 4 || kShareRecip)
   {
-    if (plus)
-      f[v] = q[v] + R(0.5) * d[v] + s[v] * dtd * R(0.5);
-    else
-      f[v] = q[v] - R(0.5) * d[v] + s[v] * dtd * R(0.5);
+    // mixed form and FP64 FMA build: two fused multiply-adds per variable
+    const R hdtd = R(0.5) * dtd, hd = plus ? R(0.5) : R(-0.5);
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+      f[v] = fma(hd, d[v], fma(s[v], hdtd, q[v]));
+  }
+  else
+  {
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+    {
+      if (plus)
+        f[v] = q[v] + R(0.5) * d[v] + s[v] * dtd * R(0.5);
+      else
+        f[v] = q[v] - R(0.5) * d[v] + s[v] * dtd * R(0.5);
+    }
   }
   f[ID] = fmax(smallr, f[ID]);
 }
@@ -190,37 +205,49 @@ __device__ __forceinline__ void
 hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
 {
   const R entho = C.entho;
-  const R rl = fmax(ql[ID], C.smallr);
-  const R pl = fmax(ql[IP], rl * C.smallp);
-  const R ul = ql[IU];
-  R       ecinl = R(0.5) * rl * ul * ul;
-  ecinl += R(0.5) * rl * ql[IV] * ql[IV];
-  if constexpr (NV == 5)
-    ecinl += R(0.5) * rl * ql[IW] * ql[IW];
-  const R etotl = pl * entho + ecinl;
-  const R ptotl = pl;
-
-  const R rr = fmax(qr[ID], C.smallr);
-  const R pr = fmax(qr[IP], rr * C.smallp);
-  const R ur = qr[IU];
-  R       ecinr = R(0.5) * rr * ur * ur;
-  ecinr += R(0.5) * rr * qr[IV] * qr[IV];
-  if constexpr (NV == 5)
-    ecinr += R(0.5) * rr * qr[IW] * qr[IW];
-  const R etotr = pr * entho + ecinr;
-  const R ptotr = pr;
-
-  R cfastl, cfastr;
+  R       rl, pl, ul, etotl, rr, pr, ur, etotr, cfastl, cfastr;
   if constexpr (sizeof(R) == 4)
   {
-    cfastl = sqrt_a(fmax(C.gamma0 * pl * rcp_a(rl), C.smallc * C.smallc));
-    cfastr = sqrt_a(fmax(C.gamma0 * pr * rcp_a(rr), C.smallc * C.smallc));
+    // mixed form: the two states in the lanes of packed FP32 pairs
+    const float2 r = f2(fmaxf(ql[ID], C.smallr), fmaxf(qr[ID], C.smallr));
+    const float2 ps = mul2(r, f2s(C.smallp));
+    const float2 p = f2(fmaxf(ql[IP], ps.x), fmaxf(qr[IP], ps.y));
+    const float2 u = f2(ql[IU], qr[IU]), v = f2(ql[IV], qr[IV]);
+    float2       k2 = fma2(v, v, mul2(u, u));
+    if constexpr (NV == 5)
+      k2 = fma2(f2(ql[IW], qr[IW]), f2(ql[IW], qr[IW]), k2);
+    const float2 etot = fma2(p, f2s(entho), mul2(mul2(f2s(0.5f), r), k2));
+    const float2 c2 = mul2(mul2(f2s(C.gamma0), p), f2(rcp_a(r.x), rcp_a(r.y)));
+    const float  sc2 = C.smallc * C.smallc;
+    rl = r.x, pl = p.x, ul = u.x, etotl = etot.x;
+    rr = r.y, pr = p.y, ur = u.y, etotr = etot.y;
+    cfastl = sqrt_a(fmaxf(c2.x, sc2));
+    cfastr = sqrt_a(fmaxf(c2.y, sc2));
   }
   else
   {
+    rl = fmax(ql[ID], C.smallr);
+    pl = fmax(ql[IP], rl * C.smallp);
+    ul = ql[IU];
+    R ecinl = R(0.5) * rl * ul * ul;
+    ecinl += R(0.5) * rl * ql[IV] * ql[IV];
+    if constexpr (NV == 5)
+      ecinl += R(0.5) * rl * ql[IW] * ql[IW];
+    etotl = pl * entho + ecinl;
+
+    rr = fmax(qr[ID], C.smallr);
+    pr = fmax(qr[IP], rr * C.smallp);
+    ur = qr[IU];
+    R ecinr = R(0.5) * rr * ur * ur;
+    ecinr += R(0.5) * rr * qr[IV] * qr[IV];
+    if constexpr (NV == 5)
+      ecinr += R(0.5) * rr * qr[IW] * qr[IW];
+    etotr = pr * entho + ecinr;
+
     cfastl = sqrt(fmax(C.gamma0 * pl / rl, C.smallc * C.smallc));
     cfastr = sqrt(fmax(C.gamma0 * pr / rr, C.smallc * C.smallc));
   }
+  const R ptotl = pl, ptotr = pr;
 
   const R SL = fmin(ul, ur) - fmax(cfastl, cfastr);
   const R SR = fmax(ul, ur) + fmax(cfastl, cfastr);
