@@ -671,6 +671,43 @@ struct UpdTile
       lj = v < TY ? v : (v < 2 * TY ? v - TY : v - 2 * TY);
     }
   }
+  // the same items by kind: z-, x-, y-faces (padded to whole warps), then y-,
+  // x-, z-edges; false for a padding item
+  static constexpr int NFACES = FZS + FXS + FYS, NFP = (NFACES + 31) & ~31;
+  static constexpr int NITEMS_K = NFP + EYS + EXS + EZS;
+  __device__ static __forceinline__ bool
+  item_by_kind(int w, int & kind, int & li, int & lj)
+  {
+    if (w < NFP)
+    {
+      if (w >= NFACES)
+        return false;
+      int f = w;
+      kind = 0;
+      if (f >= FZS)
+      {
+        f -= FZS;
+        kind = 1;
+        if (f >= FXS)
+          f -= FXS, kind = 2;
+      }
+      li = kind == 1 ? f % (TX + 1) : f % TX;
+      lj = kind == 1 ? f / (TX + 1) : f / TX;
+      return true;
+    }
+    int e = w - NFP;
+    kind = 3;
+    if (e >= EYS)
+    {
+      e -= EYS;
+      kind = 4;
+      if (e >= EXS)
+        e -= EXS, kind = 5;
+    }
+    li = kind == 4 ? e % TX : e % (TX + 1);
+    lj = kind == 4 ? e / TX : e / (TX + 1);
+    return true;
+  }
 };
 
 // The tile list of the HLLD repair pass, at the end of the mixed form's work
@@ -814,16 +851,20 @@ mhd_update_tile(const void * __restrict__ Uin, void * __restrict__ Uout, const R
     R * Ez = sEz + (k & 1) * T::EZS;
     R * Ey = sEy + (k & 1) * T::EYS;
     R * Ex = sEx + (k & 1) * T::EXS;
-    // Work items (faces and edges) ordered by rows: for each row (or group
-    // of 32 / TX rows), its z-, x- and y-faces, then its y-, x- and z-edges,
-    // TX items each; then row TY and column TX.  A warp's items are of one
-    // kind, and the items that gather a cell's trace run close together, so
-    // the repeated gathers hit L1.  Plane k1 only needs its z-faces and its
-    // y- and x-edges.
-    for (int w = threadIdx.x; w < T::NITEMS; w += NT)
+    // Work items (faces and edges).  Mixed form: ordered by rows (UpdTile::
+    // item), so the items that gather a cell's trace run close together and
+    // the repeated gathers hit L1 (four CTAs share an SM's L1).  FP64: all
+    // faces of the plane, then all edges (UpdTile::item_by_kind): one CTA
+    // per SM, bound by the FP64 pipe, and the warps' shares of the two kinds
+    // stay equal (an edge costs about twice a face).  Plane k1 only needs its
+    // z-faces and its y- and x-edges.
+    for (int w = threadIdx.x; w < (sizeof(R) == 4 ? T::NITEMS : T::NITEMS_K); w += NT)
     {
       int kind, li, lj; // kind 0..5: z-, x-, y-face, y-, x-, z-edge
-      T::item(w, kind, li, lj);
+      if constexpr (sizeof(R) == 4)
+        T::item(w, kind, li, lj);
+      else if (!T::item_by_kind(w, kind, li, lj))
+        continue;
       if (!plane && (kind == 1 || kind == 2 || kind == 5))
         continue;
       if (kind < 3)
