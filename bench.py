@@ -65,11 +65,11 @@ KERNEL_NAMES = {
 # are in profiles/); a launch's traffic on the bench workload is this figure
 # times its interior cells (these kernels' traffic grows with the cells).
 TRAFFIC_PER_CELL = {
-    ("hydro3d", "mixed"): {"hydro3d_step": 38.3},   # 158.6 + 112.7 MB / 7.08 M cells
+    ("hydro3d", "mixed"): {"hydro3d_step": 38.0},   # 159.0 + 109.9 MB / 7.08 M cells
     ("hydro3d", "fp64"): {"hydro3d_step": 78.2},    # 306.3 + 247.4 MB / 7.08 M cells
     ("mhd3d", "mixed"): {"mhd_dt_kernel": 46.0,      # 323 + 3 MB / 7.08 M cells (first step only)
                          "mhd_trace_kernel": 243.0,  # 375.4 + 1345.0 MB / 7.08 M cells
-                         "mhd_update_kernel": 335.1,  # 2049.4 + 322.7 MB / 7.08 M cells
+                         "mhd_update_kernel": 345.8,  # 2125.8 + 321.4 MB / 7.08 M cells
                          # with no tile listed (the Orszag-Tang steps) the
                          # repair kernel reads the list head only
                          "mhd_repair_kernel": 0.0},
