@@ -639,37 +639,46 @@ struct UpdTile
   static constexpr int XE = TX + 2, YE = TY + 2, PL = XE * YE; // trace cells per plane
   static constexpr int FXS = (TX + 1) * TY, FYS = TX * (TY + 1), FZS = TX * TY;
   static constexpr int EZS = (TX + 1) * (TY + 1), EYS = (TX + 1) * TY, EXS = TX * (TY + 1);
-  // the work items of a plane: rows 0..TY-1 in groups of RG rows, six kinds
-  // of TX items per row; row TY (y-faces, x-edges, z-edges: TX each); column
-  // TX (x-faces, y-edges: TY each; z-edges: TY + 1)
+  // The work items of a plane, in segments of 32 (one warp each).  First the
+  // edges of the tile: row TY (y-faces, x-edges, z-edges: TX each) and column
+  // TX (x-faces, y-edges: TY each; z-edges: TY + 1), each kind in segments of
+  // its own.  Then rows 0..TY-1 in groups of RG rows, six kinds of TX items
+  // per row, their order rotated by one kind per row group: with a fixed
+  // order, warp w would take the kinds w, w + 8, w + 16 (mod 6), always three
+  // faces or always three edges per two warps, and edges cost about twice a
+  // face.  item() is false for a padding slot.
   static constexpr int RG = TX < 32 ? 32 / TX : 1;
   static_assert(TY % RG == 0, "rows per item group must divide TY");
-  static constexpr int NMAIN = 6 * TX * TY, NROW = 3 * TX, NCOL = 3 * TY + 1;
-  static constexpr int NITEMS = NMAIN + NROW + NCOL;
-  __device__ static __forceinline__ void
+  static constexpr int RSEG = (TX + 31) / 32, CSEG = (TY + 1 + 31) / 32;
+  static constexpr int NTAIL = 32 * 3 * (RSEG + CSEG), NMAIN = 6 * TX * TY;
+  static constexpr int NITEMS = NTAIL + NMAIN;
+  __device__ static __forceinline__ bool
   item(int w, int & kind, int & li, int & lj)
   {
-    if (w < NMAIN)
+    if (w < NTAIL)
     {
-      li = w % TX;
-      const int g = w / TX; // (row group, kind, row in group)
-      kind = (g / RG) % 6;
-      lj = (g / (6 * RG)) * RG + g % RG;
-    }
-    else if (w < NMAIN + NROW)
-    {
-      const int v = w - NMAIN, q = v / TX;
-      li = v % TX;
-      lj = TY;
-      kind = q == 0 ? 2 : (q == 1 ? 4 : 5);
-    }
-    else
-    {
-      const int v = w - NMAIN - NROW;
+      const int seg = w / 32, lane = w % 32;
+      if (seg < 3 * RSEG)
+      {
+        const int q = seg / RSEG;
+        kind = q == 0 ? 2 : (q == 1 ? 4 : 5);
+        li = (seg % RSEG) * 32 + lane;
+        lj = TY;
+        return li < TX;
+      }
+      const int c = seg - 3 * RSEG, q = c / CSEG;
+      kind = q == 0 ? 1 : (q == 1 ? 3 : 5);
       li = TX;
-      kind = v < TY ? 1 : (v < 2 * TY ? 3 : 5);
-      lj = v < TY ? v : (v < 2 * TY ? v - TY : v - 2 * TY);
+      lj = (c % CSEG) * 32 + lane;
+      return lj < (q == 2 ? TY + 1 : TY);
     }
+    const int v = w - NTAIL;
+    li = v % TX;
+    const int g = v / TX; // (row group, kind position, row in group)
+    const int rg = g / (6 * RG);
+    kind = ((g / RG) % 6 + rg) % 6;
+    lj = rg * RG + g % RG;
+    return true;
   }
   // the same items by kind: z-, x-, y-faces (padded to whole warps), then y-,
   // x-, z-edges; false for a padding item
@@ -861,9 +870,7 @@ mhd_update_tile(const void * __restrict__ Uin, void * __restrict__ Uout, const R
     for (int w = threadIdx.x; w < (sizeof(R) == 4 ? T::NITEMS : T::NITEMS_K); w += NT)
     {
       int kind, li, lj; // kind 0..5: z-, x-, y-face, y-, x-, z-edge
-      if constexpr (sizeof(R) == 4)
-        T::item(w, kind, li, lj);
-      else if (!T::item_by_kind(w, kind, li, lj))
+      if (!(sizeof(R) == 4 ? T::item(w, kind, li, lj) : T::item_by_kind(w, kind, li, lj)))
         continue;
       if (!plane && (kind == 1 || kind == 2 || kind == 5))
         continue;
