@@ -142,16 +142,10 @@ mhd_constoprim(const R (&u)[5], const R (&bl)[3], const R (&br)[3], R (&q)[8], c
 }
 
 // riemann_hlld in FP32 for the mixed form: the reference's solver with each
-// shared denominator inverted once (rcp_a) and |B_n| / sqrt(rho*) as a
-// reciprocal square root; same branches and degeneracy test.
-__device__ __forceinline__ float
-mhd_speed_fast_f32(float d, float p, float a, float b, float c, float bn, float gamma0)
-{
-  const float id = rcp_a(d);
-  const float c2 = gamma0 * p * id;
-  const float d2 = 0.5f * ((a * a + b * b + c * c) * id + c2);
-  return sqrt_a(d2 + sqrt_a(d2 * d2 - c2 * bn * bn * id));
-}
+// shared denominator inverted once (rcp_a), |B_n| / sqrt(rho*) as a
+// reciprocal square root, and the left and right states in the two lanes of
+// packed FP32 pairs; the same branches, and the faces it cannot decide left
+// to FP64 (below).
 
 // The star-state denominators of HLLD, estar = rho (S - u)(S - ustar) - Bn^2,
 // cancel as the state approaches the degenerate one (transverse field near
