@@ -134,14 +134,17 @@ def test_mixed_precision_low_beta_blast_error_and_divb():
     assert _divb_inner(U0, p, 0) <= 1e-12 * bscale
 
 
-@pytest.mark.parametrize("kchunk", [0, 6])
-def test_mixed_hlld_repair_pass_low_beta_blast(kchunk):
+@pytest.mark.parametrize("n,kchunk,stage", [(64, 0, 0), (64, 6, 0), (68, 6, 0), (64, 0, 1)],
+                         ids=["64", "64_kchunk6", "68_partial_tiles", "64_staged_trace"])
+def test_mixed_hlld_repair_pass_low_beta_blast(n, kchunk, stage):
     # faces of the low-beta blast whose FP32 HLLD star-state denominator
     # rho (S - u)(S - u*) - Bn^2 cancels: the update kernel lists their tiles
     # and the repair kernel (one launch per step) recomputes them with those
-    # faces in FP64.  kchunk 6: partial tile columns along z.
-    ini, U0 = P.mhd_blast_3d(n=64, nsteps=30, by_ratio=0.1)
-    p = ek.params_from_ini(ini, precision=ek.EK_PREC_MIXED, kchunk=kchunk)
+    # faces in FP64.  kchunk 6: partial tile columns along z; 68^3: partial
+    # tiles in x and y; stage: the update and repair kernels with the trace
+    # planes staged in shared memory.
+    ini, U0 = P.mhd_blast_3d(n=n, nsteps=30, by_ratio=0.1)
+    p = ek.params_from_ini(ini, precision=ek.EK_PREC_MIXED, kchunk=kchunk, mhd_stage=stage)
     with ek.Solver(p) as s:
         s.set_state(U0)
         s.set_profiling(True)
