@@ -205,7 +205,7 @@ __device__ __forceinline__ void
 hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & C)
 {
   const R entho = C.entho;
-  R       rl, pl, ul, etotl, rr, pr, ur, etotr, cfastl, cfastr;
+  R       rl, pl, ul, etotl, rr, pr, ur, etotr, cmax; // cmax: the larger sound speed
   if constexpr (sizeof(R) == 4)
   {
     // mixed form: the two states in the lanes of packed FP32 pairs
@@ -221,8 +221,7 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
     const float  sc2 = C.smallc * C.smallc;
     rl = r.x, pl = p.x, ul = u.x, etotl = etot.x;
     rr = r.y, pr = p.y, ur = u.y, etotr = etot.y;
-    cfastl = sqrt_a(fmaxf(c2.x, sc2));
-    cfastr = sqrt_a(fmaxf(c2.y, sc2));
+    cmax = sqrt_a(fmaxf(fmaxf(c2.x, c2.y), sc2));
   }
   else
   {
@@ -244,13 +243,20 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
       ecinr += R(0.5) * rr * qr[IW] * qr[IW];
     etotr = pr * entho + ecinr;
 
-    cfastl = sqrt(fmax(C.gamma0 * pl / rl, C.smallc * C.smallc));
-    cfastr = sqrt(fmax(C.gamma0 * pr / rr, C.smallc * C.smallc));
+    const R c2l = fmax(C.gamma0 * pl / rl, C.smallc * C.smallc);
+    const R c2r = fmax(C.gamma0 * pr / rr, C.smallc * C.smallc);
+    // a correctly rounded square root is monotonic: the FP64 FMA build takes
+    // one square root of the larger square, the same bits as the larger of
+    // the two square roots the reference takes
+    if constexpr (kShareRecip)
+      cmax = sqrt(fmax(c2l, c2r));
+    else
+      cmax = fmax(sqrt(c2l), sqrt(c2r));
   }
   const R ptotl = pl, ptotr = pr;
 
-  const R SL = fmin(ul, ur) - fmax(cfastl, cfastr);
-  const R SR = fmax(ul, ur) + fmax(cfastl, cfastr);
+  const R SL = fmin(ul, ur) - cmax;
+  const R SR = fmax(ul, ur) + cmax;
 
   const R rcl = rl * (ul - SL);
   const R rcr = rr * (SR - ur);

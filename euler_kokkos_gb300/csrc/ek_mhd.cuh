@@ -36,6 +36,23 @@ mhd_speed_fast(const R (&q)[8], R gamma0)
   return sqrt(d2 + sqrt(d2 * d2 - c2 * bn * bn / d));
 }
 
+// the square of find_speed_fast<dir> before its outer square root (FP64 FMA
+// build).  A correctly rounded square root is monotonic, so the largest of
+// several speeds is the square root of the largest of these, bit for bit,
+// one square root instead of one per state.
+template <class R, int DIR>
+__device__ __forceinline__ R
+mhd_speed_fast_sq(const R (&q)[8], R gamma0)
+{
+  const R d = q[ID], p = q[IP], a = q[IA], b = q[IB], c = q[IC];
+  const R b2 = a * a + b * b + c * c;
+  const R bn = DIR == 0 ? a : (DIR == 1 ? b : c);
+  const R id = R(1) / d;
+  const R c2 = gamma0 * p * id;
+  const R d2 = R(0.5) * (b2 * id + c2);
+  return d2 + sqrt(d2 * d2 - c2 * bn * bn * id);
+}
+
 // find_speed_info<THREE_D> summed as ComputeDtFunctor3D_MHD does
 // (mhd_utils.h:319-366, MHDRunFunctors3D.h:58-76).  FP64: the reference's
 // expression; mixed: the candidate is formed in FP32 with 1/dx (the
@@ -188,7 +205,7 @@ mhd_hlld_f32(const float (&ql)[8], const float (&qr)[8], float (&flux)[NF], floa
   const float2 d2 = mul2(H, fma2(bsq, id, c2));
   const float2 dq = fma2(d2, d2, neg2(mul2(mul2(c2, A2), id)));
   const float2 cq = add2(d2, f2(sqrt_a(dq.x), sqrt_a(dq.y)));
-  const float  cmax = fmaxf(sqrt_a(cq.x), sqrt_a(cq.y));
+  const float  cmax = sqrt_a(fmaxf(cq.x, cq.y)); // the larger fast speed
   const float  sl = fminf(u.x, u.y) - cmax;
   const float  sr = fmaxf(u.x, u.y) + cmax;
   const float2 S = f2(sl, sr);
@@ -317,10 +334,14 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   const R ptotr = pr + emagr;
   const R vdotbr = ur * a + vr * br + wr * cr;
 
-  const R cfastl = mhd_speed_fast<R, 0>(ql, gamma0);
-  const R cfastr = mhd_speed_fast<R, 0>(qr, gamma0);
-  const R sl = fmin(ul, ur) - fmax(cfastl, cfastr);
-  const R sr = fmax(ul, ur) + fmax(cfastl, cfastr);
+  // the larger fast speed (FP64 FMA build: one outer square root, the same bits)
+  R cmax;
+  if constexpr (kShareRecip)
+    cmax = sqrt(fmax(mhd_speed_fast_sq<R, 0>(ql, gamma0), mhd_speed_fast_sq<R, 0>(qr, gamma0)));
+  else
+    cmax = fmax(mhd_speed_fast<R, 0>(ql, gamma0), mhd_speed_fast<R, 0>(qr, gamma0));
+  const R sl = fmin(ul, ur) - cmax;
+  const R sr = fmax(ul, ur) + cmax;
   const R rcl = rl * (ul - sl);
   const R rcr = rr * (sr - ur);
   // FP64 FMA build: one reciprocal per shared denominator (kShareRecip)
@@ -638,13 +659,15 @@ mag_riemann2d_hlld_f32(const EdgeQ<float> & LL, const EdgeQ<float> & RL, const E
                        const EdgeQ<float> & RR, float ELL, float ERL, float ELR, float ERR, float gamma0,
                        float smallc)
 {
+  // squares of the fast speeds along x and y (before the outer square root:
+  // one square root of the largest of the four corners', below)
   auto fast2 = [gamma0](const EdgeQ<float> & q, float & cx, float & cy) {
     const float ir = rcp_a(q.r);
     const float c2 = gamma0 * q.p * ir;
     const float d2 = 0.5f * ((q.a * q.a + q.b * q.b + q.c * q.c) * ir + c2);
     const float dd = d2 * d2, cr = c2 * ir;
-    cx = sqrt_a(d2 + sqrt_a(dd - cr * q.a * q.a));
-    cy = sqrt_a(d2 + sqrt_a(dd - cr * q.b * q.b));
+    cx = d2 + sqrt_a(dd - cr * q.a * q.a);
+    cy = d2 + sqrt_a(dd - cr * q.b * q.b);
   };
   const float rLL = LL.r, pLL = LL.p, uLL = LL.u, vLL = LL.v, aLL = LL.a, bLL = LL.b, cLL = LL.c;
   const float rLR = LR.r, pLR = LR.p, uLR = LR.u, vLR = LR.v, aLR = LR.a, bLR = LR.b, cLR = LR.c;
@@ -655,7 +678,7 @@ mag_riemann2d_hlld_f32(const EdgeQ<float> & LL, const EdgeQ<float> & RL, const E
   fast2(LR, cLRx, cLRy);
   fast2(RL, cRLx, cRLy);
   fast2(RR, cRRx, cRRy);
-  const float cmx = fmax4(cLLx, cLRx, cRLx, cRRx), cmy = fmax4(cLLy, cLRy, cRLy, cRRy);
+  const float cmx = sqrt_a(fmax4(cLLx, cLRx, cRLx, cRRx)), cmy = sqrt_a(fmax4(cLLy, cLRy, cRLy, cRRy));
   const float SL = fmin4(uLL, uLR, uRL, uRR) - cmx;
   const float SR = fmax4(uLL, uLR, uRL, uRR) + cmx;
   const float SB = fmin4(vLL, vLR, vRL, vRR) - cmy;
@@ -756,6 +779,9 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
     return mag_riemann2d_hlld_f32(LL, RL, LR, RR, ELL, ERL, ELR, ERR, gamma0, smallc);
   else
   {
+  // fast speed of a corner state along x or y; the FP64 FMA build returns its
+  // square (before the outer square root, see mhd_speed_fast_sq) and takes one
+  // square root of the largest
   auto fast = [gamma0](const EdgeQ<R> & q, bool ydir) {
     const R b2 = q.a * q.a + q.b * q.b + q.c * q.c;
     const R bn = ydir ? q.b : q.a;
@@ -764,7 +790,7 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
       const R ir = R(1) / q.r;
       const R c2 = gamma0 * q.p * ir;
       const R d2 = R(0.5) * (b2 * ir + c2);
-      return sqrt(d2 + sqrt(d2 * d2 - c2 * bn * bn * ir));
+      return d2 + sqrt(d2 * d2 - c2 * bn * bn * ir);
     }
     const R c2 = gamma0 * q.p / q.r;
     const R d2 = R(0.5) * (b2 / q.r + c2);
@@ -780,10 +806,13 @@ mag_riemann2d_hlld(const EdgeQ<R> & LL, const EdgeQ<R> & RL, const EdgeQ<R> & LR
   const R cFastLLy = fast(LL, true), cFastLRy = fast(LR, true);
   const R cFastRLy = fast(RL, true), cFastRRy = fast(RR, true);
 
-  const R SL = fmin4(uLL, uLR, uRL, uRR) - fmax4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
-  const R SR = fmax4(uLL, uLR, uRL, uRR) + fmax4(cFastLLx, cFastLRx, cFastRLx, cFastRRx);
-  const R SB = fmin4(vLL, vLR, vRL, vRR) - fmax4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
-  const R ST = fmax4(vLL, vLR, vRL, vRR) + fmax4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
+  R cmx = fmax4(cFastLLx, cFastLRx, cFastRLx, cFastRRx), cmy = fmax4(cFastLLy, cFastLRy, cFastRLy, cFastRRy);
+  if constexpr (kShareRecip)
+    cmx = sqrt(cmx), cmy = sqrt(cmy);
+  const R SL = fmin4(uLL, uLR, uRL, uRR) - cmx;
+  const R SR = fmax4(uLL, uLR, uRL, uRR) + cmx;
+  const R SB = fmin4(vLL, vLR, vRL, vRR) - cmy;
+  const R ST = fmax4(vLL, vLR, vRL, vRR) + cmy;
 
   const R PtotLL = pLL + R(0.5) * (aLL * aLL + bLL * bLL + cLL * cLL);
   const R PtotLR = pLR + R(0.5) * (aLR * aLR + bLR * bLR + cLR * cLR);
