@@ -1263,12 +1263,20 @@ mhd_trace_of(void * work, const KParams & P)
 {
   return reinterpret_cast<R *>(static_cast<char *>(work) + (sizeof(R) == 8 ? 0 : mhd_repair_bytes(P)));
 }
-// blocks of a repair launch: one per SM (most steps list no tile)
+// blocks of a repair launch: one per SM (most steps list no tile); the SM
+// count of each device is looked up once
 inline int
 repair_grid(long long tiles)
 {
-  int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+  static int sms_of[64] = {};
+  int        dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64)
+  {
+    sms = __atomic_load_n(&sms_of[dev], __ATOMIC_RELAXED);
+    if (sms == 0 && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+      __atomic_store_n(&sms_of[dev], sms, __ATOMIC_RELAXED);
+  }
+  if (sms <= 0)
     sms = 1;
   return (int)(tiles < sms ? (tiles > 0 ? tiles : 1) : sms);
 }
