@@ -352,12 +352,18 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
                                  : (rcr * ptotl + rcl * ptotr + rcl * rcr * (ul - ur)) / (rcr + rcl);
 
   R estar;
+  // the degenerate-state test divides both sides' estar by a^2: one
+  // reciprocal in the FP64 FMA build
+  const R ia2 = kShareRecip ? R(1) / (a * a) : R(0);
+  auto    degenerate = [&](R e) {
+    return a * a > R(0) && fabs((kShareRecip ? e * ia2 : e / (a * a)) - R(1)) <= R(1e-8);
+  };
   const R isl = kShareRecip ? R(1) / (sl - ustar) : R(0);
   const R rstarl = kShareRecip ? rl * (sl - ul) * isl : rl * (sl - ul) / (sl - ustar);
   estar = rl * (sl - ul) * (sl - ustar) - a * a;
   const R el = rl * (sl - ul) * (sl - ul) - a * a;
   R       vstarl, wstarl, bstarl, cstarl;
-  if (a * a > R(0) && fabs(estar / (a * a) - R(1)) <= R(1e-8))
+  if (degenerate(estar))
   {
     vstarl = vl;
     bstarl = bl;
@@ -383,8 +389,11 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   const R etotstarl =
     kShareRecip ? ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) * isl
                 : ((sl - ul) * etotl - ptotl * ul + ptotstar * ustar + a * (vdotbl - vdotbstarl)) / (sl - ustar);
-  const R sqrrstarl = sqrt(rstarl);
-  const R calfvenl = fabs(a) / sqrrstarl;
+  // sqrt(rho*) and |a| / sqrt(rho*): one reciprocal square root in the FP64
+  // FMA build
+  const R rsl = kShareRecip ? rsqrt(rstarl) : R(0);
+  const R sqrrstarl = kShareRecip ? rstarl * rsl : sqrt(rstarl);
+  const R calfvenl = kShareRecip ? fabs(a) * rsl : fabs(a) / sqrrstarl;
   const R sal = ustar - calfvenl;
 
   const R isr = kShareRecip ? R(1) / (sr - ustar) : R(0);
@@ -392,7 +401,7 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   estar = rr * (sr - ur) * (sr - ustar) - a * a;
   const R er = rr * (sr - ur) * (sr - ur) - a * a;
   R       vstarr, wstarr, bstarr, cstarr;
-  if (a * a > R(0) && fabs(estar / (a * a) - R(1)) <= R(1e-8))
+  if (degenerate(estar))
   {
     vstarr = vr;
     bstarr = br;
@@ -418,8 +427,9 @@ mhd_hlld(R (&ql)[8], R (&qr)[8], R (&flux)[NF], R gamma0)
   const R etotstarr =
     kShareRecip ? ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) * isr
                 : ((sr - ur) * etotr - ptotr * ur + ptotstar * ustar + a * (vdotbr - vdotbstarr)) / (sr - ustar);
-  const R sqrrstarr = sqrt(rstarr);
-  const R calfvenr = fabs(a) / sqrrstarr;
+  const R rsr = kShareRecip ? rsqrt(rstarr) : R(0);
+  const R sqrrstarr = kShareRecip ? rstarr * rsr : sqrt(rstarr);
+  const R calfvenr = kShareRecip ? fabs(a) * rsr : fabs(a) / sqrrstarr;
   const R sar = ustar + calfvenr;
 
   R ro, uo, vo, wo, bo, co, ptoto, etoto, vdotbo;
