@@ -719,9 +719,10 @@ struct UpdTile
   }
 };
 
-// The tile list of the HLLD repair pass, at the end of the mixed form's work
-// buffer: [0] tiles listed this step, [1] repair blocks done, [2..3] tiles
-// repaired since the buffer was cleared (64-bit), [4..] the tile indices.
+// The tile list of the HLLD repair pass, at the start of the mixed form's
+// work buffer (the trace follows): [0] tiles listed this step, [1] repair
+// blocks done, [2..3] tiles repaired since the list was cleared (64-bit),
+// [4..] the tile indices.
 constexpr int kRepairHead = 4;
 __host__ __device__ inline long long
 repair_tiles(const KParams & P, int TX, int TY)
