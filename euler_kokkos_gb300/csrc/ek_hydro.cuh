@@ -38,22 +38,27 @@ slope1(R q, R qp, R qm, R st)
       m = fminf(m, fabsf(0.5f * (qp - qm)));
     return (dl * dr > 0.f) ? copysignf(m, dl) : 0.f;
   }
-  const R dlft = st * (q - qm);
-  const R drgt = st * (qp - q);
-  const R dcen = R(0.5) * (qp - qm);
   if constexpr (kShareRecip)
   {
     // FP64 FMA build: the minima of non-negative values as integer minima of
     // their bit patterns (same order; a NaN pattern is the larger, as fmin
     // drops NaN) and the sign by copysign, on the integer pipes instead of
-    // GB300's 1/64-rate FP64 pipe; only the sign of a zero slope can differ
+    // GB300's 1/64-rate FP64 pipe.  As in the FP32 form, the scaling by st
+    // (0, 1 or 2) is applied once to the minimum, and the centred difference
+    // only where it can bind (st = 2); a non-zero slope has dl's sign (dl, dr
+    // and dcen share it).  Only the sign of a zero slope can differ.
     auto minpos = [](double a, double b) {
       return __longlong_as_double(min(__double_as_longlong(a), __double_as_longlong(b)));
     };
-    const R slop = minpos(fabs(dlft), fabs(drgt));
-    const R dlim = ((dlft * drgt) <= R(0)) ? R(0) : slop;
-    return copysign(minpos(dlim, fabs(dcen)), dcen);
+    const R dl = q - qm, dr = qp - q;
+    R       m = minpos(fabs(dl), fabs(dr));
+    if (st != R(1))
+      m = minpos(st * m, fabs(R(0.5) * (qp - qm)));
+    return copysign((dl * dr <= R(0)) ? R(0) : m, dl);
   }
+  const R dlft = st * (q - qm);
+  const R drgt = st * (qp - q);
+  const R dcen = R(0.5) * (qp - qm);
   const R dsgn = (dcen >= R(0)) ? R(1) : R(-1);
   const R slop = fmin(fabs(dlft), fabs(drgt));
   R       dlim = slop;
