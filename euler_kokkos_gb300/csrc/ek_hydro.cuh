@@ -248,15 +248,18 @@ hllc(const R (&ql)[NV], const R (&qr)[NV], R (&flux)[NV], const HydroConst<R> & 
       ecinr += R(0.5) * rr * qr[IW] * qr[IW];
     etotr = pr * entho + ecinr;
 
-    const R c2l = fmax(C.gamma0 * pl / rl, C.smallc * C.smallc);
-    const R c2r = fmax(C.gamma0 * pr / rr, C.smallc * C.smallc);
-    // a correctly rounded square root is monotonic: the FP64 FMA build takes
-    // one square root of the larger square, the same bits as the larger of
-    // the two square roots the reference takes
     if constexpr (kShareRecip)
-      cmax = sqrt(fmax(c2l, c2r));
+    {
+      // FP64 FMA build: the larger sound speed squared with one division (the
+      // densities are positive, so p_l / rho_l >= p_r / rho_r where p_l rho_r
+      // >= p_r rho_l, up to rounding ties), then one square root (a correctly
+      // rounded square root is monotonic)
+      const bool lbig = pl * rr >= pr * rl;
+      cmax = sqrt(fmax(C.gamma0 * (lbig ? pl : pr) / (lbig ? rl : rr), C.smallc * C.smallc));
+    }
     else
-      cmax = fmax(sqrt(c2l), sqrt(c2r));
+      cmax = fmax(sqrt(fmax(C.gamma0 * pl / rl, C.smallc * C.smallc)),
+                  sqrt(fmax(C.gamma0 * pr / rr, C.smallc * C.smallc)));
   }
   const R ptotl = pl, ptotr = pr;
 
