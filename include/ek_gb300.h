@@ -48,7 +48,8 @@ typedef enum ek_layout
 typedef enum ek_precision
 {
   EK_PREC_FP64 = 0, /* the drop-in: FP64 state and arithmetic */
-  EK_PREC_MIXED = 1 /* FP32 state/arithmetic with FP64 islands (dt, CT face B, cancellation) */
+  EK_PREC_MIXED = 1 /* FP32 state/arithmetic with FP64 islands (dt, CT face B, cancellation,
+                       ill-conditioned HLLD star states: ek_solver_hlld_repairs) */
 } ek_precision;
 
 /* Run parameters.  Field meanings and defaults follow HydroParams
