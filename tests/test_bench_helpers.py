@@ -47,3 +47,16 @@ def test_divb_inner_matches_direct_computation():
     bscale = np.abs(U0[5:]).max() / p.dx
     assert bench.divb_inner(U, p.gw, 1, p.dx, p.dy, p.dz) <= 1e-12 * bscale
     assert bench.divb_inner(U, p.gw, 0, p.dx, p.dy, p.dz) > 1e-6 * bscale
+
+
+def test_headline_traffic_covers_every_kernel_of_the_step():
+    # the headline's whole-step roofline sums traffic per cell over the
+    # step's kernels (ncu figures in bench.TRAFFIC_PER_CELL); a kernel
+    # without an entry would leave the JSON line's `traffic` null
+    names = [name for _, name in bench.KERNEL_NAMES["mhd3d"]]
+    traffic = bench.TRAFFIC_PER_CELL[("mhd3d", "mixed")]
+    assert "mhd_repair_kernel" in names
+    assert all(name in traffic for name in names), (names, sorted(traffic))
+    # and the kernel ids are distinct (ek_solver_kernel_time slots)
+    ids = [i for i, _ in bench.KERNEL_NAMES["mhd3d"]]
+    assert len(set(ids)) == len(ids) and all(0 <= i <= 3 for i in ids)
